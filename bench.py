@@ -1,0 +1,412 @@
+#!/usr/bin/env python
+"""Soft-force benchmark: tree-force Ginteractions/s at N = 1M.
+
+Workload (default ``plummer1m_bin50``): Plummer sphere of 1,048,576 centres of
+mass with 50% primordial binaries (1,572,864 particles), Kroupa IMF, Henon
+units, theta = 0.3, quadrupole superparticles, n_leaf_limit 20,
+n_group_limit 512, r_out = 0.003, r_in = 0.1 r_out, r_search = 1.5 r_out,
+eps = 0.  Interaction lists come from the package's interaction-list builder
+(the FDPS stand-in).  One step = one multi-walk force evaluation over all
+walks.
+
+Reported (one JSON line from rank 0):
+* value: Ginteractions/s of the mixed-precision kernels on device-resident
+  lists (sum over ranks / max rank time), with the L2 flushed between steps;
+* fp64_plain: the same for the plain FP64 kernel, and the speed-up;
+* accuracy: mixed vs FP64 kernel on every particle (relative force and
+  potential error; neighbour-count mismatches);
+* e2e: the same metric through the C ABI with host records (pack, copies,
+  kernels, copy back, unpack) per step;
+* roofline: FP32 flops (19 per EP-EP, 54 per EP-SP interaction) of the main
+  kernel per launch over its event-timed duration, against an FP32 FMA peak
+  measured in the same run;
+* cpu_baseline: the FP64 oracle (a CPU port of the reference functors) on a
+  sample of the walks, with every host thread.
+
+``--impl reference`` times the reference's own CPU path instead (the
+reference functors compiled from its sources when they are present on this
+host, else the oracle port) and prints the same metric with impl=reference.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    "plummer1m_bin50": dict(seed=3, n_cm=1048576, r_out=0.003, binary_fraction=0.5, theta=0.3),
+    "plummer65k": dict(seed=2, n_cm=65536, r_out=0.008, binary_fraction=0.0, theta=0.3),
+    "plummer2k": dict(seed=1, n_cm=2048, r_out=0.02, binary_fraction=0.0, theta=0.3),
+}
+FLOPS_EPEP = 19
+FLOPS_EPSP = 54
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def make_workload(name: str, rank: int):
+    from petar_gb300 import ics, walks
+    w = WORKLOADS[name]
+    t = time.time()
+    cl = ics.make_plummer_cluster(w["seed"] + 1000 * rank, w["n_cm"], w["r_out"],
+                                  binary_fraction=w["binary_fraction"], theta=w["theta"])
+    wb = walks.build_walks(cl)
+    log(f"[rank {rank}] workload {name}: {cl.n} particles, {wb.n_walk} walks, built in {time.time() - t:.1f}s")
+    return cl, wb
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = [l.split(",") for l in Path(self.file.name).read_text().splitlines() if l.strip()]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.file.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp32_peak_tflops() -> float | None:
+    import ctypes
+    from petar_gb300.build import build_probe
+    lib = ctypes.CDLL(str(build_probe()))
+    lib.pgf_probe_fp32_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    best = None
+    for _ in range(3):
+        tf, ms = ctypes.c_double(), ctypes.c_double()
+        if lib.pgf_probe_fp32_peak(20000, ctypes.byref(tf), ctypes.byref(ms)) == 0:
+            best = tf.value if best is None else max(best, tf.value)
+    return best
+
+
+def traffic_from_profiles() -> float | None:
+    """DRAM bytes per launch of the main kernel from the committed ncu summary
+    (a line 'dram_bytes_per_launch_scaled: <bytes>'), or None."""
+    p = ROOT / "profiles" / "mixed_kernel_plummer1m_bin50.md"
+    if not p.exists():
+        return None
+    m = re.search(r"dram_bytes_per_launch_scaled:\s*([0-9.eE+]+)", p.read_text())
+    return float(m.group(1)) if m else None
+
+
+def sample_walks(wb, target_interactions: float, seed: int = 7) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(wb.n_walk)
+    per = wb.n_epi.astype(np.int64) * (wb.n_epj + wb.n_spj)
+    cum = np.cumsum(per[order])
+    k = int(np.searchsorted(cum, target_interactions)) + 1
+    return np.sort(order[:max(1, min(k, wb.n_walk))])
+
+
+def cpu_reference_runner():
+    """The reference's own FP64 functors when compiled on this host
+    (oracle/_ref), else the oracle port.  Returns (kind, run(batch))."""
+    import ctypes
+    from concurrent.futures import ThreadPoolExecutor
+    import oracle
+    ref = ROOT / "oracle" / "_ref" / "libref_nosimd.so"
+    lib = None
+    if ref.exists():
+        try:
+            lib = ctypes.CDLL(str(ref))
+        except OSError:
+            lib = None
+    if lib is None:
+        return "port", lambda b: oracle.force(b)
+    vp, ci, cd = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    lib.ref_set_params.argtypes = [cd, cd, cd]
+    lib.ref_epep.argtypes = [ci, vp, vp, ci, vp, vp, vp, vp, vp, vp]
+    lib.ref_epsp.argtypes = [ci, vp, ci, vp, vp, vp, vp, vp]
+
+    def run(b):
+        lib.ref_set_params(float(np.sqrt(b.eps2)), float(np.sqrt(b.rcut2)), float(b.G))
+
+        def one(w):
+            i0, i1 = b.epi_disp[w], b.epi_disp[w + 1]
+            ni = int(i1 - i0)
+            je = b.id_epj[b.epj_disp[w]:b.epj_disp[w + 1]]
+            js = b.id_spj[b.spj_disp[w]:b.spj_disp[w + 1]]
+            xi = np.ascontiguousarray(b.epi_pos[i0:i1])
+            rsi = np.ascontiguousarray(b.epi_rs[i0:i1])
+            xj, mj, rsj = (np.ascontiguousarray(a[je]) for a in (b.epj_pos, b.epj_mass, b.epj_rs))
+            xs, ms, qs = (np.ascontiguousarray(a[js]) for a in (b.spj_pos, b.spj_mass, b.spj_quad))
+            a = np.zeros((ni, 3)); p = np.zeros(ni); n = np.zeros(ni, np.int64)
+            lib.ref_epep(ni, xi.ctypes.data, rsi.ctypes.data, je.size, xj.ctypes.data, mj.ctypes.data,
+                         rsj.ctypes.data, a.ctypes.data, p.ctypes.data, n.ctypes.data)
+            a2 = np.zeros((ni, 3)); p2 = np.zeros(ni)
+            if js.size:
+                lib.ref_epsp(ni, xi.ctypes.data, js.size, xs.ctypes.data, ms.ctypes.data, qs.ctypes.data,
+                             a2.ctypes.data, p2.ctypes.data)
+            return a + a2
+
+        with ThreadPoolExecutor(max_workers=os.cpu_count()) as ex:
+            list(ex.map(one, range(b.n_walk)))
+
+    return "reference", run
+
+
+def time_cpu(wb, seconds: float) -> tuple[str, dict, callable]:
+    """Chooses a sample of walks worth about `seconds` of CPU work."""
+    kind, run = cpu_reference_runner()
+    calib = wb.subset(sample_walks(wb, 2e8, seed=11))
+    t = time.time()
+    run(calib)
+    rate = sum(calib.interactions()) / max(time.time() - t, 1e-3)
+    sub = wb.subset(sample_walks(wb, rate * seconds))
+    n_int = sum(sub.interactions())
+    desc = (f"{sub.n_walk} of {wb.n_walk} walks chosen at random (seed 7), {n_int:.3e} of "
+            f"{sum(wb.interactions()):.3e} interactions")
+    return kind, dict(batch=sub, n_int=n_int, desc=desc), run
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    _, wb = make_workload(args.workload, 0)
+    kind, s, run = time_cpu(wb, args.cpu_seconds)
+    for _ in range(args.warmup):
+        run(s["batch"])
+    ts = []
+    for _ in range(args.steps):
+        t = time.time()
+        run(s["batch"])
+        ts.append(time.time() - t)
+    v = s["n_int"] / statistics.mean(ts) / 1e9
+    out = {"metric": "tree-force Ginteractions/s at N=1M", "impl": "reference", "value": v,
+           "unit": "Ginteractions/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * statistics.mean(ts), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": args.workload, "sample": s["desc"]},
+           "cpu_baseline": {"value": v, "unit": "Ginteractions/s", "cores": os.cpu_count(), "kind": kind,
+                            "sample": s["desc"]},
+           "e2e": {"value": v, "unit": "Ginteractions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    from petar_gb300 import gpuforce
+    from petar_gb300.gpuforce import PGF_PRECISION_FP64, PGF_PRECISION_MIXED
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    cl, wb = make_workload(args.workload, rank)
+    n_epep, n_epsp = wb.interactions()
+    n_int = n_epep + n_epsp
+    flops = FLOPS_EPEP * n_epep + FLOPS_EPSP * n_epsp
+    rec = gpuforce.Records(wb)
+    stream = torch.cuda.current_stream()
+    gpuforce.CalcForceWithLinearCutoffCUDAMultiWalk(local, wb.eps2, wb.rcut2, wb.G)
+    gpuforce.set_stream(stream.cuda_stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+
+    # ---- device-resident mixed-precision steps ----
+    gpuforce.set_precision(PGF_PRECISION_MIXED)
+    gpuforce.dispatch(rec, tag=0)
+    f_mixed = gpuforce.retrieve(rec, tag=0).copy()
+    for _ in range(args.warmup):
+        flush.zero_()
+        gpuforce.recompute(0)
+        gpuforce.wait(0)
+    gpuforce.clear_profile()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    main_ms = []
+    barrier()
+    wall0 = time.time()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for e0, e1 in evs:
+            flush.zero_()
+            e0.record(stream)
+            gpuforce.recompute(0)
+            e1.record(stream)
+            gpuforce.wait(0)
+            main_ms.append(1e3 * gpuforce.get_profile()["last_calc_main"])
+        barrier()
+    wall = time.time() - wall0
+    prof = gpuforce.get_profile()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    t_total = max_over_ranks(sum(step_ms) / 1e3)
+    value = world * n_int * args.steps / t_total / 1e9
+    clocks = clk.summary()
+    n_retest = prof["n_retest"] / max(1, prof["n_call"] or args.steps)
+
+    # ---- plain FP64 kernel on the same lists ----
+    fp64 = None
+    if not args.no_fp64:
+        gpuforce.set_precision(PGF_PRECISION_FP64)
+        gpuforce.recompute(0)
+        f64 = gpuforce.retrieve(rec, tag=0).copy()
+        ts = []
+        for _ in range(max(1, min(2, args.steps))):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            gpuforce.recompute(0)
+            e1.record(stream)
+            gpuforce.wait(0)
+            ts.append(e0.elapsed_time(e1))
+        t64 = max_over_ranks(statistics.mean(ts) / 1e3)
+        v64 = world * n_int / t64 / 1e9
+        ea = np.linalg.norm(f_mixed["acc"] - f64["acc"], axis=1) / np.linalg.norm(f64["acc"], axis=1)
+        ep = np.abs(f_mixed["pot"] - f64["pot"]) / np.abs(f64["pot"])
+        fp64 = {"value": v64, "unit": "Ginteractions/s", "ms_per_step": 1e3 * t64, "speedup_mixed_vs_fp64": value / v64,
+                "accuracy_mixed_vs_fp64": {
+                    "force_rel_err_median": float(np.median(ea)), "force_rel_err_p999": float(np.quantile(ea, 0.999)),
+                    "pot_rel_err_median": float(np.median(ep)), "pot_rel_err_p999": float(np.quantile(ep, 0.999)),
+                    "n_ngb_mismatches": int((f_mixed["n_ngb"] != f64["n_ngb"]).sum())}}
+        gpuforce.set_precision(PGF_PRECISION_MIXED)
+
+    # ---- end to end through the C ABI with host records ----
+    ni, ne, ns = wb.epi_rs.size, wb.id_epj.size, wb.id_spj.size
+    h2d = (wb.epj_mass.size * (32 + 8 + 4) + wb.spj_mass.size * 80 + ni * 32 + (ne + ns) * 4 + wb.n_walk * (64 + 4))
+    d2h = ni * (32 + 4) + 12
+    e2e_t = []
+    for k in range(args.warmup + args.steps):
+        barrier()
+        t = time.time()
+        gpuforce.dispatch(rec, tag=0, send=True)
+        gpuforce.retrieve(rec, tag=0)
+        if k >= args.warmup:
+            e2e_t.append(time.time() - t)
+    e2e_total = max_over_ranks(sum(e2e_t))
+    e2e = {"value": world * n_int * args.steps / e2e_total / 1e9, "unit": "Ginteractions/s",
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+           "ms_per_step": 1e3 * e2e_total / args.steps}
+
+    if rank != 0:
+        torch.distributed.barrier()
+        return
+
+    # ---- roofline of the main kernel ----
+    peak = fp32_peak_tflops()
+    main_s = statistics.mean(main_ms) / 1e3
+    achieved = flops / main_s / 1e12
+    roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak if peak else None, "traffic": traffic_from_profiles(),
+            "peak_source": "FP32 FMA loop measured in this run (MEASURED_PEAKS.json has no FP32 figure)",
+            "flops_per_launch": flops, "kernel": "mixed_kernel", "launch_ms": 1e3 * main_s,
+            "flop_model": "19 per EP-EP, 54 per EP-SP interaction"}
+
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        kind, s, run = time_cpu(wb, args.cpu_seconds)
+        t = time.time()
+        run(s["batch"])
+        dt = time.time() - t
+        cpu = {"value": s["n_int"] / dt / 1e9, "unit": "Ginteractions/s", "cores": os.cpu_count(),
+               "kind": kind, "sample": s["desc"], "seconds": dt}
+
+    out = {
+        "metric": "tree-force Ginteractions/s at N=1M", "value": value, "unit": "Ginteractions/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "n_particles": int(cl.n), "n_walk": int(wb.n_walk),
+                   "interactions_epep": n_epep, "interactions_epsp": n_epsp, "theta": WORKLOADS[args.workload]["theta"],
+                   "r_out": WORKLOADS[args.workload]["r_out"], "l2": "flushed between steps (256 MB write)",
+                   "replica_per_rank": True},
+        "gpu_launches": 2 * args.steps,
+        "fp64_plain": fp64, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+        "retest_records_per_step": n_retest, "wall_s_timed_region": wall,
+    }
+    print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="plummer1m_bin50")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        log("note: fewer than 3 warm-up steps")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        from petar_gb300.build import build_all
+        build_all()
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,165 @@
+/* C ABI of the GB300 soft-force kernels for PeTar.
+ *
+ * These entry points replace PeTar's CUDA soft-force functor pair:
+ *   CalcForceWithLinearCutoffCUDAMultiWalk  src/force_gpu_cuda.hpp:103-133,
+ *                                           src/force_gpu_cuda.cu:535-700
+ *   CalcForceWithLinearCutoffCUDA           src/force_gpu_cuda.hpp:137-162,
+ *                                           src/force_gpu_cuda.cu:704-827
+ *   RetrieveForceCUDA                       src/force_gpu_cuda.hpp:165-168,
+ *                                           src/force_gpu_cuda.cu:831-880
+ * and their profiling counters (GPUProfile / GPUCounter,
+ * src/force_gpu_cuda.hpp:6-93).
+ *
+ * Particle arrays are passed as the caller's own records (FDPS's EPISoft,
+ * EPJSoft, SPJSoft and ForceSoft in PeTar) together with a layout that gives
+ * the record size and the byte offsets of the fields the kernels read or
+ * write.  Positions are three consecutive doubles (FDPS F64vec), the
+ * quadrupole is six consecutive doubles in FDPS MatrixSym order
+ * (xx, yy, zz, xy, xz, yz).  The header include/petar_gpuforce.hpp wraps these
+ * calls in functors with the reference signatures.
+ *
+ * All functions return PGF_OK (0) or a PGF_ERR_* code; pgf_last_error() gives
+ * a message for the last failure.  The reference returned 0 and asserted; the
+ * C++ wrapper keeps that by aborting on a non-zero code.
+ *
+ * Threading: like the reference, one process drives one device through
+ * file-scope state; calls are not re-entrant.
+ */
+#ifndef PETAR_GPUFORCE_H
+#define PETAR_GPUFORCE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    PGF_OK = 0,
+    PGF_ERR_ARG = 1,        /* invalid argument (null pointer, negative size, bad tag) */
+    PGF_ERR_NO_DEVICE = 2,  /* no CUDA device visible */
+    PGF_ERR_CUDA = 3,       /* a CUDA runtime call failed */
+    PGF_ERR_STATE = 4,      /* call out of sequence (e.g. retrieve without dispatch) */
+    PGF_ERR_CAPACITY = 5,   /* a size exceeds what the kernels index (2^31-1 rows) */
+    PGF_ERR_DEVICE = 6      /* the kernels reported an error flag (bounded wait expired) */
+};
+
+/* Kernel selection for pgf_set_precision. */
+enum {
+    PGF_PRECISION_MIXED = 0, /* FP64 walk-relative coordinates, FP32 pair arithmetic,
+                                FP64 cross-tile sums, exact neighbour counts (default) */
+    PGF_PRECISION_FP64 = 1   /* plain FP64 throughout */
+};
+
+/* Record layouts (sizes and byte offsets). */
+typedef struct pgf_epi_layout {
+    size_t size;         /* sizeof(EPISoft) */
+    size_t off_pos;      /* F64vec pos */
+    size_t off_r_search; /* F64 r_search */
+} pgf_epi_layout;
+
+typedef struct pgf_epj_layout {
+    size_t size;         /* sizeof(EPJSoft) */
+    size_t off_mass;     /* F64 mass */
+    size_t off_pos;      /* F64vec pos */
+    size_t off_r_search; /* F64 r_search */
+} pgf_epj_layout;
+
+typedef struct pgf_spj_layout {
+    size_t size;         /* sizeof(SPJSoft) */
+    size_t off_mass;     /* F64 mass */
+    size_t off_pos;      /* F64vec pos */
+    size_t off_quad;     /* F64mat quad (xx, yy, zz, xy, xz, yz); ignored when has_quad == 0 */
+    int has_quad;        /* 0: monopole superparticles (SPJMonopoleInAndOut) */
+} pgf_spj_layout;
+
+typedef struct pgf_force_layout {
+    size_t size;         /* sizeof(ForceSoft) */
+    size_t off_acc;      /* F64vec acc (overwritten) */
+    size_t off_pot;      /* F64 pot (overwritten) */
+    size_t off_n_ngb;    /* integer n_ngb (overwritten) */
+    int n_ngb_bytes;     /* 4 or 8 */
+} pgf_force_layout;
+
+/* Timings (seconds, accumulated since the last pgf_clear_profile) and
+ * counters, mirroring GPUProfile / GPUCounter (src/force_gpu_cuda.hpp:6-93). */
+typedef struct pgf_profile {
+    double copy;         /* host packing and unpacking */
+    double send;         /* host-to-device copies */
+    double recv;         /* device-to-host copies */
+    double calc;         /* kernels, all of them */
+    double calc_main;    /* the interaction kernel alone */
+    double last_calc;    /* kernels of the most recent dispatch */
+    double last_calc_main;
+    int64_t n_walk, n_epi, n_epj, n_spj, n_call;
+    int64_t n_retest;    /* pair ranges re-tested in FP64 for exact neighbour counts */
+} pgf_profile;
+
+/* CalcForceWithLinearCutoffCUDAMultiWalk constructor / initialize()
+ * (src/force_gpu_cuda.hpp:109-118).  Selects device rank % device_count on
+ * the first call, as src/force_gpu_cuda.cu:549-553 does. */
+int pgf_initialize(int rank, double eps2, double rcut2, double G);
+
+/* Chooses the kernel used by later dispatches (PGF_PRECISION_*). */
+int pgf_set_precision(int precision);
+
+/* Launch on the caller's CUDA stream (a cudaStream_t passed as void*);
+ * NULL restores the library's own stream. */
+int pgf_set_stream(void *cuda_stream);
+
+/* CalcForceWithLinearCutoffCUDAMultiWalk::operator()
+ * (src/force_gpu_cuda.hpp:120-132, src/force_gpu_cuda.cu:535-700).
+ * send_flag != 0: copies the shared EPJ/SPJ arrays to the device and returns.
+ * send_flag == 0: packs the walks' EPI and id lists, copies them and launches
+ * the kernels for all n_walk walks; returns without waiting for the kernels.
+ * Unused arguments may be NULL for each phase. */
+int pgf_dispatch_index(int tag, int n_walk,
+                       const void *const *epi, const int *n_epi, const pgf_epi_layout *epi_layout,
+                       const int *const *id_epj, const int *n_epj,
+                       const int *const *id_spj, const int *n_spj,
+                       const void *epj, int n_epj_tot, const pgf_epj_layout *epj_layout,
+                       const void *spj, int n_spj_tot, const pgf_spj_layout *spj_layout,
+                       int send_flag);
+
+/* CalcForceWithLinearCutoffCUDA::operator() (src/force_gpu_cuda.hpp:154-161,
+ * src/force_gpu_cuda.cu:704-827): per-walk EPJ/SPJ arrays, no id lists. */
+int pgf_dispatch(int tag, int n_walk,
+                 const void *const *epi, const int *n_epi, const pgf_epi_layout *epi_layout,
+                 const void *const *epj, const int *n_epj, const pgf_epj_layout *epj_layout,
+                 const void *const *spj, const int *n_spj, const pgf_spj_layout *spj_layout);
+
+/* RetrieveForceCUDA (src/force_gpu_cuda.hpp:165-168,
+ * src/force_gpu_cuda.cu:831-880): waits for the dispatch of this tag and
+ * overwrites acc, pot and n_ngb of force[w][0..ni[w]). */
+int pgf_retrieve(int tag, int n_walk, const int *ni, void *const *force,
+                 const pgf_force_layout *force_layout);
+
+/* Per-walk r_out^2 for the next index dispatch of independent clusters in one
+ * launch (NULL or n_walk == 0 clears it).  Extends the reference, whose r_out
+ * is one functor constant (src/petar.hpp:889-891). */
+int pgf_set_walk_rcut2(const double *walk_rcut2, int n_walk);
+
+/* Re-runs the kernels of the last index dispatch of this tag on the data
+ * already on the device (no host packing, no copies); returns immediately. */
+int pgf_recompute(int tag);
+
+/* Waits for the kernels of the tag's last dispatch or recompute and adds
+ * their times to the profile, without copying results back. */
+int pgf_wait(int tag);
+
+/* Profiling counters (GPUProfile / GPUCounter). */
+int pgf_get_profile(pgf_profile *out);
+int pgf_clear_profile(void);
+
+/* Message for the last failure ("" when none). */
+const char *pgf_last_error(void);
+
+/* Releases device and pinned host memory. */
+int pgf_finalize(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PETAR_GPUFORCE_H */

@@ -1,0 +1,101 @@
+"""FP64 CPU oracle for the soft-force path (test infrastructure only).
+
+Only tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this package; the product never does.  ``oracle.c``
+restates the reference's FP64 functors (src/soft_force.hpp:38-87, 160-200)
+with the GPU functor's neighbour test (src/force_gpu_cuda.cu:62-64).  Parity of
+this restatement is pinned against the reference's own functors through the
+fixtures in ``tests/golden`` (made by ``tests/golden/make_golden.py`` from
+libraries that ``oracle/ref/build_ref.sh`` compiles out of the reference
+sources).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+_LIB = None
+
+
+def build(force: bool = False) -> Path:
+    out = HERE / "liboracle.so"
+    src = HERE / "oracle.c"
+    if force or not out.exists() or out.stat().st_mtime < src.stat().st_mtime:
+        tmp = out.with_suffix(".so.tmp")
+        subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+                        "-fno-fast-math", str(src), "-o", str(tmp), "-lm"], check=True)
+        os.replace(tmp, out)
+    return out
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        lib = ctypes.CDLL(str(build()))
+        vp = ctypes.c_void_p
+        lib.oracle_force.restype = None
+        lib.oracle_force.argtypes = [ctypes.c_int64] + [vp] * 13 + [ctypes.c_double] * 3 + [vp, ctypes.c_int] + [vp] * 7
+        lib.oracle_nnb_global.restype = None
+        lib.oracle_nnb_global.argtypes = [ctypes.c_int64, vp, vp, ctypes.c_double, vp]
+        lib.oracle_direct.restype = None
+        lib.oracle_direct.argtypes = [ctypes.c_int64, vp, ctypes.c_int64, vp, vp] + [ctypes.c_double] * 3 + [vp, vp]
+        _LIB = lib
+    return _LIB
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def force(batch, nnb_with_eps: bool = True, parts: bool = False) -> dict:
+    """Oracle acc/pot/nnb for every EPI row of a WalkBatch (walk order)."""
+    lib = _lib()
+    ni = batch.epi_rs.size
+    arrs = dict(
+        epi_disp=_c(batch.epi_disp, np.int64), epi_pos=_c(batch.epi_pos, np.float64),
+        epi_rs=_c(batch.epi_rs, np.float64), epj_pos=_c(batch.epj_pos, np.float64),
+        epj_mass=_c(batch.epj_mass, np.float64), epj_rs=_c(batch.epj_rs, np.float64),
+        spj_pos=_c(batch.spj_pos, np.float64), spj_mass=_c(batch.spj_mass, np.float64),
+        spj_quad=_c(batch.spj_quad, np.float64), epj_disp=_c(batch.epj_disp, np.int64),
+        id_epj=_c(batch.id_epj, np.int32), spj_disp=_c(batch.spj_disp, np.int64),
+        id_spj=_c(batch.id_spj, np.int32))
+    wr = None if batch.walk_rcut2 is None else _c(batch.walk_rcut2, np.float64)
+    out = dict(acc=np.zeros((ni, 3)), pot=np.zeros(ni), nnb=np.zeros(ni, np.int64))
+    if parts:
+        out.update(acc_ep=np.zeros((ni, 3)), pot_ep=np.zeros(ni), acc_sp=np.zeros((ni, 3)),
+                   pot_sp=np.zeros(ni))
+    lib.oracle_force(batch.n_walk, *[_p(arrs[k]) for k in (
+        "epi_disp", "epi_pos", "epi_rs", "epj_pos", "epj_mass", "epj_rs", "spj_pos", "spj_mass",
+        "spj_quad", "epj_disp", "id_epj", "spj_disp", "id_spj")],
+        float(batch.eps2), float(batch.rcut2), float(batch.G), _p(wr), int(bool(nnb_with_eps)),
+        _p(out["acc"]), _p(out["pot"]), _p(out["nnb"]), _p(out.get("acc_ep")), _p(out.get("pot_ep")),
+        _p(out.get("acc_sp")), _p(out.get("pot_sp")))
+    return out
+
+
+def nnb_global(pos, rs, eps2: float = 0.0) -> np.ndarray:
+    pos = _c(pos, np.float64)
+    rs = _c(rs, np.float64)
+    out = np.zeros(rs.size, np.int64)
+    _lib().oracle_nnb_global(rs.size, _p(pos), _p(rs), float(eps2), _p(out))
+    return out
+
+
+def direct(pos, mass, targets, eps2: float, rcut2: float, G: float = 1.0):
+    pos = _c(pos, np.float64)
+    mass = _c(mass, np.float64)
+    t = _c(targets, np.int64)
+    acc = np.zeros((t.size, 3))
+    pot = np.zeros(t.size)
+    _lib().oracle_direct(t.size, _p(t), mass.size, _p(pos), _p(mass), float(eps2), float(rcut2),
+                         float(G), _p(acc), _p(pot))
+    return acc, pot

@@ -1,0 +1,186 @@
+/* FP64 CPU oracle for the long-range soft-force path.
+ *
+ * TEST INFRASTRUCTURE ONLY: tests, the smoke check and the CPU-baseline leg of
+ * the benchmark use this to check and time the GPU kernels.  Nothing in the
+ * product links or calls it.
+ *
+ * It restates, per interaction list, the reference's FP64 functors:
+ *   EP-EP linear cutoff + neighbour count: src/soft_force.hpp:38-87
+ *     (CalcForceEpEpWithLinearCutoffNoSimd)
+ *   EP-SP quadrupole:                      src/soft_force.hpp:160-200
+ *     (CalcForceEpSpQuadNoSimd)
+ * with the neighbour test of the GPU functor it replaces,
+ * src/force_gpu_cuda.cu:62-64: r2 + eps2 < max(rs_i, rs_j)^2 (self included,
+ * no mass or type filtering).  nnb_with_eps = 0 selects the NoSimd form
+ * r2 < max(rs_i, rs_j)^2 instead; the two agree when eps = 0.
+ *
+ * Every expression keeps the reference's evaluation order and is compiled
+ * with -ffp-contract=off so results do not depend on the host's FMA support.
+ * Parity is pinned against the reference's own functors, compiled from the
+ * reference sources by oracle/ref/build_ref.sh, through the golden fixtures in
+ * tests/golden/.
+ */
+#include <math.h>
+#include <stdint.h>
+
+static inline double dmax(double a, double b) { return a > b ? a : b; }
+
+/* One walk's EP-EP sum for i-particle (xi, rsi) over its EPJ list.
+ * Follows src/soft_force.hpp:53-71. */
+static void epep_one(const double xi[3], double rsi, const double *epj_pos, const double *epj_mass,
+                     const double *epj_rs, const int32_t *ids, int64_t nj, double eps2, double r_out2,
+                     int nnb_with_eps, double ai[3], double *poti, int64_t *nnb) {
+    double ax = 0.0, ay = 0.0, az = 0.0, p = 0.0;
+    int64_t n = 0;
+    for (int64_t k = 0; k < nj; ++k) {
+        const int64_t j = ids[k];
+        const double rx = xi[0] - epj_pos[3 * j + 0];
+        const double ry = xi[1] - epj_pos[3 * j + 1];
+        const double rz = xi[2] - epj_pos[3 * j + 2];
+        const double r2 = rx * rx + ry * ry + rz * rz;
+        const double r2_eps = r2 + eps2;
+        const double r_search = dmax(rsi, epj_rs[j]);
+        const double r2_test = nnb_with_eps ? r2_eps : r2;
+        if (r2_test < r_search * r_search) n++;
+        const double r2_tmp = (r2_eps > r_out2) ? r2_eps : r_out2;
+        const double r_inv = 1.0 / sqrt(r2_tmp);
+        const double m_r = epj_mass[j] * r_inv;
+        const double m_r3 = m_r * r_inv * r_inv;
+        ax -= m_r3 * rx;
+        ay -= m_r3 * ry;
+        az -= m_r3 * rz;
+        p -= m_r;
+    }
+    ai[0] = ax;
+    ai[1] = ay;
+    ai[2] = az;
+    *poti = p;
+    *nnb = n;
+}
+
+/* One walk's EP-SP quadrupole sum.  Follows src/soft_force.hpp:174-195;
+ * quad is (xx, yy, zz, xy, xz, yz), the raw second moment about the centre of
+ * mass. */
+static void epsp_one(const double xi[3], const double *spj_pos, const double *spj_mass,
+                     const double *spj_quad, const int32_t *ids, int64_t nj, double eps2, double ai[3],
+                     double *poti) {
+    double ax = 0.0, ay = 0.0, az = 0.0, p = 0.0;
+    for (int64_t k = 0; k < nj; ++k) {
+        const int64_t j = ids[k];
+        const double mj = spj_mass[j];
+        const double rx = xi[0] - spj_pos[3 * j + 0];
+        const double ry = xi[1] - spj_pos[3 * j + 1];
+        const double rz = xi[2] - spj_pos[3 * j + 2];
+        const double r2 = rx * rx + ry * ry + rz * rz + eps2;
+        const double *q = spj_quad + 6 * j;
+        const double qxx = q[0], qyy = q[1], qzz = q[2], qxy = q[3], qxz = q[4], qyz = q[5];
+        const double tr = qxx + qyy + qzz;
+        const double qrx = qxx * rx + qxy * ry + qxz * rz;
+        const double qry = qyy * ry + qyz * rz + qxy * rx;
+        const double qrz = qzz * rz + qxz * rx + qyz * ry;
+        const double qrr = qrx * rx + qry * ry + qrz * rz;
+        const double r_inv = 1.0f / sqrt(r2);
+        const double r2_inv = r_inv * r_inv;
+        const double r3_inv = r2_inv * r_inv;
+        const double r5_inv = r2_inv * r3_inv * 1.5;
+        const double qrr_r5 = r5_inv * qrr;
+        const double qrr_r7 = r2_inv * qrr_r5;
+        const double A = mj * r3_inv - tr * r5_inv + 5 * qrr_r7;
+        const double B = -2.0 * r5_inv;
+        ax -= A * rx + B * qrx;
+        ay -= A * ry + B * qry;
+        az -= A * rz + B * qrz;
+        p -= mj * r_inv - 0.5 * tr * r3_inv + qrr_r5;
+    }
+    ai[0] = ax;
+    ai[1] = ay;
+    ai[2] = az;
+    *poti = p;
+}
+
+/* Full multi-walk evaluation.  Outputs are per EPI row (walk order):
+ *   acc[3*i], pot[i]       : G*ai_ep + G*ai_sp, as the two functors accumulate
+ *                            into one ForceSoft (src/soft_force.hpp:73,77,196-197)
+ *   nnb[i]                 : neighbour count
+ *   acc_ep/pot_ep/acc_sp/pot_sp (each may be NULL): the separate G-scaled parts.
+ * walk_rcut2 (may be NULL) overrides r_out^2 per walk for independent clusters. */
+void oracle_force(int64_t n_walk, const int64_t *epi_disp, const double *epi_pos, const double *epi_rs,
+                  const double *epj_pos, const double *epj_mass, const double *epj_rs,
+                  const double *spj_pos, const double *spj_mass, const double *spj_quad,
+                  const int64_t *epj_disp, const int32_t *id_epj, const int64_t *spj_disp,
+                  const int32_t *id_spj, double eps2, double rcut2, double G, const double *walk_rcut2,
+                  int nnb_with_eps, double *acc, double *pot, int64_t *nnb, double *acc_ep,
+                  double *pot_ep, double *acc_sp, double *pot_sp) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t w = 0; w < n_walk; ++w) {
+        const double r_out2 = walk_rcut2 ? walk_rcut2[w] : rcut2;
+        for (int64_t i = epi_disp[w]; i < epi_disp[w + 1]; ++i) {
+            const double *xi = epi_pos + 3 * i;
+            double ae[3], pe, as[3], ps;
+            int64_t n;
+            epep_one(xi, epi_rs[i], epj_pos, epj_mass, epj_rs, id_epj + epj_disp[w],
+                     epj_disp[w + 1] - epj_disp[w], eps2, r_out2, nnb_with_eps, ae, &pe, &n);
+            epsp_one(xi, spj_pos, spj_mass, spj_quad, id_spj + spj_disp[w], spj_disp[w + 1] - spj_disp[w],
+                     eps2, as, &ps);
+            double f[3], p;
+            for (int d = 0; d < 3; ++d) f[d] = 0.0 + G * ae[d];
+            p = 0.0 + G * pe;
+            for (int d = 0; d < 3; ++d) f[d] += G * as[d];
+            p += G * ps;
+            for (int d = 0; d < 3; ++d) acc[3 * i + d] = f[d];
+            pot[i] = p;
+            nnb[i] = n;
+            if (acc_ep) for (int d = 0; d < 3; ++d) acc_ep[3 * i + d] = G * ae[d];
+            if (pot_ep) pot_ep[i] = G * pe;
+            if (acc_sp) for (int d = 0; d < 3; ++d) acc_sp[3 * i + d] = G * as[d];
+            if (pot_sp) pot_sp[i] = G * ps;
+        }
+    }
+}
+
+/* Global neighbour count over all particles (no tree): for each i, the number
+ * of j with |xi-xj|^2 + eps2 < max(rs_i, rs_j)^2, self included. */
+void oracle_nnb_global(int64_t n, const double *pos, const double *rs, double eps2, int64_t *nnb) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t c = 0;
+        for (int64_t j = 0; j < n; ++j) {
+            const double rx = pos[3 * i + 0] - pos[3 * j + 0];
+            const double ry = pos[3 * i + 1] - pos[3 * j + 1];
+            const double rz = pos[3 * i + 2] - pos[3 * j + 2];
+            const double r2 = rx * rx + ry * ry + rz * rz + eps2;
+            const double r_search = dmax(rs[i], rs[j]);
+            if (r2 < r_search * r_search) c++;
+        }
+        nnb[i] = c;
+    }
+}
+
+/* Direct N^2 FP64 sum of unsoftened gravity with the same linear cutoff, for
+ * the truth side of force-error statistics (no tree, no multipoles). */
+void oracle_direct(int64_t n_target, const int64_t *target, int64_t n, const double *pos,
+                   const double *mass, double eps2, double rcut2, double G, double *acc, double *pot) {
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t t = 0; t < n_target; ++t) {
+        const int64_t i = target[t];
+        double ax = 0, ay = 0, az = 0, p = 0;
+        for (int64_t j = 0; j < n; ++j) {
+            const double rx = pos[3 * i + 0] - pos[3 * j + 0];
+            const double ry = pos[3 * i + 1] - pos[3 * j + 1];
+            const double rz = pos[3 * i + 2] - pos[3 * j + 2];
+            const double r2 = rx * rx + ry * ry + rz * rz + eps2;
+            const double r2c = r2 > rcut2 ? r2 : rcut2;
+            const double ri = 1.0 / sqrt(r2c);
+            const double mr = mass[j] * ri;
+            const double mr3 = mr * ri * ri;
+            ax -= mr3 * rx;
+            ay -= mr3 * ry;
+            az -= mr3 * rz;
+            p -= mr;
+        }
+        acc[3 * t + 0] = G * ax;
+        acc[3 * t + 1] = G * ay;
+        acc[3 * t + 2] = G * az;
+        pot[t] = G * p;
+    }
+}

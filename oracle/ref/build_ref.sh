@@ -1,0 +1,35 @@
+#!/usr/bin/env bash
+# Compiles the reference's own CPU force functors from the reference sources,
+# in place, into oracle/_ref/ (git-ignored):
+#   libref_nosimd.so   FP64 NoSimd functors          (src/soft_force.hpp)
+#   libref_simd32.so   AVX-512 PhantomGrapeQuad FP32  (src/phantomquad_for_p3t_x86.hpp),
+#                      EP with one Newton-Raphson step as PeTar's default
+#                      (RSQRT_NR_EPJ_X2, src/petar.hpp:1-15)
+#   libref_simd64.so   AVX-512 PhantomGrapeQuad64Bit  (P3T_64BIT: CALC_EP_64bit,
+#                      CALC_SP_64bit, RSQRT_NR_EPJ_X4, RSQRT_NR_SPJ_X4)
+# The SIMD kernels are x86 only; on other hosts only the NoSimd library is
+# built.  The NoSimd build uses -ffp-contract=off so its FP64 results are
+# defined by source order alone.
+# Usage: oracle/ref/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+set -euo pipefail
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+REF="${1:-/root/reference}"
+SRC="$REF/src"
+OUT="$HERE/../_ref"
+if [ ! -f "$SRC/soft_force.hpp" ]; then
+    echo "reference sources not found under $SRC" >&2
+    exit 1
+fi
+mkdir -p "$OUT"
+CXX="${CXX:-g++}"
+COMMON=(-std=c++17 -fPIC -shared -fopenmp -I"$HERE" -I"$SRC" -DUSE_QUAD)
+"$CXX" -O2 -ffp-contract=off "${COMMON[@]}" -DREF_NOSIMD "$HERE/ref_driver.cpp" -o "$OUT/libref_nosimd.so" &
+if [ "$(uname -m)" = "x86_64" ]; then
+    SIMD=(-O2 -march=skylake-avx512 -DUSE_SIMD -DINTRINSIC_X86)
+    "$CXX" "${SIMD[@]}" "${COMMON[@]}" -DREF_SIMD -DRSQRT_NR_EPJ_X2 \
+        "$HERE/ref_driver.cpp" -o "$OUT/libref_simd32.so" &
+    "$CXX" "${SIMD[@]}" "${COMMON[@]}" -DREF_SIMD -DCALC_EP_64bit -DCALC_SP_64bit \
+        -DRSQRT_NR_EPJ_X4 -DRSQRT_NR_SPJ_X4 "$HERE/ref_driver.cpp" -o "$OUT/libref_simd64.so" &
+fi
+wait
+ls "$OUT"

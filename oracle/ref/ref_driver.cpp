@@ -1,0 +1,127 @@
+// C entry points around the reference's own force functors, for building
+// golden fixtures.  Compiled once per variant by build_ref.sh:
+//   REF_NOSIMD : CalcForceEpEpWithLinearCutoffNoSimd, CalcForceEpSpQuadNoSimd,
+//                SearchNeighborEpEpNoSimd  (src/soft_force.hpp:11-34,38-87,160-200)
+//   REF_SIMD   : CalcForceEpEpWithLinearCutoffSimd, CalcForceEpSpQuadSimd,
+//                SearchNeighborEpEpSimd    (src/soft_force.hpp:239-283,350-425,491-554)
+//                over PhantomGrapeQuad (FP32) or, with CALC_EP_64bit /
+//                CALC_SP_64bit, PhantomGrapeQuad64Bit.
+// Each call evaluates one i-set against one j-set, as one FDPS walk would.
+#include "ref_shim.hpp"
+#include "soft_force.hpp"
+
+PS::F64 ForceSoft::grav_const = 1.0;
+PS::F64 EPISoft::eps = 0.0;
+PS::F64 EPISoft::r_out = 0.0;
+
+#if defined(REF_NOSIMD)
+typedef CalcForceEpEpWithLinearCutoffNoSimd EpEp;
+typedef CalcForceEpSpQuadNoSimd EpSp;
+typedef SearchNeighborEpEpNoSimd Nb;
+#elif defined(REF_SIMD)
+typedef CalcForceEpEpWithLinearCutoffSimd EpEp;
+typedef CalcForceEpSpQuadSimd EpSp;
+typedef SearchNeighborEpEpSimd Nb;
+#else
+#error "define REF_NOSIMD or REF_SIMD"
+#endif
+
+static void load_i(int ni, const double* xi, const double* rsi, EPISoft* epi) {
+    for (int i = 0; i < ni; ++i) {
+        epi[i].id = i;
+        epi[i].pos = PS::F64vec(xi[3 * i], xi[3 * i + 1], xi[3 * i + 2]);
+        epi[i].r_search = rsi[i];
+        epi[i].rank_org = 0;
+        epi[i].type = 1;
+    }
+}
+
+extern "C" {
+
+void ref_set_params(double eps, double r_out, double G) {
+    EPISoft::eps = eps;
+    EPISoft::r_out = r_out;
+    ForceSoft::grav_const = G;
+}
+
+// EP-EP linear cutoff: acc, pot and n_ngb of ni i-particles against nj j-particles.
+void ref_epep(int ni, const double* xi, const double* rsi, int nj, const double* xj, const double* mj,
+              const double* rsj, double* acc, double* pot, long long* nnb) {
+    EPISoft* epi = new EPISoft[ni > 0 ? ni : 1];
+    EPJSoft* epj = new EPJSoft[nj > 0 ? nj : 1];
+    ForceSoft* f = new ForceSoft[ni > 0 ? ni : 1];
+    load_i(ni, xi, rsi, epi);
+    for (int j = 0; j < nj; ++j) {
+        epj[j].id = j;
+        epj[j].mass = mj[j];
+        epj[j].pos = PS::F64vec(xj[3 * j], xj[3 * j + 1], xj[3 * j + 2]);
+        epj[j].r_search = rsj[j];
+    }
+    for (int i = 0; i < ni; ++i) f[i].clear();
+    EpEp()(epi, ni, epj, nj, f);
+    for (int i = 0; i < ni; ++i) {
+        acc[3 * i] = f[i].acc.x;
+        acc[3 * i + 1] = f[i].acc.y;
+        acc[3 * i + 2] = f[i].acc.z;
+        pot[i] = f[i].pot;
+        nnb[i] = f[i].n_ngb;
+    }
+    delete[] epi;
+    delete[] epj;
+    delete[] f;
+}
+
+// EP-SP quadrupole; quad rows are (xx, yy, zz, xy, xz, yz).
+void ref_epsp(int ni, const double* xi, int nj, const double* xj, const double* mj, const double* qj,
+              double* acc, double* pot) {
+    EPISoft* epi = new EPISoft[ni > 0 ? ni : 1];
+    SPJSoft* spj = new SPJSoft[nj > 0 ? nj : 1];
+    ForceSoft* f = new ForceSoft[ni > 0 ? ni : 1];
+    double* zero = new double[ni > 0 ? ni : 1]();
+    load_i(ni, xi, zero, epi);
+    for (int j = 0; j < nj; ++j) {
+        spj[j].mass = mj[j];
+        spj[j].pos = PS::F64vec(xj[3 * j], xj[3 * j + 1], xj[3 * j + 2]);
+        spj[j].quad.xx = qj[6 * j + 0];
+        spj[j].quad.yy = qj[6 * j + 1];
+        spj[j].quad.zz = qj[6 * j + 2];
+        spj[j].quad.xy = qj[6 * j + 3];
+        spj[j].quad.xz = qj[6 * j + 4];
+        spj[j].quad.yz = qj[6 * j + 5];
+    }
+    for (int i = 0; i < ni; ++i) f[i].clear();
+    EpSp()(epi, ni, spj, nj, f);
+    for (int i = 0; i < ni; ++i) {
+        acc[3 * i] = f[i].acc.x;
+        acc[3 * i + 1] = f[i].acc.y;
+        acc[3 * i + 2] = f[i].acc.z;
+        pot[i] = f[i].pot;
+    }
+    delete[] epi;
+    delete[] spj;
+    delete[] f;
+    delete[] zero;
+}
+
+// Neighbour search only.
+void ref_nb(int ni, const double* xi, const double* rsi, int nj, const double* xj, const double* rsj,
+            long long* nnb) {
+    EPISoft* epi = new EPISoft[ni > 0 ? ni : 1];
+    EPJSoft* epj = new EPJSoft[nj > 0 ? nj : 1];
+    ForceSoft* f = new ForceSoft[ni > 0 ? ni : 1];
+    load_i(ni, xi, rsi, epi);
+    for (int j = 0; j < nj; ++j) {
+        epj[j].id = j;
+        epj[j].mass = 1.0;
+        epj[j].pos = PS::F64vec(xj[3 * j], xj[3 * j + 1], xj[3 * j + 2]);
+        epj[j].r_search = rsj[j];
+    }
+    for (int i = 0; i < ni; ++i) f[i].clear();
+    Nb()(epi, ni, epj, nj, f);
+    for (int i = 0; i < ni; ++i) nnb[i] = f[i].n_ngb;
+    delete[] epi;
+    delete[] epj;
+    delete[] f;
+}
+
+}  // extern "C"

@@ -1,0 +1,682 @@
+// Host side of the soft-force C ABI (include/petar_gpuforce.h).
+//
+// Replaces the reference functors' host code (src/force_gpu_cuda.cu:535-880):
+// the caller's FDPS records are packed with OpenMP into pinned staging
+// buffers in the device layout of pgf_internal.cuh, copied with asynchronous
+// cudaMemcpyAsync on one stream, and all walks of a dispatch run in one
+// persistent launch.  Dispatch returns once the work is queued; retrieve
+// waits, copies the results back and unpacks them into the caller's
+// ForceSoft records (overwriting acc, pot and n_ngb as the reference does).
+//
+// Device buffers are process-wide like the reference's file-static
+// cudaPointer objects (src/force_gpu_cuda.cu:513-533), but they grow on demand
+// instead of being capped at NI_LIMIT / NJ_LIMIT.
+#include "petar_gpuforce.h"
+#include "pgf_internal.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+namespace {
+
+using namespace pgf;
+
+constexpr int kMaxTags = 16;
+constexpr int64_t kMaxRows = 0x7fffffff;
+
+std::string g_error;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_error = buf;
+    return code;
+}
+
+#define PGF_CUDA(call)                                                                         \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(PGF_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));         \
+    } while (0)
+
+template <class T>
+struct DevBuf {
+    T* d = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t n) {
+        if (n <= cap && d) return cudaSuccess;
+        size_t want = std::max<size_t>(n, cap + cap / 2);
+        if (want == 0) want = 1;
+        if (d) cudaFree(d);
+        d = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&d, want * sizeof(T));
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (d) cudaFree(d);
+        d = nullptr;
+        cap = 0;
+    }
+};
+
+template <class T>
+struct HostBuf {
+    T* h = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t n) {
+        if (n <= cap && h) return cudaSuccess;
+        size_t want = std::max<size_t>(n, cap + cap / 2);
+        if (want == 0) want = 1;
+        if (h) cudaFreeHost(h);
+        h = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMallocHost(&h, want * sizeof(T));
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (h) cudaFreeHost(h);
+        h = nullptr;
+        cap = 0;
+    }
+};
+
+struct TagState {
+    bool dispatched = false;  // dispatched and not yet retrieved
+    bool has_data = false;    // device holds a complete dispatch (for recompute)
+    int n_walk = 0;
+    int64_t ni_tot = 0;
+    int precision = PGF_PRECISION_MIXED;
+    std::vector<int> n_epi;
+    std::vector<int64_t> epi_disp;
+    DevBuf<EpiDev> epi;
+    DevBuf<int32_t> id_epj, id_spj, order;
+    DevBuf<WalkDesc> walks;
+    DevBuf<double4> accp;
+    DevBuf<int32_t> nnb;
+    HostBuf<EpiDev> h_epi;
+    HostBuf<int32_t> h_id_epj, h_id_spj, h_order;
+    HostBuf<WalkDesc> h_walks;
+    HostBuf<double4> h_accp;
+    HostBuf<int32_t> h_nnb;
+    HostBuf<int32_t> h_flags;  // err, n_retest
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool times_pending = false;  // kernel events recorded, not yet added to the profile
+    Params params{};
+};
+
+struct State {
+    bool init = false;
+    int device = -1;
+    int num_sms = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    bool user_stream = false;
+    double eps2 = 0, rcut2 = 0, G = 1;
+    int precision = PGF_PRECISION_MIXED;
+    // shared j data
+    DevBuf<EpjDev> epj;
+    DevBuf<double> epj_rs;
+    DevBuf<float> epj_rs2f;
+    DevBuf<SpjDev> spj;
+    HostBuf<EpjDev> h_epj;
+    HostBuf<double> h_epj_rs;
+    HostBuf<float> h_epj_rs2f;
+    HostBuf<SpjDev> h_spj;
+    int64_t n_epj_tot = 0, n_spj_tot = 0;
+    bool j_sent = false;
+    // scratch
+    DevBuf<int32_t> scratch;  // [0] queue head, [1] n_retest, [2] err
+    DevBuf<Retest> retest;
+    int retest_cap = 0;
+    std::vector<double> walk_rcut2;
+    TagState tags[kMaxTags];
+    pgf_profile prof{};
+    cudaEvent_t ev_send0 = nullptr, ev_send1 = nullptr;
+};
+
+State g;
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+int ensure_init() {
+    if (!g.init) return fail(PGF_ERR_STATE, "pgf_initialize has not been called");
+    return PGF_OK;
+}
+
+int setup_device(int rank) {
+    int ngpu = 0;
+    cudaError_t e = cudaGetDeviceCount(&ngpu);
+    if (e != cudaSuccess || ngpu <= 0) {
+        cudaGetLastError();
+        return fail(PGF_ERR_NO_DEVICE, "no CUDA device available (%s)",
+                    e == cudaSuccess ? "device count 0" : cudaGetErrorString(e));
+    }
+    g.device = (rank < 0 ? -rank : rank) % ngpu;
+    PGF_CUDA(cudaSetDevice(g.device));
+    PGF_CUDA(cudaDeviceGetAttribute(&g.num_sms, cudaDevAttrMultiProcessorCount, g.device));
+    PGF_CUDA(cudaStreamCreateWithFlags(&g.own_stream, cudaStreamNonBlocking));
+    if (!g.user_stream) g.stream = g.own_stream;
+    PGF_CUDA(cudaEventCreate(&g.ev_send0));
+    PGF_CUDA(cudaEventCreate(&g.ev_send1));
+    for (auto& t : g.tags)
+        for (auto& ev : t.ev) PGF_CUDA(cudaEventCreate(&ev));
+    PGF_CUDA(g.scratch.ensure(4));
+    g.retest_cap = 1 << 20;
+    PGF_CUDA(g.retest.ensure((size_t)g.retest_cap));
+    PGF_CUDA(cudaMemset(g.scratch.d, 0, 4 * sizeof(int32_t)));
+    g.init = true;
+    return PGF_OK;
+}
+
+inline const double* dptr(const void* base, size_t off) {
+    return reinterpret_cast<const double*>(reinterpret_cast<const char*>(base) + off);
+}
+
+// Packs the shared EPJ / SPJ arrays (the send_flag phase,
+// src/force_gpu_cuda.cu:577-619).
+int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, const void* spj,
+                    int64_t n_spj, const pgf_spj_layout* sl) {
+    if (n_epj < 0 || n_spj < 0) return fail(PGF_ERR_ARG, "negative EPJ/SPJ count");
+    if ((n_epj > 0 && (!epj || !el)) || (n_spj > 0 && (!spj || !sl)))
+        return fail(PGF_ERR_ARG, "EPJ/SPJ array or layout is NULL");
+    // Kernels of earlier dispatches may still read the device j arrays and
+    // pending copies may still read the pinned staging: finish them before
+    // either is reused or reallocated.
+    PGF_CUDA(cudaStreamSynchronize(g.stream));
+    const double t0 = now_s();
+    PGF_CUDA(g.h_epj.ensure(n_epj));
+    PGF_CUDA(g.h_epj_rs.ensure(n_epj));
+    PGF_CUDA(g.h_epj_rs2f.ensure(n_epj));
+    PGF_CUDA(g.h_spj.ensure(n_spj));
+    PGF_CUDA(g.epj.ensure(n_epj));
+    PGF_CUDA(g.epj_rs.ensure(n_epj));
+    PGF_CUDA(g.epj_rs2f.ensure(n_epj));
+    PGF_CUDA(g.spj.ensure(n_spj));
+#pragma omp parallel for schedule(static)
+    for (int64_t j = 0; j < n_epj; ++j) {
+        const char* r = reinterpret_cast<const char*>(epj) + j * el->size;
+        const double* p = dptr(r, el->off_pos);
+        const double rs = *dptr(r, el->off_r_search);
+        g.h_epj.h[j] = EpjDev{p[0], p[1], p[2], *dptr(r, el->off_mass)};
+        g.h_epj_rs.h[j] = rs;
+        g.h_epj_rs2f.h[j] = (float)(rs * rs);
+    }
+#pragma omp parallel for schedule(static)
+    for (int64_t j = 0; j < n_spj; ++j) {
+        const char* r = reinterpret_cast<const char*>(spj) + j * sl->size;
+        const double* p = dptr(r, sl->off_pos);
+        SpjDev s;
+        s.x = p[0];
+        s.y = p[1];
+        s.z = p[2];
+        s.m = *dptr(r, sl->off_mass);
+        if (sl->has_quad) {
+            const double* q = dptr(r, sl->off_quad);
+            for (int k = 0; k < 6; ++k) s.q[k] = q[k];
+        } else {
+            for (int k = 0; k < 6; ++k) s.q[k] = 0.0;
+        }
+        g.h_spj.h[j] = s;
+    }
+    g.prof.copy += now_s() - t0;
+    PGF_CUDA(cudaEventRecord(g.ev_send0, g.stream));
+    if (n_epj) {
+        PGF_CUDA(cudaMemcpyAsync(g.epj.d, g.h_epj.h, n_epj * sizeof(EpjDev), cudaMemcpyHostToDevice, g.stream));
+        PGF_CUDA(cudaMemcpyAsync(g.epj_rs.d, g.h_epj_rs.h, n_epj * sizeof(double), cudaMemcpyHostToDevice, g.stream));
+        PGF_CUDA(cudaMemcpyAsync(g.epj_rs2f.d, g.h_epj_rs2f.h, n_epj * sizeof(float), cudaMemcpyHostToDevice,
+                                 g.stream));
+    }
+    if (n_spj)
+        PGF_CUDA(cudaMemcpyAsync(g.spj.d, g.h_spj.h, n_spj * sizeof(SpjDev), cudaMemcpyHostToDevice, g.stream));
+    PGF_CUDA(cudaEventRecord(g.ev_send1, g.stream));
+    PGF_CUDA(cudaEventSynchronize(g.ev_send1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, g.ev_send0, g.ev_send1);
+    g.prof.send += 1e-3 * ms;
+    g.n_epj_tot = n_epj;
+    g.n_spj_tot = n_spj;
+    g.j_sent = true;
+    return PGF_OK;
+}
+
+int launch_tag(TagState& t) {
+    Params& p = t.params;
+    p.queue_head = g.scratch.d;
+    p.n_retest = g.scratch.d + 1;
+    p.err = g.scratch.d + 2;
+    p.retest = g.retest.d;
+    p.retest_cap = g.retest_cap;
+    PGF_CUDA(cudaEventRecord(t.ev[1], g.stream));
+    cudaError_t e;
+    if (t.precision == PGF_PRECISION_FP64) {
+        e = launch_fp64(p, g.stream, g.num_sms);
+        if (e == cudaSuccess) e = cudaEventRecord(t.ev[2], g.stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), g.stream);
+    } else {
+        e = launch_mixed(p, g.stream, g.num_sms);
+        if (e == cudaSuccess) e = cudaEventRecord(t.ev[2], g.stream);
+        if (e == cudaSuccess && p.n_walk > 0) e = launch_retest(p, g.stream, g.num_sms);
+    }
+    if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+    PGF_CUDA(cudaEventRecord(t.ev[3], g.stream));
+    t.dispatched = true;
+    t.has_data = true;
+    t.times_pending = true;
+    return PGF_OK;
+}
+
+// Adds the kernel times of the tag's last launch to the profile (once).
+void harvest_times(TagState& t) {
+    if (!t.times_pending) return;
+    float ms_send = 0, ms_calc = 0, ms_main = 0;
+    cudaEventElapsedTime(&ms_send, t.ev[0], t.ev[1]);
+    cudaEventElapsedTime(&ms_calc, t.ev[1], t.ev[3]);
+    cudaEventElapsedTime(&ms_main, t.ev[1], t.ev[2]);
+    g.prof.send += 1e-3 * ms_send;
+    g.prof.calc += 1e-3 * ms_calc;
+    g.prof.calc_main += 1e-3 * ms_main;
+    g.prof.last_calc = 1e-3 * ms_calc;
+    g.prof.last_calc_main = 1e-3 * ms_main;
+    t.times_pending = false;
+}
+
+// Packs the walks of one index dispatch (src/force_gpu_cuda.cu:621-699).
+int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi, const pgf_epi_layout* il,
+                   const int* const* id_epj, const int* n_epj, const int* const* id_spj, const int* n_spj) {
+    TagState& t = g.tags[tag];
+    if (n_walk < 0) return fail(PGF_ERR_ARG, "n_walk < 0");
+    if (n_walk > 0 && (!epi || !n_epi || !il || !n_epj || !n_spj))
+        return fail(PGF_ERR_ARG, "walk arrays or EPI layout are NULL");
+    if (!g.walk_rcut2.empty() && (int)g.walk_rcut2.size() != n_walk)
+        return fail(PGF_ERR_ARG, "per-walk r_out^2 was set for %zu walks, dispatch has %d",
+                    g.walk_rcut2.size(), n_walk);
+    // The previous dispatch of this tag may still be copying from staging.
+    if (t.dispatched) PGF_CUDA(cudaEventSynchronize(t.ev[3]));
+    const double t0 = now_s();
+    std::vector<int64_t> idisp(n_walk + 1, 0), edisp(n_walk + 1, 0), sdisp(n_walk + 1, 0);
+    for (int w = 0; w < n_walk; ++w) {
+        if (n_epi[w] < 0 || n_epj[w] < 0 || n_spj[w] < 0) return fail(PGF_ERR_ARG, "negative count in walk %d", w);
+        if ((n_epi[w] > 0 && !epi[w]) || (n_epj[w] > 0 && (!id_epj || !id_epj[w])) ||
+            (n_spj[w] > 0 && (!id_spj || !id_spj[w])))
+            return fail(PGF_ERR_ARG, "NULL array for walk %d", w);
+        idisp[w + 1] = idisp[w] + n_epi[w];
+        edisp[w + 1] = edisp[w] + n_epj[w];
+        sdisp[w + 1] = sdisp[w] + n_spj[w];
+    }
+    const int64_t ni = idisp[n_walk], ne = edisp[n_walk], ns = sdisp[n_walk];
+    if (ni > kMaxRows) return fail(PGF_ERR_CAPACITY, "%lld i-particles exceed 2^31-1", (long long)ni);
+    if (ne > 0 && !g.j_sent) return fail(PGF_ERR_STATE, "EPJ ids given before the EPJ array was sent");
+    PGF_CUDA(t.h_epi.ensure(ni));
+    PGF_CUDA(t.h_id_epj.ensure(ne));
+    PGF_CUDA(t.h_id_spj.ensure(ns));
+    PGF_CUDA(t.h_walks.ensure(n_walk));
+    PGF_CUDA(t.h_order.ensure(n_walk));
+    PGF_CUDA(t.epi.ensure(ni));
+    PGF_CUDA(t.id_epj.ensure(ne));
+    PGF_CUDA(t.id_spj.ensure(ns));
+    PGF_CUDA(t.walks.ensure(n_walk));
+    PGF_CUDA(t.order.ensure(n_walk));
+    PGF_CUDA(t.accp.ensure(ni));
+    PGF_CUDA(t.nnb.ensure(ni));
+    int bad_id = -1;
+#pragma omp parallel for schedule(dynamic, 4) reduction(max : bad_id)
+    for (int w = 0; w < n_walk; ++w) {
+        double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+        const char* base = reinterpret_cast<const char*>(epi[w]);
+        for (int i = 0; i < n_epi[w]; ++i) {
+            const char* r = base + (size_t)i * il->size;
+            const double* p = dptr(r, il->off_pos);
+            EpiDev e{p[0], p[1], p[2], *dptr(r, il->off_r_search)};
+            t.h_epi.h[idisp[w] + i] = e;
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = std::min(lo[d], p[d]);
+                hi[d] = std::max(hi[d], p[d]);
+            }
+        }
+        if (n_epj[w]) {
+            std::memcpy(t.h_id_epj.h + edisp[w], id_epj[w], sizeof(int32_t) * n_epj[w]);
+            for (int k = 0; k < n_epj[w]; ++k)
+                if ((unsigned)id_epj[w][k] >= (unsigned)g.n_epj_tot) bad_id = std::max(bad_id, w);
+        }
+        if (n_spj[w]) {
+            std::memcpy(t.h_id_spj.h + sdisp[w], id_spj[w], sizeof(int32_t) * n_spj[w]);
+            for (int k = 0; k < n_spj[w]; ++k)
+                if ((unsigned)id_spj[w][k] >= (unsigned)g.n_spj_tot) bad_id = std::max(bad_id, w);
+        }
+        WalkDesc d;
+        d.epj_begin = edisp[w];
+        d.spj_begin = sdisp[w];
+        d.i_begin = (int32_t)idisp[w];
+        d.n_i = n_epi[w];
+        d.n_epj = n_epj[w];
+        d.n_spj = n_spj[w];
+        if (n_epi[w] > 0) {
+            d.cx = 0.5 * (lo[0] + hi[0]);
+            d.cy = 0.5 * (lo[1] + hi[1]);
+            d.cz = 0.5 * (lo[2] + hi[2]);
+        } else {
+            d.cx = d.cy = d.cz = 0.0;
+        }
+        d.rcut2 = g.walk_rcut2.empty() ? g.rcut2 : g.walk_rcut2[w];
+        t.h_walks.h[w] = d;
+    }
+    if (bad_id >= 0) return fail(PGF_ERR_ARG, "walk %d has an EPJ/SPJ id outside the sent arrays", bad_id);
+    // Work queue: walks by descending cost, EP-SP pairs weighted by their
+    // larger instruction count.
+    {
+        std::vector<int32_t> ord(n_walk);
+        std::iota(ord.begin(), ord.end(), 0);
+        std::vector<double> cost(n_walk);
+        for (int w = 0; w < n_walk; ++w)
+            cost[w] = (double)n_epi[w] * ((double)n_epj[w] + 2.0 * (double)n_spj[w]) + 1.0;
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+        std::memcpy(t.h_order.h, ord.data(), sizeof(int32_t) * n_walk);
+    }
+    t.n_walk = n_walk;
+    t.ni_tot = ni;
+    t.n_epi.assign(n_epi, n_epi + n_walk);
+    t.epi_disp = idisp;
+    t.precision = g.precision;
+    g.prof.copy += now_s() - t0;
+
+    cudaStream_t s = g.stream;
+    PGF_CUDA(cudaEventRecord(t.ev[0], s));
+    if (ni) PGF_CUDA(cudaMemcpyAsync(t.epi.d, t.h_epi.h, ni * sizeof(EpiDev), cudaMemcpyHostToDevice, s));
+    if (ne) PGF_CUDA(cudaMemcpyAsync(t.id_epj.d, t.h_id_epj.h, ne * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    if (ns) PGF_CUDA(cudaMemcpyAsync(t.id_spj.d, t.h_id_spj.h, ns * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    if (n_walk) {
+        PGF_CUDA(cudaMemcpyAsync(t.walks.d, t.h_walks.h, n_walk * sizeof(WalkDesc), cudaMemcpyHostToDevice, s));
+        PGF_CUDA(cudaMemcpyAsync(t.order.d, t.h_order.h, n_walk * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+    }
+    Params& p = t.params;
+    p = Params{};
+    p.epi = t.epi.d;
+    p.epj = g.epj.d;
+    p.epj_rs = g.epj_rs.d;
+    p.epj_rs2f = g.epj_rs2f.d;
+    p.spj = g.spj.d;
+    p.id_epj = t.id_epj.d;
+    p.id_spj = t.id_spj.d;
+    p.walks = t.walks.d;
+    p.order = t.order.d;
+    p.n_walk = n_walk;
+    p.eps2 = g.eps2;
+    p.G = g.G;
+    p.out_accp = t.accp.d;
+    p.out_nnb = t.nnb.d;
+    g.prof.n_walk += n_walk;
+    g.prof.n_epi += ni;
+    g.prof.n_epj += ne;
+    g.prof.n_spj += ns;
+    g.prof.n_call += 1;
+    return launch_tag(t);
+}
+
+bool valid_tag(int tag) { return tag >= 0 && tag < kMaxTags; }
+
+}  // namespace
+
+extern "C" {
+
+int pgf_initialize(int rank, double eps2, double rcut2, double G) {
+    if (!(eps2 >= 0) || !(rcut2 >= 0) || !std::isfinite(G))
+        return fail(PGF_ERR_ARG, "eps2 and rcut2 must be >= 0 and G finite");
+    if (!g.init) {
+        int r = setup_device(rank);
+        if (r != PGF_OK) return r;
+    } else {
+        PGF_CUDA(cudaSetDevice(g.device));
+    }
+    g.eps2 = eps2;
+    g.rcut2 = rcut2;
+    g.G = G;
+    g_error.clear();
+    return PGF_OK;
+}
+
+int pgf_set_precision(int precision) {
+    if (precision != PGF_PRECISION_MIXED && precision != PGF_PRECISION_FP64)
+        return fail(PGF_ERR_ARG, "unknown precision %d", precision);
+    g.precision = precision;
+    return PGF_OK;
+}
+
+int pgf_set_stream(void* cuda_stream) {
+    g.user_stream = cuda_stream != nullptr;
+    g.stream = cuda_stream ? (cudaStream_t)cuda_stream : g.own_stream;
+    return PGF_OK;
+}
+
+int pgf_set_walk_rcut2(const double* walk_rcut2, int n_walk) {
+    if (n_walk < 0 || (n_walk > 0 && !walk_rcut2)) return fail(PGF_ERR_ARG, "bad per-walk r_out^2 array");
+    for (int w = 0; w < n_walk; ++w)
+        if (!(walk_rcut2[w] >= 0)) return fail(PGF_ERR_ARG, "per-walk r_out^2 must be >= 0");
+    g.walk_rcut2.assign(walk_rcut2, walk_rcut2 + n_walk);
+    return PGF_OK;
+}
+
+int pgf_dispatch_index(int tag, int n_walk, const void* const* epi, const int* n_epi,
+                       const pgf_epi_layout* epi_layout, const int* const* id_epj, const int* n_epj,
+                       const int* const* id_spj, const int* n_spj, const void* epj, int n_epj_tot,
+                       const pgf_epj_layout* epj_layout, const void* spj, int n_spj_tot,
+                       const pgf_spj_layout* spj_layout, int send_flag) {
+    if (int r = ensure_init()) return r;
+    if (!valid_tag(tag)) return fail(PGF_ERR_ARG, "tag %d outside [0, %d)", tag, kMaxTags);
+    PGF_CUDA(cudaSetDevice(g.device));
+    if (send_flag) return pack_and_send_j(epj, n_epj_tot, epj_layout, spj, n_spj_tot, spj_layout);
+    return dispatch_walks(tag, n_walk, epi, n_epi, epi_layout, id_epj, n_epj, id_spj, n_spj);
+}
+
+int pgf_dispatch(int tag, int n_walk, const void* const* epi, const int* n_epi, const pgf_epi_layout* epi_layout,
+                 const void* const* epj, const int* n_epj, const pgf_epj_layout* epj_layout,
+                 const void* const* spj, const int* n_spj, const pgf_spj_layout* spj_layout) {
+    if (int r = ensure_init()) return r;
+    if (!valid_tag(tag)) return fail(PGF_ERR_ARG, "tag %d outside [0, %d)", tag, kMaxTags);
+    if (n_walk < 0) return fail(PGF_ERR_ARG, "n_walk < 0");
+    if (n_walk > 0 && (!n_epj || !n_spj)) return fail(PGF_ERR_ARG, "per-walk counts are NULL");
+    PGF_CUDA(cudaSetDevice(g.device));
+    // The per-walk j arrays are concatenated into the shared arrays and
+    // addressed through identity id lists.
+    int64_t ne = 0, ns = 0;
+    for (int w = 0; w < n_walk; ++w) {
+        if (n_epj[w] < 0 || n_spj[w] < 0) return fail(PGF_ERR_ARG, "negative count in walk %d", w);
+        if ((n_epj[w] > 0 && (!epj || !epj[w] || !epj_layout)) || (n_spj[w] > 0 && (!spj || !spj[w] || !spj_layout)))
+            return fail(PGF_ERR_ARG, "NULL j array for walk %d", w);
+        ne += n_epj[w];
+        ns += n_spj[w];
+    }
+    if (ne > kMaxRows || ns > kMaxRows) return fail(PGF_ERR_CAPACITY, "j rows exceed 2^31-1");
+    std::vector<char> ej(ne * sizeof(double) * 5), sj(ns * sizeof(double) * 10);
+    std::vector<int> ids_e(ne), ids_s(ns);
+    std::vector<const int*> pe(n_walk), ps(n_walk);
+    int64_t oe = 0, os = 0;
+    for (int w = 0; w < n_walk; ++w) {
+        for (int k = 0; k < n_epj[w]; ++k) {
+            const char* r = reinterpret_cast<const char*>(epj[w]) + (size_t)k * epj_layout->size;
+            double* o = reinterpret_cast<double*>(ej.data()) + 5 * (oe + k);
+            const double* p = dptr(r, epj_layout->off_pos);
+            o[0] = *dptr(r, epj_layout->off_mass);
+            o[1] = p[0];
+            o[2] = p[1];
+            o[3] = p[2];
+            o[4] = *dptr(r, epj_layout->off_r_search);
+            ids_e[oe + k] = (int)(oe + k);
+        }
+        for (int k = 0; k < n_spj[w]; ++k) {
+            const char* r = reinterpret_cast<const char*>(spj[w]) + (size_t)k * spj_layout->size;
+            double* o = reinterpret_cast<double*>(sj.data()) + 10 * (os + k);
+            const double* p = dptr(r, spj_layout->off_pos);
+            o[0] = *dptr(r, spj_layout->off_mass);
+            o[1] = p[0];
+            o[2] = p[1];
+            o[3] = p[2];
+            for (int c = 0; c < 6; ++c) o[4 + c] = spj_layout->has_quad ? dptr(r, spj_layout->off_quad)[c] : 0.0;
+            ids_s[os + k] = (int)(os + k);
+        }
+        pe[w] = ids_e.data() + oe;
+        ps[w] = ids_s.data() + os;
+        oe += n_epj[w];
+        os += n_spj[w];
+    }
+    const pgf_epj_layout el{5 * sizeof(double), 0, sizeof(double), 4 * sizeof(double)};
+    const pgf_spj_layout sl{10 * sizeof(double), 0, sizeof(double), 4 * sizeof(double), 1};
+    int r = pack_and_send_j(ej.data(), ne, &el, sj.data(), ns, &sl);
+    if (r != PGF_OK) return r;
+    return dispatch_walks(tag, n_walk, epi, n_epi, epi_layout, pe.data(), n_epj, ps.data(), n_spj);
+}
+
+int pgf_recompute(int tag) {
+    if (int r = ensure_init()) return r;
+    if (!valid_tag(tag)) return fail(PGF_ERR_ARG, "tag %d outside [0, %d)", tag, kMaxTags);
+    TagState& t = g.tags[tag];
+    if (!t.has_data) return fail(PGF_ERR_STATE, "tag %d has no dispatched data", tag);
+    PGF_CUDA(cudaSetDevice(g.device));
+    PGF_CUDA(cudaEventRecord(t.ev[0], g.stream));
+    t.precision = g.precision;
+    return launch_tag(t);
+}
+
+int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const pgf_force_layout* fl) {
+    if (int r = ensure_init()) return r;
+    if (!valid_tag(tag)) return fail(PGF_ERR_ARG, "tag %d outside [0, %d)", tag, kMaxTags);
+    TagState& t = g.tags[tag];
+    if (!t.dispatched) return fail(PGF_ERR_STATE, "retrieve for tag %d without a dispatch", tag);
+    if (n_walk != t.n_walk) return fail(PGF_ERR_ARG, "retrieve n_walk %d != dispatched %d", n_walk, t.n_walk);
+    if (n_walk > 0 && (!ni || !force || !fl)) return fail(PGF_ERR_ARG, "NULL ni/force/layout");
+    if (fl && fl->n_ngb_bytes != 4 && fl->n_ngb_bytes != 8) return fail(PGF_ERR_ARG, "n_ngb_bytes must be 4 or 8");
+    for (int w = 0; w < n_walk; ++w) {
+        if (ni[w] != t.n_epi[w]) return fail(PGF_ERR_ARG, "walk %d: ni %d != dispatched %d", w, ni[w], t.n_epi[w]);
+        if (ni[w] > 0 && !force[w]) return fail(PGF_ERR_ARG, "force[%d] is NULL", w);
+    }
+    PGF_CUDA(cudaSetDevice(g.device));
+    const int64_t n = t.ni_tot;
+    PGF_CUDA(t.h_accp.ensure(n));
+    PGF_CUDA(t.h_nnb.ensure(n));
+    PGF_CUDA(t.h_flags.ensure(4));
+    cudaStream_t s = g.stream;
+    PGF_CUDA(cudaEventRecord(t.ev[4], s));
+    if (n) {
+        PGF_CUDA(cudaMemcpyAsync(t.h_accp.h, t.accp.d, n * sizeof(double4), cudaMemcpyDeviceToHost, s));
+        PGF_CUDA(cudaMemcpyAsync(t.h_nnb.h, t.nnb.d, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    }
+    PGF_CUDA(cudaMemcpyAsync(t.h_flags.h, g.scratch.d, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    PGF_CUDA(cudaEventRecord(t.ev[5], s));
+    PGF_CUDA(cudaEventSynchronize(t.ev[5]));
+    t.dispatched = false;
+    harvest_times(t);
+    float ms_recv = 0;
+    cudaEventElapsedTime(&ms_recv, t.ev[4], t.ev[5]);
+    g.prof.recv += 1e-3 * ms_recv;
+    g.prof.n_retest += t.h_flags.h[1];
+    if (t.h_flags.h[2] != 0) return fail(PGF_ERR_DEVICE, "device error word %d", t.h_flags.h[2]);
+    const double t0 = now_s();
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int w = 0; w < n_walk; ++w) {
+        char* base = reinterpret_cast<char*>(force[w]);
+        const int64_t o = t.epi_disp[w];
+        for (int i = 0; i < ni[w]; ++i) {
+            char* r = base + (size_t)i * fl->size;
+            const double4 a = t.h_accp.h[o + i];
+            double* acc = reinterpret_cast<double*>(r + fl->off_acc);
+            acc[0] = a.x;
+            acc[1] = a.y;
+            acc[2] = a.z;
+            *reinterpret_cast<double*>(r + fl->off_pot) = a.w;
+            if (fl->n_ngb_bytes == 8)
+                *reinterpret_cast<int64_t*>(r + fl->off_n_ngb) = t.h_nnb.h[o + i];
+            else
+                *reinterpret_cast<int32_t*>(r + fl->off_n_ngb) = t.h_nnb.h[o + i];
+        }
+    }
+    g.prof.copy += now_s() - t0;
+    return PGF_OK;
+}
+
+int pgf_wait(int tag) {
+    if (int r = ensure_init()) return r;
+    if (!valid_tag(tag)) return fail(PGF_ERR_ARG, "tag %d outside [0, %d)", tag, kMaxTags);
+    TagState& t = g.tags[tag];
+    if (!t.has_data) return fail(PGF_ERR_STATE, "tag %d has no dispatched data", tag);
+    PGF_CUDA(cudaSetDevice(g.device));
+    PGF_CUDA(cudaEventSynchronize(t.ev[3]));
+    harvest_times(t);
+    return PGF_OK;
+}
+
+int pgf_get_profile(pgf_profile* out) {
+    if (!out) return fail(PGF_ERR_ARG, "NULL profile");
+    *out = g.prof;
+    return PGF_OK;
+}
+
+int pgf_clear_profile(void) {
+    g.prof = pgf_profile{};
+    return PGF_OK;
+}
+
+const char* pgf_last_error(void) { return g_error.c_str(); }
+
+int pgf_finalize(void) {
+    if (!g.init) return PGF_OK;
+    cudaSetDevice(g.device);
+    cudaStreamSynchronize(g.stream);
+    for (auto& t : g.tags) {
+        t.epi.release();
+        t.id_epj.release();
+        t.id_spj.release();
+        t.order.release();
+        t.walks.release();
+        t.accp.release();
+        t.nnb.release();
+        t.h_epi.release();
+        t.h_id_epj.release();
+        t.h_id_spj.release();
+        t.h_order.release();
+        t.h_walks.release();
+        t.h_accp.release();
+        t.h_nnb.release();
+        t.h_flags.release();
+        for (auto& ev : t.ev) {
+            if (ev) cudaEventDestroy(ev);
+            ev = nullptr;
+        }
+        t.dispatched = t.has_data = false;
+    }
+    g.epj.release();
+    g.epj_rs.release();
+    g.epj_rs2f.release();
+    g.spj.release();
+    g.h_epj.release();
+    g.h_epj_rs.release();
+    g.h_epj_rs2f.release();
+    g.h_spj.release();
+    g.scratch.release();
+    g.retest.release();
+    if (g.ev_send0) cudaEventDestroy(g.ev_send0);
+    if (g.ev_send1) cudaEventDestroy(g.ev_send1);
+    g.ev_send0 = g.ev_send1 = nullptr;
+    if (g.own_stream) cudaStreamDestroy(g.own_stream);
+    g.own_stream = nullptr;
+    if (!g.user_stream) g.stream = nullptr;
+    g.j_sent = false;
+    g.init = false;
+    return PGF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,101 @@
+// Device data layout and kernel interfaces of the soft-force library.
+//
+// HBM layout (one copy per process, grown on demand, never shrunk):
+//   EpjDev[n_epj_tot]    32 B: FP64 position and mass
+//   epj_rs[n_epj_tot]     8 B: FP64 r_search (exact neighbour tests)
+//   epj_rs2f[n_epj_tot]   4 B: (float)(r_search^2), the square taken in FP64
+//   SpjDev[n_spj_tot]    80 B: FP64 position, mass and raw quadrupole
+//   EpiDev[ni_tot]       32 B: FP64 position and r_search
+//   id_epj / id_spj      int32 per list entry, walks concatenated
+//   WalkDesc[n_walk]     64 B: list offsets, walk centre (FP64), r_out^2
+//   order[n_walk]        walks sorted by descending work (the work queue)
+//   out_accp[ni_tot]     double4: acc.xyz, pot (G applied)
+//   out_nnb[ni_tot]      int32 neighbour count
+// The EPJ and SPJ arrays of a 1.5M-particle problem (about 60 MB + 23 MB)
+// stay resident in the 129 MB L2 while the id lists stream from HBM once.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pgf {
+
+struct __align__(32) EpjDev {
+    double x, y, z, m;
+};
+static_assert(sizeof(EpjDev) == 32, "EpjDev layout");
+
+struct __align__(16) SpjDev {
+    double x, y, z, m;
+    double q[6];  // xx, yy, zz, xy, xz, yz (zero for monopole superparticles)
+};
+static_assert(sizeof(SpjDev) == 80, "SpjDev layout");
+
+struct __align__(32) EpiDev {
+    double x, y, z, rs;
+};
+static_assert(sizeof(EpiDev) == 32, "EpiDev layout");
+
+struct __align__(16) WalkDesc {
+    int64_t epj_begin;  // offset of the walk's EPJ ids in id_epj
+    int64_t spj_begin;  // offset of the walk's SPJ ids in id_spj
+    int32_t i_begin;    // first EPI row of the walk
+    int32_t n_i;
+    int32_t n_epj;
+    int32_t n_spj;
+    double cx, cy, cz;  // walk centre: centre of the EPI bounding box
+    double rcut2;       // r_out^2 of the walk
+};
+static_assert(sizeof(WalkDesc) == 64, "WalkDesc layout");
+
+// A pair range whose FP32 neighbour test came within rounding distance of
+// r_search: the retest kernel recounts it in FP64.
+struct Retest {
+    int64_t j_begin;  // offset in id_epj
+    int32_t i;        // EPI row
+    int32_t n;        // number of list entries
+};
+
+struct Params {
+    const EpiDev* epi;
+    const EpjDev* epj;
+    const double* epj_rs;
+    const float* epj_rs2f;
+    const SpjDev* spj;
+    const int32_t* id_epj;
+    const int32_t* id_spj;
+    const WalkDesc* walks;
+    const int32_t* order;
+    int32_t n_walk;
+    int32_t pad0;
+    double eps2;
+    double G;
+    double4* out_accp;
+    int32_t* out_nnb;
+    // scratch
+    int32_t* queue_head;   // work-queue cursor, zeroed before each launch
+    Retest* retest;        // FP64 re-test records
+    int32_t* n_retest;     // number of records pushed (may exceed capacity)
+    int32_t retest_cap;
+    int32_t pad1;
+    int32_t* err;          // device error word (0 = ok)
+};
+
+// Exact FP64 neighbour test of one pair, in the oracle's evaluation order
+// (src/force_gpu_cuda.cu:62-64 semantics, src/soft_force.hpp:58-64 order):
+// r2 = ((dx*dx) + (dy*dy)) + (dz*dz); (r2 + eps2) < max(rs_i, rs_j)^2.
+__device__ __forceinline__ int exact_neighbour(double xi, double yi, double zi, double rsi, double xj,
+                                               double yj, double zj, double rsj, double eps2) {
+    const double dx = __dsub_rn(xi, xj);
+    const double dy = __dsub_rn(yi, yj);
+    const double dz = __dsub_rn(zi, zj);
+    const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    const double rs = rsi > rsj ? rsi : rsj;
+    return __dadd_rn(r2, eps2) < __dmul_rn(rs, rs) ? 1 : 0;
+}
+
+// Launchers (stream-ordered, asynchronous).
+cudaError_t launch_fp64(const Params& p, cudaStream_t s, int num_sms);
+cudaError_t launch_mixed(const Params& p, cudaStream_t s, int num_sms);
+cudaError_t launch_retest(const Params& p, cudaStream_t s, int num_sms);
+
+}  // namespace pgf

@@ -1,0 +1,151 @@
+"""Generates the golden fixtures that pin the FP64 oracle to the reference.
+
+Runs the reference's own CPU force functors -- compiled from the reference
+sources by ``oracle/ref/build_ref.sh`` into ``oracle/_ref/`` -- on seeded
+inputs and stores inputs and outputs as compressed ``.npz`` files next to this
+script.  Needs the reference tree (only present where the fixtures are made);
+the tests only read the committed ``.npz`` files.
+
+Cases
+-----
+``kernel_test.npz``
+    A restatement of the reference's kernel test (src/simd_test.cxx:59-131):
+    1000 EPI and 2000 EPJ from an equal-mass Plummer model, 1000 random SPJ with
+    the distributions of ``setSpj`` (src/simd_test.cxx:44-57), r_out = 0.01,
+    eps = 1e-4, G = 1, r_search = r_out (search_factor = 0).  The RNG is this
+    project's (numpy PCG64), not FDPS's.
+``kernel_test_rsvar.npz``
+    The same with per-particle r_search = r_out + |v| * dt * 3 (the form of
+    Ptcl::calcRSearch, src/ptcl.hpp:227-238) so max(rs_i, rs_j) matters.
+``plummer2048_walks.npz``
+    Workload C1: Kroupa-mass Plummer sphere, N = 2048, theta = 0.3, r_out = 0.02,
+    r_search = 1.5 r_out, eps = 0, lists from this package's interaction-list
+    builder; reference outputs per walk.
+
+Outputs per case and reference variant (``nosimd``: FP64 NoSimd functors;
+``simd32``: AVX-512 PhantomGrapeQuad; ``simd64``: AVX-512 PhantomGrapeQuad64Bit):
+EP-EP acc/pot/n_ngb and EP-SP acc/pot, G-scaled as the functors write them.
+
+Usage: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ctypes
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+REF_LIBS = ROOT / "oracle" / "_ref"
+VARIANTS = ("nosimd", "simd32", "simd64")
+
+
+def _load(variant: str):
+    lib = ctypes.CDLL(str(REF_LIBS / f"libref_{variant}.so"))
+    vp, ci, cd = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    lib.ref_set_params.argtypes = [cd, cd, cd]
+    lib.ref_epep.argtypes = [ci, vp, vp, ci, vp, vp, vp, vp, vp, vp]
+    lib.ref_epsp.argtypes = [ci, vp, ci, vp, vp, vp, vp, vp]
+    lib.ref_nb.argtypes = [ci, vp, vp, ci, vp, vp, vp]
+    return lib
+
+
+def _p(a):
+    return a.ctypes.data
+
+
+def run_ref(lib, eps, r_out, G, walks):
+    """walks: list of dicts with xi, rsi, xj, mj, rsj, xs, ms, qs (contiguous).
+    Returns per-EPI arrays concatenated in walk order."""
+    lib.ref_set_params(eps, r_out, G)
+    out = {k: [] for k in ("acc_ep", "pot_ep", "nnb_ep", "acc_sp", "pot_sp", "nnb_search")}
+    for w in walks:
+        ni, nj, ns = w["rsi"].size, w["mj"].size, w["ms"].size
+        a = np.zeros((ni, 3)); p = np.zeros(ni); n = np.zeros(ni, np.int64)
+        lib.ref_epep(ni, _p(w["xi"]), _p(w["rsi"]), nj, _p(w["xj"]), _p(w["mj"]), _p(w["rsj"]),
+                     _p(a), _p(p), _p(n))
+        out["acc_ep"].append(a); out["pot_ep"].append(p); out["nnb_ep"].append(n)
+        a = np.zeros((ni, 3)); p = np.zeros(ni)
+        if ns:
+            lib.ref_epsp(ni, _p(w["xi"]), ns, _p(w["xs"]), _p(w["ms"]), _p(w["qs"]), _p(a), _p(p))
+        out["acc_sp"].append(a); out["pot_sp"].append(p)
+        n = np.zeros(ni, np.int64)
+        lib.ref_nb(ni, _p(w["xi"]), _p(w["rsi"]), nj, _p(w["xj"]), _p(w["rsj"]), _p(n))
+        out["nnb_search"].append(n)
+    return {k: np.concatenate(v) for k, v in out.items()}
+
+
+def kernel_test_case(seed: int, rs_var: bool) -> dict:
+    from petar_gb300 import ics
+    rng = np.random.default_rng(seed)
+    n_epi, n_epj, n_spj = 1000, 2000, 1000
+    N = max(n_epi, n_epj)
+    mass = np.full(N, 1.0 / N)
+    pos, vel = ics.plummer(rng, mass)
+    r_out, eps, G = 0.01, 1e-4, 1.0
+    if rs_var:
+        rs = r_out + np.sqrt((vel ** 2).sum(1)) * (1.0 / 2048.0) * 3.0
+    else:
+        rs = np.full(N, r_out)
+    # setSpj (src/simd_test.cxx:44-57): mass 1/N + 0.001/N * U, pos 1 + 10 U, quad 10 U.
+    sm = 1.0 / N + 0.001 / N * rng.random(n_spj)
+    sp = 1.0 + 10.0 * rng.random((n_spj, 3))
+    q = 10.0 * rng.random((n_spj, 6))
+    return dict(epi_pos=pos[:n_epi].copy(), epi_rs=rs[:n_epi].copy(), epj_pos=pos[:n_epj].copy(),
+                epj_mass=mass[:n_epj].copy(), epj_rs=rs[:n_epj].copy(), spj_pos=sp, spj_mass=sm,
+                spj_quad=q, epi_disp=np.array([0, n_epi], np.int64),
+                epj_disp=np.array([0, n_epj], np.int64), id_epj=np.arange(n_epj, dtype=np.int32),
+                spj_disp=np.array([0, n_spj], np.int64), id_spj=np.arange(n_spj, dtype=np.int32),
+                eps=np.float64(eps), r_out=np.float64(r_out), G=np.float64(G))
+
+
+def plummer2048_case(seed: int) -> dict:
+    from petar_gb300 import ics, walks
+    cl = ics.make_plummer_cluster(seed, 2048, 0.02, binary_fraction=0.0, theta=0.3, n_group_limit=512)
+    wb = walks.build_walks(cl)
+    return dict(epi_pos=wb.epi_pos, epi_rs=wb.epi_rs, epj_pos=wb.epj_pos, epj_mass=wb.epj_mass,
+                epj_rs=wb.epj_rs, spj_pos=wb.spj_pos, spj_mass=wb.spj_mass, spj_quad=wb.spj_quad,
+                epi_disp=wb.epi_disp, epj_disp=wb.epj_disp, id_epj=wb.id_epj, spj_disp=wb.spj_disp,
+                id_spj=wb.id_spj, eps=np.float64(0.0), r_out=np.float64(cl.r_out), G=np.float64(1.0))
+
+
+def walks_of(case: dict) -> list[dict]:
+    out = []
+    nw = case["epi_disp"].size - 1
+    for w in range(nw):
+        i0, i1 = case["epi_disp"][w], case["epi_disp"][w + 1]
+        je = case["id_epj"][case["epj_disp"][w]:case["epj_disp"][w + 1]]
+        js = case["id_spj"][case["spj_disp"][w]:case["spj_disp"][w + 1]]
+        c = np.ascontiguousarray
+        out.append(dict(xi=c(case["epi_pos"][i0:i1]), rsi=c(case["epi_rs"][i0:i1]),
+                        xj=c(case["epj_pos"][je]), mj=c(case["epj_mass"][je]), rsj=c(case["epj_rs"][je]),
+                        xs=c(case["spj_pos"][js]), ms=c(case["spj_mass"][js]), qs=c(case["spj_quad"][js])))
+    return out
+
+
+def main() -> None:
+    if not (REF_LIBS / "libref_nosimd.so").exists():
+        subprocess.run([str(ROOT / "oracle" / "ref" / "build_ref.sh")], check=True)
+    sys.path.insert(0, str(ROOT))
+    cases = {
+        "kernel_test": kernel_test_case(20240, rs_var=False),
+        "kernel_test_rsvar": kernel_test_case(20241, rs_var=True),
+        "plummer2048_walks": plummer2048_case(1),
+    }
+    libs = {v: _load(v) for v in VARIANTS if (REF_LIBS / f"libref_{v}.so").exists()}
+    for name, case in cases.items():
+        ws = walks_of(case)
+        payload = dict(case)
+        for v, lib in libs.items():
+            res = run_ref(lib, float(case["eps"]), float(case["r_out"]), float(case["G"]), ws)
+            for k, a in res.items():
+                payload[f"{v}__{k}"] = a
+        np.savez_compressed(HERE / f"{name}.npz", **payload)
+        print(name, {k: v.shape for k, v in payload.items() if "__" in k and k.endswith("nnb_ep")})
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,217 @@
+"""GPU parity: both kernels through the C ABI against the FP64 oracle.
+
+Tolerances:
+* neighbour counts: bit-exact (both kernels);
+* plain FP64 kernel: relative force and potential error <= 1e-12 per particle;
+* mixed-precision kernel: median relative error <= 1e-6 and 99.9th
+  percentile <= 1e-5 for force and potential (the accuracy target of the
+  mixed-precision design), and max <= 1e-3.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from helpers import load_golden, rel_err, rel_err_vec, stats
+from petar_gb300 import gpuforce, ics, walks
+from petar_gb300.gpuforce import PGF_PRECISION_FP64, PGF_PRECISION_MIXED
+
+pytestmark = pytest.mark.gpu
+
+MIXED_MEDIAN = 1e-6
+MIXED_P999 = 1e-5
+MIXED_MAX = 1e-3
+FP64_MAX = 1e-12
+
+
+def check(batch, res, precision, o=None, label=""):
+    o = o if o is not None else oracle.force(batch)
+    np.testing.assert_array_equal(res["nnb"], o["nnb"], err_msg=f"{label} neighbour counts")
+    fa = rel_err_vec(res["acc"], o["acc"])
+    fp = rel_err(res["pot"], o["pot"])
+    if precision == PGF_PRECISION_FP64:
+        assert fa.max() <= FP64_MAX, (label, stats(fa))
+        assert fp.max() <= FP64_MAX, (label, stats(fp))
+    else:
+        sa, sp = stats(fa), stats(fp)
+        assert sa["median"] <= MIXED_MEDIAN and sa["p999"] <= MIXED_P999 and sa["max"] <= MIXED_MAX, (label, sa)
+        assert sp["median"] <= MIXED_MEDIAN and sp["p999"] <= MIXED_P999 and sp["max"] <= MIXED_MAX, (label, sp)
+    return fa, fp
+
+
+@pytest.mark.parametrize("precision", [PGF_PRECISION_MIXED, PGF_PRECISION_FP64])
+@pytest.mark.parametrize("case", ["kernel_test", "kernel_test_rsvar", "plummer2048_walks"])
+def test_golden_cases(case, precision):
+    wb, _ = load_golden(case)
+    res = gpuforce.compute(wb, precision)
+    check(wb, res, precision, label=case)
+
+
+@pytest.mark.parametrize("precision", [PGF_PRECISION_MIXED, PGF_PRECISION_FP64])
+def test_plummer_65k(precision):
+    cl = ics.make_plummer_cluster(2, 65536, 0.008)
+    wb = walks.build_walks(cl)
+    res = gpuforce.compute(wb, precision)
+    check(wb, res, precision, label="plummer65k")
+
+
+def _ragged_batch(seed=11):
+    """Walks of sizes the kernel's i-blocking and j-tiling must handle: empty
+    walks, single particles, n_i across the 64/512 boundaries, empty EPJ or SPJ
+    lists, zero-mass j, and a j that coincides with an i."""
+    rng = np.random.default_rng(seed)
+    n_epj, n_spj = 3000, 400
+    epj_pos = rng.normal(size=(n_epj, 3)) * 0.05
+    epj_mass = rng.random(n_epj) / n_epj
+    epj_mass[::17] = 0.0
+    epj_rs = 0.004 + 0.004 * rng.random(n_epj)
+    spj_pos = rng.normal(size=(n_spj, 3)) * 0.5 + 1.0
+    spj_mass = rng.random(n_spj) / n_spj
+    spj_quad = rng.random((n_spj, 6)) * 1e-6
+    sizes = [(0, 10, 5), (1, 0, 0), (1, 1, 1), (31, 257, 129), (63, 5, 0), (64, 0, 7), (65, 300, 3),
+             (127, 1000, 200), (200, 2999, 399), (511, 700, 50), (512, 256, 128), (513, 513, 1),
+             (700, 1500, 300), (1100, 999, 77), (0, 0, 0), (5, 3000, 400)]
+    epi_pos, epi_rs, id_e, id_s, ne, ns, ni = [], [], [], [], [], [], []
+    for a, b, c in sizes:
+        src = rng.integers(0, n_epj, a)
+        p = epj_pos[src] + (rng.random((a, 3)) < 0.5) * rng.normal(size=(a, 3)) * 1e-3
+        epi_pos.append(p)
+        epi_rs.append(0.003 + 0.006 * rng.random(a))
+        ids = rng.choice(n_epj, b, replace=False) if b else np.zeros(0, int)
+        if a and b:
+            ids[0] = src[0]  # the walk's first i sits exactly on a listed j
+        id_e.append(ids)
+        id_s.append(rng.choice(n_spj, c, replace=False) if c else np.zeros(0, int))
+        ni.append(a)
+        ne.append(b)
+        ns.append(c)
+    disp = lambda n: np.concatenate([[0], np.cumsum(n)]).astype(np.int64)
+    return walks.WalkBatch(
+        epi_pos=np.concatenate(epi_pos), epi_rs=np.concatenate(epi_rs), epi_disp=disp(ni),
+        epj_pos=epj_pos, epj_mass=epj_mass, epj_rs=epj_rs, spj_pos=spj_pos, spj_mass=spj_mass,
+        spj_quad=spj_quad, epj_disp=disp(ne), id_epj=np.concatenate(id_e).astype(np.int32),
+        spj_disp=disp(ns), id_spj=np.concatenate(id_s).astype(np.int32), eps2=0.0,
+        rcut2=0.002 ** 2, G=1.0)
+
+
+@pytest.mark.parametrize("precision", [PGF_PRECISION_MIXED, PGF_PRECISION_FP64])
+def test_ragged_walks(precision):
+    wb = _ragged_batch()
+    res = gpuforce.compute(wb, precision)
+    check(wb, res, precision, label="ragged")
+
+
+@pytest.mark.parametrize("precision", [PGF_PRECISION_MIXED, PGF_PRECISION_FP64])
+def test_softened_and_g(precision):
+    wb = _ragged_batch(12)
+    wb.eps2 = (3e-4) ** 2
+    wb.G = 0.7
+    res = gpuforce.compute(wb, precision)
+    check(wb, res, precision, label="eps,G")
+
+
+def test_counts_on_the_boundary():
+    """Pairs placed at |xi - xj| = r_search to within a few FP64 ulps: the FP32
+    test cannot decide them and the FP64 re-test must reproduce the oracle."""
+    rng = np.random.default_rng(5)
+    n = 4000
+    rs = 0.01
+    xi = rng.normal(size=(1, 3)) * 0.02
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    r = rs * (1.0 + rng.integers(-8, 9, n) * 2.0 ** -52)
+    xj = xi + u * r[:, None]
+    wb = walks.WalkBatch(
+        epi_pos=xi, epi_rs=np.array([rs]), epi_disp=np.array([0, 1], np.int64),
+        epj_pos=xj, epj_mass=np.full(n, 1.0 / n), epj_rs=np.full(n, rs), spj_pos=np.zeros((0, 3)),
+        spj_mass=np.zeros(0), spj_quad=np.zeros((0, 6)), epj_disp=np.array([0, n], np.int64),
+        id_epj=np.arange(n, dtype=np.int32), spj_disp=np.array([0, 0], np.int64),
+        id_spj=np.zeros(0, np.int32), eps2=0.0, rcut2=(0.3 * rs) ** 2, G=1.0)
+    o = oracle.force(wb)
+    assert 0 < o["nnb"][0] < n
+    before = gpuforce.get_profile()["n_retest"]
+    res = gpuforce.compute(wb, PGF_PRECISION_MIXED)
+    np.testing.assert_array_equal(res["nnb"], o["nnb"])
+    assert gpuforce.get_profile()["n_retest"] > before
+
+
+def test_ensemble_per_walk_rcut2():
+    """Independent clusters with their own r_out in one launch."""
+    bs = []
+    for k, n in enumerate((1024, 3000, 2048)):
+        cl = ics.make_plummer_cluster(40 + k, n, 0.05 * n ** (-1 / 3), binary_fraction=0.3 if k else 0.0)
+        b = walks.build_walks(cl)
+        b.walk_rcut2 = np.full(b.n_walk, cl.r_out ** 2)
+        bs.append(b)
+    wb = walks.concat_batches(bs)
+    for prec in (PGF_PRECISION_MIXED, PGF_PRECISION_FP64):
+        check(wb, gpuforce.compute(wb, prec), prec, label="ensemble")
+
+
+def test_non_index_dispatch_matches_index_dispatch():
+    """CalcForceWithLinearCutoffCUDA (per-walk j arrays) vs the index form."""
+    wb, _ = load_golden("plummer2048_walks")
+    rec = gpuforce.Records(wb)
+    gpuforce.set_precision(PGF_PRECISION_MIXED)
+    epi = [rec.epi[wb.epi_disp[w]:wb.epi_disp[w + 1]] for w in range(wb.n_walk)]
+    epj = [rec.epj[wb.id_epj[wb.epj_disp[w]:wb.epj_disp[w + 1]]] for w in range(wb.n_walk)]
+    spj = [rec.spj[wb.id_spj[wb.spj_disp[w]:wb.spj_disp[w + 1]]] for w in range(wb.n_walk)]
+    f = gpuforce.CalcForceWithLinearCutoffCUDA(0, wb.eps2, wb.rcut2, wb.G)
+    f(1, wb.n_walk, epi, rec.n_epi, epj, rec.n_epj, spj, rec.n_spj)
+    force = [np.zeros(n, gpuforce.FORCE_DTYPE) for n in rec.n_epi]
+    gpuforce.RetrieveForceCUDA(1, wb.n_walk, rec.n_epi, force)
+    force = np.concatenate(force)
+    check(wb, dict(acc=force["acc"], pot=force["pot"], nnb=force["n_ngb"]), PGF_PRECISION_MIXED,
+          label="non-index")
+
+
+def test_reference_call_sequence_and_tags():
+    """FDPS's call order: send_flag=true, then walk batches with retrieve in
+    between, several tags outstanding (src/simd_test.cxx:148-155)."""
+    wb, _ = load_golden("plummer2048_walks")
+    o = oracle.force(wb)
+    rec = gpuforce.Records(wb)
+    gpuforce.set_precision(PGF_PRECISION_MIXED)
+    f = gpuforce.CalcForceWithLinearCutoffCUDAMultiWalk(0, wb.eps2, wb.rcut2, wb.G)
+    f(0, 0, None, None, None, None, None, None, rec.epj, rec.epj.size, rec.spj, rec.spj.size, True)
+    halves = [np.arange(0, wb.n_walk // 2), np.arange(wb.n_walk // 2, wb.n_walk)]
+    for tag, ws in enumerate(halves):
+        f(tag + 2, ws.size, rec.p_epi[ws], rec.n_epi[ws], rec.p_id_epj[ws], rec.n_epj[ws], rec.p_id_spj[ws],
+          rec.n_spj[ws], None, 0, None, 0, False)
+    for tag, ws in enumerate(halves):
+        gpuforce.RetrieveForceCUDA(tag + 2, ws.size, rec.n_epi[ws], rec.p_force[ws])
+    np.testing.assert_array_equal(rec.force["n_ngb"], o["nnb"])
+    assert rel_err_vec(rec.force["acc"], o["acc"]).max() < MIXED_MAX
+
+
+def test_retrieve_errors():
+    wb, _ = load_golden("kernel_test")
+    rec = gpuforce.Records(wb)
+    gpuforce.dispatch(rec, tag=4)
+    with pytest.raises(gpuforce.GpuForceError) as e:
+        gpuforce.RetrieveForceCUDA(4, rec.n_walk, rec.n_epi + 1, rec.p_force)
+    assert e.value.code == 1
+    gpuforce.RetrieveForceCUDA(4, rec.n_walk, rec.n_epi, rec.p_force)
+    with pytest.raises(gpuforce.GpuForceError) as e:
+        gpuforce.RetrieveForceCUDA(4, rec.n_walk, rec.n_epi, rec.p_force)
+    assert e.value.code == 4
+
+
+def test_bad_id_rejected():
+    wb, _ = load_golden("kernel_test")
+    wb.id_epj = wb.id_epj.copy()
+    wb.id_epj[5] = wb.epj_mass.size  # one past the end
+    with pytest.raises(gpuforce.GpuForceError) as e:
+        gpuforce.compute(wb)
+    assert e.value.code == 1
+
+
+def test_recompute_reproduces():
+    wb, _ = load_golden("plummer2048_walks")
+    rec = gpuforce.Records(wb)
+    gpuforce.set_precision(PGF_PRECISION_MIXED)
+    gpuforce.dispatch(rec, tag=0)
+    a = gpuforce.retrieve(rec, tag=0).copy()
+    gpuforce.recompute(0)
+    b = gpuforce.retrieve(rec, tag=0).copy()
+    np.testing.assert_array_equal(a["n_ngb"], b["n_ngb"])
+    np.testing.assert_array_equal(a["acc"], b["acc"])
