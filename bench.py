@@ -73,6 +73,69 @@ def make_workload(name: str, rank: int):
     return cl, wb
 
 
+class NvmlSampler:
+    """SM clock and clock-event reasons every 2 ms through NVML (ctypes), in a
+    background thread, while running."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, pci_bus_id: str | None, index: int):
+        import ctypes
+        import threading
+        self.ok = False
+        self.samples, self.reasons, self.max_mhz = [], set(), None
+        try:
+            self.nvml = ctypes.CDLL("libnvidia-ml.so.1")
+            if self.nvml.nvmlInit_v2() != 0:
+                return
+            self.h = ctypes.c_void_p()
+            rc = 1
+            if pci_bus_id:
+                rc = self.nvml.nvmlDeviceGetHandleByPciBusId_v2(pci_bus_id.encode(), ctypes.byref(self.h))
+            if rc != 0:
+                rc = self.nvml.nvmlDeviceGetHandleByIndex_v2(index, ctypes.byref(self.h))
+            if rc != 0:
+                return
+            mx = ctypes.c_uint()
+            if self.nvml.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(mx)) == 0:
+                self.max_mhz = mx.value
+            self.reason_fn = getattr(self.nvml, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                getattr(self.nvml, "nvmlDeviceGetCurrentClocksThrottleReasons", None)
+            self.ok = True
+        except (OSError, AttributeError):
+            return
+        self._stop = threading.Event()
+        self._thread = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        import ctypes
+        clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self._stop.is_set():
+            if self.nvml.nvmlDeviceGetClockInfo(self.h, 1, ctypes.byref(clk)) == 0:
+                self.samples.append(clk.value)
+            if self.reason_fn is not None and self.reason_fn(self.h, ctypes.byref(rs)) == 0:
+                for bit, name in self.REASONS.items():
+                    if rs.value & bit:
+                        self.reasons.add(name)
+            time.sleep(0.002)
+
+    def __enter__(self):
+        if self.ok:
+            self._thread.start()
+        return self
+
+    def __exit__(self, *exc):
+        if self.ok:
+            self._stop.set()
+            self._thread.join()
+
+    def summary(self) -> dict | None:
+        if not self.ok or not self.samples:
+            return None
+        return {"sm_mhz": statistics.median(self.samples), "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(self.reasons), "samples": len(self.samples), "source": "nvml"}
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples every 200 ms while running."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -268,7 +331,10 @@ def run_ours(args):
     n_int = n_epep + n_epsp
     flops = FLOPS_EPEP * n_epep + FLOPS_EPSP * n_epsp
     rec = gpuforce.Records(wb)
-    stream = torch.cuda.current_stream()
+    # A dedicated (non-default) stream: the library launches on it and the
+    # CUDA events below are recorded on it.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     gpuforce.CalcForceWithLinearCutoffCUDAMultiWalk(local, wb.eps2, wb.rcut2, wb.G)
     gpuforce.set_stream(stream.cuda_stream)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
@@ -286,7 +352,11 @@ def run_ours(args):
     main_ms = []
     barrier()
     wall0 = time.time()
-    with ClockSampler(torch.cuda.current_device()) as clk:
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    bus = getattr(props, "pci_bus_id", None)
+    bus = f"{getattr(props, 'pci_domain_id', 0):08x}:{bus:02x}:{getattr(props, 'pci_device_id', 0):02x}.0" \
+        if isinstance(bus, int) else bus
+    with NvmlSampler(bus, torch.cuda.current_device()) as nv, ClockSampler(torch.cuda.current_device()) as clk:
         for e0, e1 in evs:
             flush.zero_()
             e0.record(stream)
@@ -300,7 +370,7 @@ def run_ours(args):
     step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
     t_total = max_over_ranks(sum(step_ms) / 1e3)
     value = world * n_int * args.steps / t_total / 1e9
-    clocks = clk.summary()
+    clocks = nv.summary() or clk.summary()
     n_retest = prof["n_retest"] / max(1, prof["n_call"] or args.steps)
 
     # ---- plain FP64 kernel on the same lists ----
@@ -336,15 +406,19 @@ def run_ours(args):
     e2e_t = []
     for k in range(args.warmup + args.steps):
         barrier()
+        if k == args.warmup:
+            gpuforce.clear_profile()
         t = time.time()
         gpuforce.dispatch(rec, tag=0, send=True)
         gpuforce.retrieve(rec, tag=0)
         if k >= args.warmup:
             e2e_t.append(time.time() - t)
     e2e_total = max_over_ranks(sum(e2e_t))
+    bd = gpuforce.get_profile()
     e2e = {"value": world * n_int * args.steps / e2e_total / 1e9, "unit": "Ginteractions/s",
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-           "ms_per_step": 1e3 * e2e_total / args.steps}
+           "ms_per_step": 1e3 * e2e_total / args.steps,
+           "breakdown_ms_per_step": {k: 1e3 * bd[k] / args.steps for k in ("copy", "send", "calc", "recv")}}
 
     if rank != 0:
         torch.distributed.barrier()

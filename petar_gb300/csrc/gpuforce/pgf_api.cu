@@ -105,12 +105,12 @@ struct TagState {
     DevBuf<EpiDev> epi;
     DevBuf<int32_t> id_epj, id_spj, order;
     DevBuf<WalkDesc> walks;
-    DevBuf<double4> accp;
+    DevBuf<Accp> accp;
     DevBuf<int32_t> nnb;
     HostBuf<EpiDev> h_epi;
     HostBuf<int32_t> h_id_epj, h_id_spj, h_order;
     HostBuf<WalkDesc> h_walks;
-    HostBuf<double4> h_accp;
+    HostBuf<Accp> h_accp;
     HostBuf<int32_t> h_nnb;
     HostBuf<int32_t> h_flags;  // err, n_retest
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -128,14 +128,14 @@ struct State {
     double eps2 = 0, rcut2 = 0, G = 1;
     int precision = PGF_PRECISION_MIXED;
     // shared j data
-    DevBuf<EpjDev> epj;
-    DevBuf<double> epj_rs;
-    DevBuf<float> epj_rs2f;
-    DevBuf<SpjDev> spj;
-    HostBuf<EpjDev> h_epj;
-    HostBuf<double> h_epj_rs;
-    HostBuf<float> h_epj_rs2f;
-    HostBuf<SpjDev> h_spj;
+    DevBuf<EpjMix> epj;
+    DevBuf<double> epj_m64, epj_rs64;
+    DevBuf<SpjMix> spj;
+    DevBuf<SpjQ64> spj_q64;
+    HostBuf<EpjMix> h_epj;
+    HostBuf<double> h_epj_m64, h_epj_rs64;
+    HostBuf<SpjMix> h_spj;
+    HostBuf<SpjQ64> h_spj_q64;
     int64_t n_epj_tot = 0, n_spj_tot = 0;
     bool j_sent = false;
     // scratch
@@ -184,6 +184,13 @@ int setup_device(int rank) {
     return PGF_OK;
 }
 
+// Smallest float not below v (v >= 0).
+inline float round_up(double v) {
+    float f = (float)v;
+    if ((double)f < v) f = std::nextafter(f, HUGE_VALF);
+    return f;
+}
+
 inline const double* dptr(const void* base, size_t off) {
     return reinterpret_cast<const double*>(reinterpret_cast<const char*>(base) + off);
 }
@@ -201,49 +208,72 @@ int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, co
     PGF_CUDA(cudaStreamSynchronize(g.stream));
     const double t0 = now_s();
     PGF_CUDA(g.h_epj.ensure(n_epj));
-    PGF_CUDA(g.h_epj_rs.ensure(n_epj));
-    PGF_CUDA(g.h_epj_rs2f.ensure(n_epj));
+    PGF_CUDA(g.h_epj_m64.ensure(n_epj));
+    PGF_CUDA(g.h_epj_rs64.ensure(n_epj));
     PGF_CUDA(g.h_spj.ensure(n_spj));
+    PGF_CUDA(g.h_spj_q64.ensure(n_spj));
     PGF_CUDA(g.epj.ensure(n_epj));
-    PGF_CUDA(g.epj_rs.ensure(n_epj));
-    PGF_CUDA(g.epj_rs2f.ensure(n_epj));
+    PGF_CUDA(g.epj_m64.ensure(n_epj));
+    PGF_CUDA(g.epj_rs64.ensure(n_epj));
     PGF_CUDA(g.spj.ensure(n_spj));
+    PGF_CUDA(g.spj_q64.ensure(n_spj));
 #pragma omp parallel for schedule(static)
     for (int64_t j = 0; j < n_epj; ++j) {
         const char* r = reinterpret_cast<const char*>(epj) + j * el->size;
         const double* p = dptr(r, el->off_pos);
         const double rs = *dptr(r, el->off_r_search);
-        g.h_epj.h[j] = EpjDev{p[0], p[1], p[2], *dptr(r, el->off_mass)};
-        g.h_epj_rs.h[j] = rs;
-        g.h_epj_rs2f.h[j] = (float)(rs * rs);
+        const double m = *dptr(r, el->off_mass);
+        g.h_epj.h[j] = EpjMix{p[0], p[1], p[2], (float)m, (float)(rs * rs)};
+        g.h_epj_m64.h[j] = m;
+        g.h_epj_rs64.h[j] = rs;
     }
 #pragma omp parallel for schedule(static)
     for (int64_t j = 0; j < n_spj; ++j) {
         const char* r = reinterpret_cast<const char*>(spj) + j * sl->size;
         const double* p = dptr(r, sl->off_pos);
-        SpjDev s;
+        const double m = *dptr(r, sl->off_mass);
+        double q[6] = {0, 0, 0, 0, 0, 0};
+        if (sl->has_quad) {
+            const double* qq = dptr(r, sl->off_quad);
+            for (int k = 0; k < 6; ++k) q[k] = qq[k];
+        }
+        // Traceless form in FP64, then rounded once (see pgf_kernels_mixed.cu).
+        const double tr = q[0] + q[1] + q[2];
+        SpjMix s;
         s.x = p[0];
         s.y = p[1];
         s.z = p[2];
-        s.m = *dptr(r, sl->off_mass);
-        if (sl->has_quad) {
-            const double* q = dptr(r, sl->off_quad);
-            for (int k = 0; k < 6; ++k) s.q[k] = q[k];
-        } else {
-            for (int k = 0; k < 6; ++k) s.q[k] = 0.0;
-        }
+        s.m = (float)m;
+        s.pad0 = 0.f;
+        s.Q[0] = (float)(3.0 * q[0] - tr);
+        s.Q[1] = (float)(3.0 * q[1] - tr);
+        s.Q[2] = (float)(3.0 * q[2] - tr);
+        s.Q[3] = (float)(3.0 * q[3]);
+        s.Q[4] = (float)(3.0 * q[4]);
+        s.Q[5] = (float)(3.0 * q[5]);
+        s.tr = (float)tr;
+        s.pad1 = 0.f;
         g.h_spj.h[j] = s;
+        SpjQ64 d;
+        d.m = m;
+        for (int k = 0; k < 6; ++k) d.q[k] = q[k];
+        d.pad = 0.0;
+        g.h_spj_q64.h[j] = d;
     }
     g.prof.copy += now_s() - t0;
     PGF_CUDA(cudaEventRecord(g.ev_send0, g.stream));
     if (n_epj) {
-        PGF_CUDA(cudaMemcpyAsync(g.epj.d, g.h_epj.h, n_epj * sizeof(EpjDev), cudaMemcpyHostToDevice, g.stream));
-        PGF_CUDA(cudaMemcpyAsync(g.epj_rs.d, g.h_epj_rs.h, n_epj * sizeof(double), cudaMemcpyHostToDevice, g.stream));
-        PGF_CUDA(cudaMemcpyAsync(g.epj_rs2f.d, g.h_epj_rs2f.h, n_epj * sizeof(float), cudaMemcpyHostToDevice,
+        PGF_CUDA(cudaMemcpyAsync(g.epj.d, g.h_epj.h, n_epj * sizeof(EpjMix), cudaMemcpyHostToDevice, g.stream));
+        PGF_CUDA(cudaMemcpyAsync(g.epj_m64.d, g.h_epj_m64.h, n_epj * sizeof(double), cudaMemcpyHostToDevice,
+                                 g.stream));
+        PGF_CUDA(cudaMemcpyAsync(g.epj_rs64.d, g.h_epj_rs64.h, n_epj * sizeof(double), cudaMemcpyHostToDevice,
                                  g.stream));
     }
-    if (n_spj)
-        PGF_CUDA(cudaMemcpyAsync(g.spj.d, g.h_spj.h, n_spj * sizeof(SpjDev), cudaMemcpyHostToDevice, g.stream));
+    if (n_spj) {
+        PGF_CUDA(cudaMemcpyAsync(g.spj.d, g.h_spj.h, n_spj * sizeof(SpjMix), cudaMemcpyHostToDevice, g.stream));
+        PGF_CUDA(cudaMemcpyAsync(g.spj_q64.d, g.h_spj_q64.h, n_spj * sizeof(SpjQ64), cudaMemcpyHostToDevice,
+                                 g.stream));
+    }
     PGF_CUDA(cudaEventRecord(g.ev_send1, g.stream));
     PGF_CUDA(cudaEventSynchronize(g.ev_send1));
     float ms = 0;
@@ -338,12 +368,14 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
 #pragma omp parallel for schedule(dynamic, 4) reduction(max : bad_id)
     for (int w = 0; w < n_walk; ++w) {
         double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+        double rs_max = 0.0;
         const char* base = reinterpret_cast<const char*>(epi[w]);
         for (int i = 0; i < n_epi[w]; ++i) {
             const char* r = base + (size_t)i * il->size;
             const double* p = dptr(r, il->off_pos);
             EpiDev e{p[0], p[1], p[2], *dptr(r, il->off_r_search)};
             t.h_epi.h[idisp[w] + i] = e;
+            rs_max = std::max(rs_max, e.rs);
             for (int d = 0; d < 3; ++d) {
                 lo[d] = std::min(lo[d], p[d]);
                 hi[d] = std::max(hi[d], p[d]);
@@ -370,9 +402,17 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
             d.cx = 0.5 * (lo[0] + hi[0]);
             d.cy = 0.5 * (lo[1] + hi[1]);
             d.cz = 0.5 * (lo[2] + hi[2]);
+            // Half-extents about the centre and the largest r_search, rounded
+            // up so the kernel's far-field classification stays conservative.
+            d.hx = round_up(std::max(hi[0] - d.cx, d.cx - lo[0]));
+            d.hy = round_up(std::max(hi[1] - d.cy, d.cy - lo[1]));
+            d.hz = round_up(std::max(hi[2] - d.cz, d.cz - lo[2]));
+            d.rs_max = round_up(rs_max);
         } else {
             d.cx = d.cy = d.cz = 0.0;
+            d.hx = d.hy = d.hz = d.rs_max = 0.f;
         }
+        d.pad[0] = d.pad[1] = d.pad[2] = d.pad[3] = 0.f;
         d.rcut2 = g.walk_rcut2.empty() ? g.rcut2 : g.walk_rcut2[w];
         t.h_walks.h[w] = d;
     }
@@ -408,9 +448,10 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     p = Params{};
     p.epi = t.epi.d;
     p.epj = g.epj.d;
-    p.epj_rs = g.epj_rs.d;
-    p.epj_rs2f = g.epj_rs2f.d;
+    p.epj_m64 = g.epj_m64.d;
+    p.epj_rs64 = g.epj_rs64.d;
     p.spj = g.spj.d;
+    p.spj_q64 = g.spj_q64.d;
     p.id_epj = t.id_epj.d;
     p.id_spj = t.id_spj.d;
     p.walks = t.walks.d;
@@ -572,7 +613,7 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
     cudaStream_t s = g.stream;
     PGF_CUDA(cudaEventRecord(t.ev[4], s));
     if (n) {
-        PGF_CUDA(cudaMemcpyAsync(t.h_accp.h, t.accp.d, n * sizeof(double4), cudaMemcpyDeviceToHost, s));
+        PGF_CUDA(cudaMemcpyAsync(t.h_accp.h, t.accp.d, n * sizeof(Accp), cudaMemcpyDeviceToHost, s));
         PGF_CUDA(cudaMemcpyAsync(t.h_nnb.h, t.nnb.d, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     }
     PGF_CUDA(cudaMemcpyAsync(t.h_flags.h, g.scratch.d, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
@@ -592,7 +633,7 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
         const int64_t o = t.epi_disp[w];
         for (int i = 0; i < ni[w]; ++i) {
             char* r = base + (size_t)i * fl->size;
-            const double4 a = t.h_accp.h[o + i];
+            const Accp a = t.h_accp.h[o + i];
             double* acc = reinterpret_cast<double*>(r + fl->off_acc);
             acc[0] = a.x;
             acc[1] = a.y;
@@ -659,13 +700,15 @@ int pgf_finalize(void) {
         t.dispatched = t.has_data = false;
     }
     g.epj.release();
-    g.epj_rs.release();
-    g.epj_rs2f.release();
+    g.epj_m64.release();
+    g.epj_rs64.release();
     g.spj.release();
+    g.spj_q64.release();
     g.h_epj.release();
-    g.h_epj_rs.release();
-    g.h_epj_rs2f.release();
+    g.h_epj_m64.release();
+    g.h_epj_rs64.release();
     g.h_spj.release();
+    g.h_spj_q64.release();
     g.scratch.release();
     g.retest.release();
     if (g.ev_send0) cudaEventDestroy(g.ev_send0);

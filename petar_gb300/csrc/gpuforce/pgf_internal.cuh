@@ -1,41 +1,58 @@
 // Device data layout and kernel interfaces of the soft-force library.
 //
 // HBM layout (one copy per process, grown on demand, never shrunk):
-//   EpjDev[n_epj_tot]    32 B: FP64 position and mass
-//   epj_rs[n_epj_tot]     8 B: FP64 r_search (exact neighbour tests)
-//   epj_rs2f[n_epj_tot]   4 B: (float)(r_search^2), the square taken in FP64
-//   SpjDev[n_spj_tot]    80 B: FP64 position, mass and raw quadrupole
+//   EpjMix[n_epj_tot]    32 B: FP64 position, FP32 mass, FP32 r_search^2
+//   epj_m64[n_epj_tot]    8 B: FP64 mass       (plain FP64 kernel)
+//   epj_rs64[n_epj_tot]   8 B: FP64 r_search   (plain FP64 kernel, exact re-tests)
+//   SpjMix[n_spj_tot]    64 B: FP64 position, FP32 mass, FP32 traceless
+//                              quadrupole Q = 3q - tr(q) I and tr(q)
+//   SpjQ64[n_spj_tot]    64 B: FP64 mass and raw quadrupole (plain FP64 kernel)
 //   EpiDev[ni_tot]       32 B: FP64 position and r_search
 //   id_epj / id_spj      int32 per list entry, walks concatenated
-//   WalkDesc[n_walk]     64 B: list offsets, walk centre (FP64), r_out^2
+//   WalkDesc[n_walk]     96 B: list offsets, walk centre (FP64), box
+//                              half-extents, largest i r_search, r_out^2
 //   order[n_walk]        walks sorted by descending work (the work queue)
-//   out_accp[ni_tot]     double4: acc.xyz, pot (G applied)
+//   out_accp[ni_tot]     Accp (32 B): acc.xyz, pot (G applied)
 //   out_nnb[ni_tot]      int32 neighbour count
-// The EPJ and SPJ arrays of a 1.5M-particle problem (about 60 MB + 23 MB)
-// stay resident in the 129 MB L2 while the id lists stream from HBM once.
+// The j arrays of a 1.5M-particle problem (about 50 MB EPJ + 18 MB SPJ for the
+// mixed kernel) stay resident in the 129 MB L2 while the id lists stream from
+// HBM once per force evaluation.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
 
 namespace pgf {
 
-struct __align__(32) EpjDev {
-    double x, y, z, m;
+struct __align__(32) EpjMix {
+    double x, y, z;
+    float m;
+    float rs2;  // (float)(r_search * r_search), the square taken in FP64
 };
-static_assert(sizeof(EpjDev) == 32, "EpjDev layout");
+static_assert(sizeof(EpjMix) == 32, "EpjMix layout");
 
-struct __align__(16) SpjDev {
-    double x, y, z, m;
-    double q[6];  // xx, yy, zz, xy, xz, yz (zero for monopole superparticles)
+struct __align__(32) SpjMix {
+    double x, y, z;
+    float m;
+    float pad0;
+    float Q[6];  // traceless 3q - tr(q) I: xx, yy, zz, xy, xz, yz
+    float tr;    // tr(q)
+    float pad1;
 };
-static_assert(sizeof(SpjDev) == 80, "SpjDev layout");
+static_assert(sizeof(SpjMix) == 64, "SpjMix layout");
+
+struct __align__(16) SpjQ64 {
+    double m;
+    double q[6];  // raw second moment: xx, yy, zz, xy, xz, yz (zero for monopoles)
+    double pad;
+};
+static_assert(sizeof(SpjQ64) == 64, "SpjQ64 layout");
 
 struct __align__(32) EpiDev {
     double x, y, z, rs;
 };
 static_assert(sizeof(EpiDev) == 32, "EpiDev layout");
 
-struct __align__(16) WalkDesc {
+struct __align__(32) WalkDesc {
     int64_t epj_begin;  // offset of the walk's EPJ ids in id_epj
     int64_t spj_begin;  // offset of the walk's SPJ ids in id_spj
     int32_t i_begin;    // first EPI row of the walk
@@ -44,11 +61,20 @@ struct __align__(16) WalkDesc {
     int32_t n_spj;
     double cx, cy, cz;  // walk centre: centre of the EPI bounding box
     double rcut2;       // r_out^2 of the walk
+    float hx, hy, hz;   // EPI box half-extents, rounded up
+    float rs_max;       // largest r_search of the walk's EPI, rounded up
+    float pad[4];
 };
-static_assert(sizeof(WalkDesc) == 64, "WalkDesc layout");
+static_assert(sizeof(WalkDesc) == 96, "WalkDesc layout");
 
-// A pair range whose FP32 neighbour test came within rounding distance of
-// r_search: the retest kernel recounts it in FP64.
+// Result of one i-particle: acceleration and potential with G applied.
+struct __align__(32) Accp {
+    double x, y, z, w;
+};
+static_assert(sizeof(Accp) == 32, "Accp layout");
+
+// An (i, EPJ tile) whose FP32 neighbour test came within rounding distance of
+// r_search for some pair: the retest kernel recounts the tile in FP64.
 struct Retest {
     int64_t j_begin;  // offset in id_epj
     int32_t i;        // EPI row
@@ -57,10 +83,11 @@ struct Retest {
 
 struct Params {
     const EpiDev* epi;
-    const EpjDev* epj;
-    const double* epj_rs;
-    const float* epj_rs2f;
-    const SpjDev* spj;
+    const EpjMix* epj;
+    const double* epj_m64;
+    const double* epj_rs64;
+    const SpjMix* spj;
+    const SpjQ64* spj_q64;
     const int32_t* id_epj;
     const int32_t* id_spj;
     const WalkDesc* walks;
@@ -69,7 +96,7 @@ struct Params {
     int32_t pad0;
     double eps2;
     double G;
-    double4* out_accp;
+    Accp* out_accp;
     int32_t* out_nnb;
     // scratch
     int32_t* queue_head;   // work-queue cursor, zeroed before each launch

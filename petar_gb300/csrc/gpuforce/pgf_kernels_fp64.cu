@@ -46,12 +46,12 @@ __global__ __launch_bounds__(kT) void fp64_kernel(Params p) {
                 __syncthreads();
                 if (tid < nt) {
                     const int id = p.id_epj[wd.epj_begin + t0 + tid];
-                    const EpjDev j = p.epj[id];
+                    const EpjMix j = p.epj[id];
                     sx[tid] = j.x;
                     sy[tid] = j.y;
                     sz[tid] = j.z;
-                    sm[tid] = j.m;
-                    srs[tid] = p.epj_rs[id];
+                    sm[tid] = p.epj_m64[id];
+                    srs[tid] = p.epj_rs64[id];
                 }
                 __syncthreads();
                 if (valid) {
@@ -81,12 +81,13 @@ __global__ __launch_bounds__(kT) void fp64_kernel(Params p) {
                 __syncthreads();
                 if (tid < nt) {
                     const int id = p.id_spj[wd.spj_begin + t0 + tid];
-                    const SpjDev j = p.spj[id];
+                    const SpjMix j = p.spj[id];
+                    const SpjQ64 q = p.spj_q64[id];
                     sx[tid] = j.x;
                     sy[tid] = j.y;
                     sz[tid] = j.z;
-                    sm[tid] = j.m;
-                    for (int c = 0; c < 6; ++c) sq[c][tid] = j.q[c];
+                    sm[tid] = q.m;
+                    for (int c = 0; c < 6; ++c) sq[c][tid] = q.q[c];
                 }
                 __syncthreads();
                 if (valid) {
@@ -120,7 +121,7 @@ __global__ __launch_bounds__(kT) void fp64_kernel(Params p) {
             if (valid) {
                 const double G = p.G;
                 const int gi = wd.i_begin + li;
-                p.out_accp[gi] = make_double4(G * ax + G * bx, G * ay + G * by, G * az + G * bz, G * pe + G * ps);
+                p.out_accp[gi] = Accp{G * ax + G * bx, G * ay + G * by, G * az + G * bz, G * pe + G * ps};
                 p.out_nnb[gi] = nnb;
             }
         }

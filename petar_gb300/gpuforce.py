@@ -18,6 +18,7 @@ CPU fallback: without the compiled library or a GPU every call fails.
 from __future__ import annotations
 
 import ctypes
+import os
 from pathlib import Path
 
 import numpy as np
@@ -100,6 +101,9 @@ def load(build: bool = True) -> ctypes.CDLL:
     if _LIB is not None:
         return _LIB
     path = library_path()
+    override = os.environ.get("PETAR_GPUFORCE_LIB")
+    if override:
+        path, build = Path(override), False
     if build:
         from .build import build_gpuforce
         path = build_gpuforce()
@@ -244,9 +248,10 @@ class CalcForceWithLinearCutoffCUDA:
         n_epi = np.ascontiguousarray(n_epi, dtype=np.int32)
         n_epj = np.ascontiguousarray(n_epj, dtype=np.int32)
         n_spj = np.ascontiguousarray(n_spj, dtype=np.int32)
-        _check(lib.pgf_dispatch(tag, int(n_walk), _ptr(_ptr_table(epi)), _ptr(n_epi), ctypes.byref(el),
-                                _ptr(_ptr_table(epj)), _ptr(n_epj), ctypes.byref(jl), _ptr(_ptr_table(spj)),
-                                _ptr(n_spj), ctypes.byref(sl)))
+        # The pointer tables must stay referenced until the call returns.
+        pe, pj, ps = _ptr_table(epi), _ptr_table(epj), _ptr_table(spj)
+        _check(lib.pgf_dispatch(tag, int(n_walk), _ptr(pe), _ptr(n_epi), ctypes.byref(el), _ptr(pj), _ptr(n_epj),
+                                ctypes.byref(jl), _ptr(ps), _ptr(n_spj), ctypes.byref(sl)))
         return 0
 
 
