@@ -62,6 +62,23 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """Largest value of x over all ranks (the step time that bounds the job)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(interactions_per_rank: int, steps: int, t_max_s: float, world: int) -> float:
+    """Whole-job Ginteractions/s: every rank evaluates its own replica, so the
+    job does world x interactions per step in the slowest rank's time."""
+    return world * interactions_per_rank * steps / t_max_s / 1e9
+
+
 def make_workload(name: str, rank: int):
     from petar_gb300 import ics, walks
     w = WORKLOADS[name]
@@ -319,13 +336,6 @@ def run_ours(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
-
     cl, wb = make_workload(args.workload, rank)
     n_epep, n_epsp = wb.interactions()
     n_int = n_epep + n_epsp
@@ -368,8 +378,8 @@ def run_ours(args):
     wall = time.time() - wall0
     prof = gpuforce.get_profile()
     step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
-    t_total = max_over_ranks(sum(step_ms) / 1e3)
-    value = world * n_int * args.steps / t_total / 1e9
+    t_total = max_over_ranks(sum(step_ms) / 1e3, world)
+    value = job_throughput(n_int, args.steps, t_total, world)
     clocks = nv.summary() or clk.summary()
     n_retest = prof["n_retest"] / max(1, prof["n_call"] or args.steps)
 
@@ -388,7 +398,7 @@ def run_ours(args):
             e1.record(stream)
             gpuforce.wait(0)
             ts.append(e0.elapsed_time(e1))
-        t64 = max_over_ranks(statistics.mean(ts) / 1e3)
+        t64 = max_over_ranks(statistics.mean(ts) / 1e3, world)
         v64 = world * n_int / t64 / 1e9
         ea = np.linalg.norm(f_mixed["acc"] - f64["acc"], axis=1) / np.linalg.norm(f64["acc"], axis=1)
         ep = np.abs(f_mixed["pot"] - f64["pot"]) / np.abs(f64["pot"])
@@ -413,7 +423,7 @@ def run_ours(args):
         gpuforce.retrieve(rec, tag=0)
         if k >= args.warmup:
             e2e_t.append(time.time() - t)
-    e2e_total = max_over_ranks(sum(e2e_t))
+    e2e_total = max_over_ranks(sum(e2e_t), world)
     bd = gpuforce.get_profile()
     e2e = {"value": world * n_int * args.steps / e2e_total / 1e9, "unit": "Ginteractions/s",
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
