@@ -155,6 +155,60 @@ int pgf_clear_profile(void);
 /* Message for the last failure ("" when none). */
 const char *pgf_last_error(void);
 
+/* ---- Allocation-free variant (no counterpart in the reference) ----
+ *
+ * For callers that cannot let a library allocate device memory: codes that
+ * carve all device memory out of one arena they size at start-up, or loops
+ * that cannot pay for the device-wide synchronisation cudaMalloc and cudaFree
+ * imply.  The caller passes inputs and outputs already in device memory in
+ * the formats below; the function itself calls no cudaMalloc, cudaFree or
+ * other allocating routine.
+ *
+ * The mixed-precision kernels still need scratch (walk descriptors, work
+ * order, queue cursor, FP64 re-test records).  It lives in one static device
+ * array of about 2.6 MB that every GPU loading the library keeps until the
+ * process exits, sized for at most PGF_NOALLOC_MAX_WALKS walks per call;
+ * larger calls return PGF_ERR_CAPACITY.  The first call on each device looks
+ * up that array's device address (with the device current); make that first
+ * call before any stream capture.  All calls share the array: calls on one
+ * stream are ordered and safe, calls whose work overlaps on the GPU (other
+ * streams, other host threads) race and corrupt each other's results.
+ *
+ * walk_table: 6 int64 per walk: i_begin, n_i, epj_begin, n_epj, spj_begin,
+ *   n_spj (rows of epi; offsets into id_epj / id_spj).
+ * epi: 4 doubles per i-particle: x, y, z, r_search.
+ * epj: pgf_epj_device records; epj_r_search: the FP64 r_search of each.
+ * spj: pgf_spj_device records.
+ * accp: 4 doubles per i-particle: acc x, y, z, pot (G applied); n_ngb: one
+ *   int per i-particle.  Rows that no walk covers are left untouched.
+ * epi, epj, spj and accp must be 32-byte aligned.  Walk rows and ids are
+ * checked on the device before the force kernels start (the call waits for
+ * that check); the force kernels themselves are left running on the stream
+ * (a cudaStream_t passed as void*; NULL is the legacy default stream).
+ * errbuf (optional, errbuf_len bytes) receives a message on failure. */
+#define PGF_NOALLOC_MAX_WALKS 16384
+
+typedef struct pgf_epj_device { /* 32 bytes */
+    double pos[3];
+    float mass;
+    float r_search2;      /* (float)(r_search * r_search), the square taken in double */
+} pgf_epj_device;
+
+typedef struct pgf_spj_device { /* 64 bytes */
+    double pos[3];
+    float mass;
+    float pad0;
+    float quad_traceless[6]; /* 3q - tr(q) I of the raw second moment q: xx, yy, zz, xy, xz, yz */
+    float trace;             /* tr(q) */
+    float pad1;
+} pgf_spj_device;
+
+int pgf_force_device_noalloc(int n_walk, const int64_t *walk_table, const double *epi, int64_t n_epi_total,
+                             const pgf_epj_device *epj, const double *epj_r_search, int64_t n_epj_total,
+                             const pgf_spj_device *spj, int64_t n_spj_total, const int *id_epj, int64_t n_id_epj,
+                             const int *id_spj, int64_t n_id_spj, double eps2, double rcut2, double G,
+                             double *accp, int *n_ngb, void *cuda_stream, char *errbuf, size_t errbuf_len);
+
 /* Releases device and pinned host memory. */
 int pgf_finalize(void);
 
