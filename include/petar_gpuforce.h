@@ -104,6 +104,20 @@ int pgf_initialize(int rank, double eps2, double rcut2, double G);
 /* Chooses the kernel used by later dispatches (PGF_PRECISION_*). */
 int pgf_set_precision(int precision);
 
+/* Mixed-precision kernel variants: 0 is the CTA-synchronous tiled kernel;
+ * 1..PGF_NUM_KERNEL_VARIANTS-1 are warp-specialised producer/consumer kernels
+ * with different consumer-warp counts and i-particles per thread.  The
+ * choice applies to later dispatches. */
+#define PGF_NUM_KERNEL_VARIANTS 5
+int pgf_set_kernel_variant(int variant);
+int pgf_get_kernel_variant(int *variant);
+
+/* Autotuner: times every kernel variant `repeats` times on the data of the
+ * tag's last index dispatch (already on the device), keeps the fastest for
+ * later dispatches and reports it and its mean main-kernel time.  The results
+ * of the tag are those of the last variant run; retrieve after a recompute. */
+int pgf_autotune(int tag, int repeats, int *best_variant, double *best_ms);
+
 /* Launch on the caller's CUDA stream (a cudaStream_t passed as void*);
  * NULL restores the library's own stream. */
 int pgf_set_stream(void *cuda_stream);

@@ -57,6 +57,7 @@ GPU_SOURCES = [
     "gpuforce/pgf_api.cu",
     "gpuforce/pgf_kernels_fp64.cu",
     "gpuforce/pgf_kernels_mixed.cu",
+    "gpuforce/pgf_kernels_ws.cu",
     "gpuforce/pgf_noalloc.cu",
 ]
 GPU_HEADERS = [

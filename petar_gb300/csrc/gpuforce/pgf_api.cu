@@ -29,6 +29,7 @@ namespace {
 using namespace pgf;
 
 constexpr int kMaxTags = 16;
+static_assert(PGF_NUM_KERNEL_VARIANTS == 1 + kNumWsVariants, "variant 0 plus the warp-specialised variants");
 constexpr int64_t kMaxRows = 0x7fffffff;
 
 std::string g_error;
@@ -100,6 +101,7 @@ struct TagState {
     int n_walk = 0;
     int64_t ni_tot = 0;
     int precision = PGF_PRECISION_MIXED;
+    int variant = 0;
     std::vector<int> n_epi;
     std::vector<int64_t> epi_disp;
     DevBuf<EpiDev> epi;
@@ -127,6 +129,7 @@ struct State {
     bool user_stream = false;
     double eps2 = 0, rcut2 = 0, G = 1;
     int precision = PGF_PRECISION_MIXED;
+    int variant = 0;  // mixed-precision kernel variant (pgf_set_kernel_variant)
     // shared j data
     DevBuf<EpjMix> epj;
     DevBuf<double> epj_m64, epj_rs64;
@@ -299,7 +302,7 @@ int launch_tag(TagState& t) {
         if (e == cudaSuccess) e = cudaEventRecord(t.ev[2], g.stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), g.stream);
     } else {
-        e = launch_mixed(p, g.stream, g.num_sms);
+        e = t.variant == 0 ? launch_mixed(p, g.stream, g.num_sms) : launch_ws(p, g.stream, g.num_sms, t.variant - 1);
         if (e == cudaSuccess) e = cudaEventRecord(t.ev[2], g.stream);
         if (e == cudaSuccess && p.n_walk > 0) e = launch_retest(p, g.stream, g.num_sms);
     }
@@ -433,6 +436,7 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     t.n_epi.assign(n_epi, n_epi + n_walk);
     t.epi_disp = idisp;
     t.precision = g.precision;
+    t.variant = g.variant;
     g.prof.copy += now_s() - t0;
 
     cudaStream_t s = g.stream;
@@ -590,7 +594,56 @@ int pgf_recompute(int tag) {
     PGF_CUDA(cudaSetDevice(g.device));
     PGF_CUDA(cudaEventRecord(t.ev[0], g.stream));
     t.precision = g.precision;
+    t.variant = g.variant;
     return launch_tag(t);
+}
+
+int pgf_set_kernel_variant(int variant) {
+    if (variant < 0 || variant >= PGF_NUM_KERNEL_VARIANTS)
+        return fail(PGF_ERR_ARG, "kernel variant %d outside [0, %d)", variant, PGF_NUM_KERNEL_VARIANTS);
+    g.variant = variant;
+    return PGF_OK;
+}
+
+int pgf_get_kernel_variant(int* variant) {
+    if (!variant) return fail(PGF_ERR_ARG, "NULL variant");
+    *variant = g.variant;
+    return PGF_OK;
+}
+
+int pgf_autotune(int tag, int repeats, int* best_variant, double* best_ms) {
+    if (int r = ensure_init()) return r;
+    if (!valid_tag(tag)) return fail(PGF_ERR_ARG, "tag %d outside [0, %d)", tag, kMaxTags);
+    TagState& t = g.tags[tag];
+    if (!t.has_data) return fail(PGF_ERR_STATE, "autotune needs a dispatched tag");
+    if (repeats < 1) repeats = 1;
+    PGF_CUDA(cudaSetDevice(g.device));
+    const int saved_precision = g.precision;
+    g.precision = PGF_PRECISION_MIXED;
+    int best = g.variant;
+    double best_t = HUGE_VAL;
+    for (int v = 0; v < PGF_NUM_KERNEL_VARIANTS; ++v) {
+        g.variant = v;
+        double sum = 0.0;
+        for (int k = 0; k <= repeats; ++k) {  // the first run warms up
+            int r = pgf_recompute(tag);
+            if (r == PGF_OK) r = pgf_wait(tag);
+            if (r != PGF_OK) {
+                g.precision = saved_precision;
+                return r;
+            }
+            if (k > 0) sum += g.prof.last_calc_main;
+        }
+        if (sum < best_t) {
+            best_t = sum;
+            best = v;
+        }
+    }
+    g.variant = best;
+    g.precision = saved_precision;
+    if (best_variant) *best_variant = best;
+    if (best_ms) *best_ms = 1e3 * best_t / repeats;
+    return PGF_OK;
 }
 
 int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const pgf_force_layout* fl) {

@@ -124,5 +124,8 @@ __device__ __forceinline__ int exact_neighbour(double xi, double yi, double zi, 
 cudaError_t launch_fp64(const Params& p, cudaStream_t s, int num_sms);
 cudaError_t launch_mixed(const Params& p, cudaStream_t s, int num_sms);
 cudaError_t launch_retest(const Params& p, cudaStream_t s, int num_sms);
+// Warp-specialised kernel, variants 0..kNumWsVariants-1 (see pgf_kernels_ws.cu).
+constexpr int kNumWsVariants = 4;
+cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant);
 
 }  // namespace pgf

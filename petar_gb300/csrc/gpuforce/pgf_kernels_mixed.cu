@@ -45,14 +45,36 @@
 namespace pgf {
 namespace {
 
-constexpr int kThreads = 256;
+#ifndef PGF_THREADS
+#define PGF_THREADS 256
+#endif
+#ifndef PGF_KI
+#define PGF_KI 2
+#endif
+#ifndef PGF_MINB
+#define PGF_MINB 2
+#endif
+#ifndef PGF_FAR_UNROLL
+#define PGF_FAR_UNROLL 4
+#endif
+#ifndef PGF_NEAR_UNROLL
+#define PGF_NEAR_UNROLL 2
+#endif
+#ifndef PGF_SP_UNROLL
+#define PGF_SP_UNROLL 2
+#endif
+
+constexpr int kThreads = PGF_THREADS;
 constexpr int kWarps = kThreads / 32;
-constexpr int kI = 2;                    // i-particles per thread
+constexpr int kI = PGF_KI;               // i-particles per thread
 constexpr int kMaxPass = kThreads * kI;  // i-particles per pass
 constexpr int kTileEP = kThreads;        // one EPJ per thread per tile
 constexpr int kTileSP = kThreads / 2;    // two threads stage one SPJ
 constexpr int kFlush = 256;              // pairs per thread between FP64 flushes
 constexpr int kKMax = 1 << 22;
+constexpr int kNearUnroll = PGF_NEAR_UNROLL;
+constexpr int kFarUnroll = PGF_FAR_UNROLL;
+constexpr int kSpUnroll = PGF_SP_UNROLL;
 
 __device__ __forceinline__ float rsqrt_approx(float x) {
     float y;
@@ -141,7 +163,7 @@ __device__ __forceinline__ double as_double(unsigned lo, unsigned hi) {
     return __hiloint2double((int)hi, (int)lo);
 }
 
-__global__ __launch_bounds__(kThreads, 2) void mixed_kernel(Params p) {
+__global__ __launch_bounds__(kThreads, PGF_MINB) void mixed_kernel(Params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem& s = *reinterpret_cast<Smem*>(smem_raw);
     const int tid = threadIdx.x;
@@ -331,7 +353,7 @@ __global__ __launch_bounds__(kThreads, 2) void mixed_kernel(Params p) {
                         const int pn = (nn_cur + n_js - 1) / n_js;
                         const int j0 = min(nn_cur, js * pn);
                         const int j1 = min(nn_cur, j0 + pn);
-#pragma unroll 2
+#pragma unroll kNearUnroll
                         for (int j = j0; j < j1; ++j) {
                             const float4 h = s.nh[cur][j];
                             const float4 l = s.nl[cur][j];
@@ -360,7 +382,7 @@ __global__ __launch_bounds__(kThreads, 2) void mixed_kernel(Params p) {
                         const int pf = (nf_cur + n_js - 1) / n_js;
                         const int f0 = min(nf_cur, js * pf);
                         const int f1 = min(nf_cur, f0 + pf);
-#pragma unroll 4
+#pragma unroll kFarUnroll
                         for (int j = f0; j < f1; ++j) {
                             const float4 h = s.fr[cur][j];
 #pragma unroll
@@ -388,7 +410,7 @@ __global__ __launch_bounds__(kThreads, 2) void mixed_kernel(Params p) {
                         const int ps = (nn_cur + n_js - 1) / n_js;
                         const int j0 = min(nn_cur, js * ps);
                         const int j1 = min(nn_cur, j0 + ps);
-#pragma unroll 2
+#pragma unroll kSpUnroll
                         for (int j = j0; j < j1; ++j) {
                             const float4 q0 = s.sp[cur][j][0];
                             const float4 qa = s.sp[cur][j][1];

@@ -1,0 +1,596 @@
+// Warp-specialised mixed-precision soft-force kernel for sm_103a.
+//
+// Same pair arithmetic, precision scheme and outputs as mixed_kernel
+// (pgf_kernels_mixed.cu): walk-relative coordinates formed in FP64 and rounded
+// to FP32, near EPJ with hi/lo coordinates, the linear cutoff and the exact
+// neighbour count, far EPJ as plain gravity, EP-SP with the traceless
+// quadrupole, FP32 partial sums flushed into FP64.  The difference is the
+// data flow inside a CTA:
+//
+// * One producer warp walks the work queue.  For every walk pass it emits a
+//   PASS_BEGIN item, then one item per j tile, then PASS_END.  For a tile it
+//   gathers the EPJ/SPJ records through the id list (L2-resident), forms x - c
+//   in FP64, classifies near/far, compacts with warp ballots and writes the
+//   FP32 tile into a slot of a shared-memory ring.
+// * CW consumer warps take the items in order.  They never stage data and
+//   never wait for each other inside a pass: each waits only for the slot it
+//   needs (mbarrier "full") and releases it when done (mbarrier "empty").  The
+//   producer therefore runs ahead, across walk boundaries, by up to kSlots
+//   items.
+// * Ambiguous neighbour pairs (within the guard band of r_search) are pushed
+//   one by one as Retest records with their own list index, so no thread has
+//   to coordinate its counts with another.
+// * Every mbarrier wait is bounded by 1 s of %globaltimer; on expiry the thread
+//   sets the device error word and returns.  The host reports PGF_ERR_DEVICE.
+#include "pgf_internal.cuh"
+
+namespace pgf {
+namespace {
+
+constexpr int kTileEP = 128;  // EPJ entries per tile (4 per producer lane)
+constexpr int kTileSP = 64;   // SPJ entries per tile (2 per producer lane)
+constexpr int kSlots = 4;     // ring depth
+constexpr int kFlush = 256;   // pairs per consumer thread between FP64 flushes
+constexpr int kKMax = 1 << 22;
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;
+constexpr int kErrWaitTimeout = 1;
+
+enum : int { kItemEP = 0, kItemSP = 1, kItemBegin = 2, kItemEnd = 3, kItemExit = 4 };
+
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// See kband_near in pgf_kernels_mixed.cu for the derivation.
+__device__ __forceinline__ int kband_near(double D, double rs, double eps2) {
+    const double r2ref = rs * rs - eps2;
+    if (!(r2ref > 0.0)) return kKMax;
+    const double k = 48.0 + 1e-5 * D / sqrt(r2ref);
+    return k >= double(kKMax) ? kKMax : int(k) + 1;
+}
+
+__device__ __forceinline__ double as_double(unsigned lo, unsigned hi) {
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile(
+        "{\n\t.reg .b64 st;\n\t"
+        "mbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_addr(bar))
+        : "memory");
+}
+
+// Waits for the phase of the given parity to complete; false after 1 s.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int32_t* err) {
+    const uint32_t a = smem_addr(bar);
+    unsigned done = 0;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    const unsigned long long t0 = globaltimer();
+    for (;;) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (globaltimer() - t0 > kWaitLimitNs) {
+            atomicOr(err, kErrWaitTimeout);
+            return false;
+        }
+    }
+}
+
+// Named barrier among the consumer warps only (the producer never joins).
+__device__ __forceinline__ void consumers_sync(int n_threads) {
+    asm volatile("bar.sync 1, %0;" ::"r"(n_threads) : "memory");
+}
+
+struct SlotEP {
+    float4 nh[kTileEP];  // near: hi x, y, z, m
+    float4 nl[kTileEP];  // near: lo x, y, z, rs2
+    float4 fr[kTileEP];  // far:  hi x, y, z, m
+    int nidx[kTileEP];   // near: entry index in the tile (for re-tests)
+};
+struct SlotSP {
+    float4 sp[kTileSP][3];
+};
+union Slot {
+    SlotEP ep;
+    SlotSP sp;
+};
+struct Hdr {
+    int kind;
+    int nn;     // near entries (EP), entries (SP)
+    int nf;     // far entries (EP)
+    int walk;   // walk index (kItemBegin)
+    int ipass;  // first i of the pass (kItemBegin)
+    int pad;
+    int64_t base;  // first list entry of the tile
+};
+
+template <int CW, int KI>
+struct Smem {
+    Slot slot[kSlots];
+    Hdr hdr[kSlots];
+    uint64_t full[kSlots];
+    uint64_t empty[kSlots];
+    double acc[KI][4][CW * 32];
+    int cnt[KI][CW * 32];
+};
+
+// ---------------------------------------------------------------- producer
+
+template <int CW, int KI>
+__device__ void producer(const Params& p, Smem<CW, KI>& s, int lane) {
+    constexpr int kMaxPass = CW * 32 * KI;
+    const float eps2 = (float)p.eps2;
+    unsigned item = 0;
+    auto acquire = [&](int& sl) -> bool {
+        sl = item % kSlots;
+        const unsigned parity = ((item / kSlots) & 1u) ^ 1u;
+        return mbar_wait(&s.empty[sl], parity, p.err);
+    };
+    auto publish = [&](int sl) {
+        __syncwarp();
+        mbar_arrive(&s.full[sl]);  // 32 arrivals complete the phase
+        ++item;
+    };
+    for (;;) {
+        int w_q = 0;
+        if (lane == 0) w_q = atomicAdd(p.queue_head, 1);
+        w_q = __shfl_sync(0xffffffffu, w_q, 0);
+        if (w_q >= p.n_walk) {
+            int sl;
+            if (!acquire(sl)) return;
+            if (lane == 0) s.hdr[sl].kind = kItemExit;
+            publish(sl);
+            return;
+        }
+        const int widx = p.order[w_q];
+        const WalkDesc wd = p.walks[widx];
+        const double cx = wd.cx, cy = wd.cy, cz = wd.cz;
+        const float rcut2 = (float)wd.rcut2;
+        const float rsmax2 = wd.rs_max * wd.rs_max;
+        const float hmax = fmaxf(wd.hx, fmaxf(wd.hy, wd.hz));
+        const int n_ept = (wd.n_epj + kTileEP - 1) / kTileEP;
+        const int n_spt = (wd.n_spj + kTileSP - 1) / kTileSP;
+        for (int ipass = 0; ipass < wd.n_i; ipass += kMaxPass) {
+            int sl;
+            if (!acquire(sl)) return;
+            if (lane == 0) {
+                s.hdr[sl].kind = kItemBegin;
+                s.hdr[sl].walk = widx;
+                s.hdr[sl].ipass = ipass;
+            }
+            publish(sl);
+            // EPJ tiles: ids and records for 4 entries per lane.
+            for (int t = 0; t < n_ept; ++t) {
+                const int64_t base = wd.epj_begin + (int64_t)t * kTileEP;
+                const int nt = min(kTileEP, wd.n_epj - t * kTileEP);
+                int id[4];
+                uint4 r0[4], r1[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int e = q * 32 + lane;
+                    id[q] = e < nt ? __ldg(p.id_epj + base + e) : -1;
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (id[q] >= 0) {
+                        const uint4* src = reinterpret_cast<const uint4*>(p.epj + id[q]);
+                        r0[q] = __ldg(src);
+                        r1[q] = __ldg(src + 1);
+                    } else {
+                        r0[q] = r1[q] = make_uint4(0, 0, 0, 0);
+                    }
+                }
+                if (!acquire(sl)) return;
+                SlotEP& S = s.slot[sl].ep;
+                int nn = 0, nf = 0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int e = q * 32 + lane;
+                    const bool valid = e < nt;
+                    bool near = false;
+                    float hx = 0.f, hy = 0.f, hz = 0.f, m = 0.f, rs2 = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
+                    if (valid) {
+                        const double dx = as_double(r0[q].x, r0[q].y) - cx;
+                        const double dy = as_double(r0[q].z, r0[q].w) - cy;
+                        const double dz = as_double(r1[q].x, r1[q].y) - cz;
+                        hx = (float)dx;
+                        hy = (float)dy;
+                        hz = (float)dz;
+                        m = __uint_as_float(r1[q].z);
+                        rs2 = __uint_as_float(r1[q].w);
+                        const float ex = fmaxf(fabsf(hx) - wd.hx, 0.f);
+                        const float ey = fmaxf(fabsf(hy) - wd.hy, 0.f);
+                        const float ez = fmaxf(fabsf(hz) - wd.hz, 0.f);
+                        const float dist2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+                        const float R = sqrtf(fmaxf(fmaxf(rsmax2, rs2), rcut2));
+                        const float dmax = fmaxf(fabsf(hx), fmaxf(fabsf(hy), fabsf(hz)));
+                        const float Rm = R * 1.001f + 1e-6f * (dmax + hmax);
+                        near = !(dist2 > Rm * Rm);
+                        if (near) {
+                            lx = (float)(dx - (double)hx);
+                            ly = (float)(dy - (double)hy);
+                            lz = (float)(dz - (double)hz);
+                        }
+                    }
+                    const unsigned bn = __ballot_sync(0xffffffffu, valid && near);
+                    const unsigned bf = __ballot_sync(0xffffffffu, valid && !near);
+                    const unsigned lt = (1u << lane) - 1u;
+                    if (valid && near) {
+                        const int pos = nn + __popc(bn & lt);
+                        S.nh[pos] = make_float4(hx, hy, hz, m);
+                        S.nl[pos] = make_float4(lx, ly, lz, rs2);
+                        S.nidx[pos] = e;
+                    } else if (valid) {
+                        S.fr[nf + __popc(bf & lt)] = make_float4(hx, hy, hz, m);
+                    }
+                    nn += __popc(bn);
+                    nf += __popc(bf);
+                }
+                if (lane == 0) {
+                    s.hdr[sl].kind = kItemEP;
+                    s.hdr[sl].nn = nn;
+                    s.hdr[sl].nf = nf;
+                    s.hdr[sl].base = base;
+                }
+                publish(sl);
+            }
+            // SPJ tiles: 2 entries per lane, 64-byte records.
+            for (int t = 0; t < n_spt; ++t) {
+                const int64_t base = wd.spj_begin + (int64_t)t * kTileSP;
+                const int nt = min(kTileSP, wd.n_spj - t * kTileSP);
+                int id[2];
+                uint4 r[2][4];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int e = q * 32 + lane;
+                    id[q] = e < nt ? __ldg(p.id_spj + base + e) : -1;
+                }
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    if (id[q] >= 0) {
+                        const uint4* src = reinterpret_cast<const uint4*>(p.spj + id[q]);
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) r[q][u] = __ldg(src + u);
+                    }
+                }
+                if (!acquire(sl)) return;
+                SlotSP& S = s.slot[sl].sp;
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int e = q * 32 + lane;
+                    if (e < nt) {
+                        const float hx = (float)(as_double(r[q][0].x, r[q][0].y) - cx);
+                        const float hy = (float)(as_double(r[q][0].z, r[q][0].w) - cy);
+                        const float hz = (float)(as_double(r[q][1].x, r[q][1].y) - cz);
+                        S.sp[e][0] = make_float4(hx, hy, hz, __uint_as_float(r[q][1].z));
+                        S.sp[e][1] = make_float4(__uint_as_float(r[q][2].x), __uint_as_float(r[q][2].y),
+                                                 __uint_as_float(r[q][2].z), __uint_as_float(r[q][2].w));
+                        S.sp[e][2] = make_float4(__uint_as_float(r[q][3].x), __uint_as_float(r[q][3].y),
+                                                 -__uint_as_float(r[q][3].z) * eps2, 0.f);
+                    }
+                }
+                if (lane == 0) {
+                    s.hdr[sl].kind = kItemSP;
+                    s.hdr[sl].nn = nt;
+                    s.hdr[sl].nf = 0;
+                    s.hdr[sl].base = base;
+                }
+                publish(sl);
+            }
+            if (!acquire(sl)) return;
+            if (lane == 0) s.hdr[sl].kind = kItemEnd;
+            publish(sl);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- consumer
+
+template <int CW, int KI>
+__device__ void consumer(const Params& p, Smem<CW, KI>& s, int ct) {
+    constexpr int CT = CW * 32;
+    constexpr int kMaxPass = CT * KI;
+    const double eps2d = p.eps2;
+    const float eps2 = (float)p.eps2;
+    unsigned item = 0;
+
+    // Pass state.
+    WalkDesc wd{};
+    float rcut2 = 0.f;
+    int nip = 0, S = 1, n_js = 1, js = 0, slot = 0;
+    bool active = false;
+    float xih[KI], yih[KI], zih[KI], xil[KI], yil[KI], zil[KI], rsi2[KI];
+    int kb[KI], gi[KI], cnt[KI];
+    bool valid[KI];
+    float a[KI][4];
+    int since = 0;
+#pragma unroll
+    for (int k = 0; k < KI; ++k) {
+        xih[k] = yih[k] = zih[k] = xil[k] = yil[k] = zil[k] = rsi2[k] = 0.f;
+        kb[k] = gi[k] = cnt[k] = 0;
+        valid[k] = false;
+        a[k][0] = a[k][1] = a[k][2] = a[k][3] = 0.f;
+    }
+
+    auto flush = [&]() {
+#pragma unroll
+        for (int k = 0; k < KI; ++k)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                s.acc[k][q][ct] += (double)a[k][q];
+                a[k][q] = 0.f;
+            }
+        since = 0;
+    };
+    auto push_retest = [&](int k, int64_t jidx) -> int {
+        const int r = atomicAdd(p.n_retest, 1);
+        if (r < p.retest_cap) {
+            Retest rr;
+            rr.j_begin = jidx;
+            rr.i = gi[k];
+            rr.n = 1;
+            p.retest[r] = rr;
+            return 0;
+        }
+        const EpiDev ei = p.epi[gi[k]];
+        const int id = p.id_epj[jidx];
+        const EpjMix e = p.epj[id];
+        return exact_neighbour(ei.x, ei.y, ei.z, ei.rs, e.x, e.y, e.z, p.epj_rs64[id], p.eps2);
+    };
+
+    for (;;) {
+        const int sl = item % kSlots;
+        if (!mbar_wait(&s.full[sl], (item / kSlots) & 1u, p.err)) return;
+        const Hdr h = s.hdr[sl];
+        if (h.kind == kItemExit) return;
+        if (h.kind == kItemBegin) {
+            wd = p.walks[h.walk];
+            rcut2 = (float)wd.rcut2;
+            nip = min(kMaxPass, wd.n_i - h.ipass);
+            S = (nip + KI - 1) / KI;
+            n_js = CT / S;
+            js = ct / S;
+            slot = ct - js * S;
+            active = js < n_js;
+#pragma unroll
+            for (int k = 0; k < KI; ++k) {
+                const int li = slot + k * S;
+                valid[k] = active && li < nip;
+                gi[k] = wd.i_begin + h.ipass + li;
+                xih[k] = yih[k] = zih[k] = xil[k] = yil[k] = zil[k] = 0.f;
+                rsi2[k] = 0.f;
+                kb[k] = 0;
+                cnt[k] = 0;
+                if (valid[k]) {
+                    const EpiDev e = p.epi[gi[k]];
+                    const double dx = e.x - wd.cx, dy = e.y - wd.cy, dz = e.z - wd.cz;
+                    xih[k] = (float)dx;
+                    yih[k] = (float)dy;
+                    zih[k] = (float)dz;
+                    xil[k] = (float)(dx - (double)xih[k]);
+                    yil[k] = (float)(dy - (double)yih[k]);
+                    zil[k] = (float)(dz - (double)zih[k]);
+                    rsi2[k] = (float)(e.rs * e.rs);
+                    kb[k] = kband_near(fmax(fabs(dx), fmax(fabs(dy), fabs(dz))), e.rs, eps2d);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    a[k][q] = 0.f;
+                    s.acc[k][q][ct] = 0.0;
+                }
+            }
+            since = 0;
+        } else if (h.kind == kItemEP) {
+            if (active) {
+                const SlotEP& T = s.slot[sl].ep;
+                int c[KI];
+#pragma unroll
+                for (int k = 0; k < KI; ++k) c[k] = 0;
+                const int pn = (h.nn + n_js - 1) / n_js;
+                const int j0 = min(h.nn, js * pn);
+                const int j1 = min(h.nn, j0 + pn);
+#pragma unroll 2
+                for (int j = j0; j < j1; ++j) {
+                    const float4 hh = T.nh[j];
+                    const float4 ll = T.nl[j];
+#pragma unroll
+                    for (int k = 0; k < KI; ++k) {
+                        const float dx = (hh.x - xih[k]) + (ll.x - xil[k]);
+                        const float dy = (hh.y - yih[k]) + (ll.y - yil[k]);
+                        const float dz = (hh.z - zih[k]) + (ll.z - zil[k]);
+                        float r2 = fmaf(dx, dx, eps2);
+                        r2 = fmaf(dy, dy, r2);
+                        r2 = fmaf(dz, dz, r2);
+                        const float rs2 = fmaxf(rsi2[k], ll.w);
+                        const int e = __float_as_int(r2) - __float_as_int(rs2) + kb[k];
+                        c[k] += (int)((unsigned)e >> 31);
+                        if ((unsigned)e < (unsigned)(2 * kb[k]) && valid[k]) c[k] += push_retest(k, h.base + T.nidx[j]);
+                        const float ri = rsqrt_approx(fmaxf(r2, rcut2));
+                        const float mri = hh.w * ri;
+                        const float mri3 = mri * (ri * ri);
+                        a[k][0] = fmaf(mri3, dx, a[k][0]);
+                        a[k][1] = fmaf(mri3, dy, a[k][1]);
+                        a[k][2] = fmaf(mri3, dz, a[k][2]);
+                        a[k][3] -= mri;
+                    }
+                }
+                const int pf = (h.nf + n_js - 1) / n_js;
+                const int f0 = min(h.nf, js * pf);
+                const int f1 = min(h.nf, f0 + pf);
+#pragma unroll 4
+                for (int j = f0; j < f1; ++j) {
+                    const float4 hh = T.fr[j];
+#pragma unroll
+                    for (int k = 0; k < KI; ++k) {
+                        const float dx = hh.x - xih[k];
+                        const float dy = hh.y - yih[k];
+                        const float dz = hh.z - zih[k];
+                        float r2 = fmaf(dx, dx, eps2);
+                        r2 = fmaf(dy, dy, r2);
+                        r2 = fmaf(dz, dz, r2);
+                        const float ri = rsqrt_approx(r2);
+                        const float mri = hh.w * ri;
+                        const float mri3 = mri * (ri * ri);
+                        a[k][0] = fmaf(mri3, dx, a[k][0]);
+                        a[k][1] = fmaf(mri3, dy, a[k][1]);
+                        a[k][2] = fmaf(mri3, dz, a[k][2]);
+                        a[k][3] -= mri;
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < KI; ++k) cnt[k] += c[k];
+                since += (j1 - j0) + (f1 - f0);
+                if (since >= kFlush) flush();
+            }
+        } else if (h.kind == kItemSP) {
+            if (active) {
+                const SlotSP& T = s.slot[sl].sp;
+                const int ps = (h.nn + n_js - 1) / n_js;
+                const int j0 = min(h.nn, js * ps);
+                const int j1 = min(h.nn, j0 + ps);
+#pragma unroll 2
+                for (int j = j0; j < j1; ++j) {
+                    const float4 q0 = T.sp[j][0];
+                    const float4 qa = T.sp[j][1];
+                    const float4 qb = T.sp[j][2];
+#pragma unroll
+                    for (int k = 0; k < KI; ++k) {
+                        const float dx = q0.x - xih[k];
+                        const float dy = q0.y - yih[k];
+                        const float dz = q0.z - zih[k];
+                        float r2 = fmaf(dx, dx, eps2);
+                        r2 = fmaf(dy, dy, r2);
+                        r2 = fmaf(dz, dz, r2);
+                        const float ri = rsqrt_approx(r2);
+                        const float qdx = fmaf(qa.x, dx, fmaf(qa.w, dy, qb.x * dz));
+                        const float qdy = fmaf(qa.w, dx, fmaf(qa.y, dy, qb.y * dz));
+                        const float qdz = fmaf(qb.x, dx, fmaf(qb.y, dy, qa.z * dz));
+                        const float sq = fmaf(qdx, dx, fmaf(qdy, dy, fmaf(qdz, dz, qb.z)));
+                        const float ri2 = ri * ri;
+                        const float ri3 = ri2 * ri;
+                        const float ri5 = ri3 * ri2;
+                        const float tq = sq * ri5;
+                        const float A = fmaf(tq * ri2, 2.5f, q0.w * ri3);
+                        a[k][0] = fmaf(A, dx, fmaf(-ri5, qdx, a[k][0]));
+                        a[k][1] = fmaf(A, dy, fmaf(-ri5, qdy, a[k][1]));
+                        a[k][2] = fmaf(A, dz, fmaf(-ri5, qdz, a[k][2]));
+                        a[k][3] = fmaf(-0.5f, tq, fmaf(-q0.w, ri, a[k][3]));
+                    }
+                }
+                since += j1 - j0;
+                if (since >= kFlush) flush();
+            }
+        } else {  // kItemEnd: reduce the j-slices of the pass and write
+            if (active) {
+                flush();
+#pragma unroll
+                for (int k = 0; k < KI; ++k) s.cnt[k][ct] = cnt[k];
+            }
+            consumers_sync(CT);
+            if (active && js == 0) {
+                const double G = p.G;
+#pragma unroll
+                for (int k = 0; k < KI; ++k) {
+                    if (!valid[k]) continue;
+                    double r[4] = {0.0, 0.0, 0.0, 0.0};
+                    int n = 0;
+                    for (int q = 0; q < n_js; ++q) {
+                        const int src = q * S + slot;
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) r[c] += s.acc[k][c][src];
+                        n += s.cnt[k][src];
+                    }
+                    p.out_accp[gi[k]] = Accp{G * r[0], G * r[1], G * r[2], G * r[3]};
+                    p.out_nnb[gi[k]] = n;
+                }
+            }
+            consumers_sync(CT);
+        }
+        mbar_arrive(&s.empty[sl]);
+        ++item;
+    }
+}
+
+template <int CW, int KI, int MINB>
+__global__ __launch_bounds__((CW + 1) * 32, MINB) void ws_kernel(Params p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Smem<CW, KI>& s = *reinterpret_cast<Smem<CW, KI>*>(smem_raw);
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        for (int i = 0; i < kSlots; ++i) {
+            mbar_init(&s.full[i], 32);
+            mbar_init(&s.empty[i], CW * 32);
+        }
+    }
+    __syncthreads();
+    if (tid >= CW * 32)
+        producer<CW, KI>(p, s, tid - CW * 32);
+    else
+        consumer<CW, KI>(p, s, tid);
+}
+
+template <int CW, int KI, int MINB>
+cudaError_t launch_ws_t(const Params& p, cudaStream_t st, int num_sms) {
+    cudaError_t e = cudaMemsetAsync(p.queue_head, 0, sizeof(int32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), st);
+    if (e != cudaSuccess) return e;
+    if (p.n_walk <= 0) return cudaSuccess;
+    static int per_sm = 0;
+    const size_t smem = sizeof(Smem<CW, KI>);
+    if (per_sm == 0) {
+        e = cudaFuncSetAttribute(ws_kernel<CW, KI, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ws_kernel<CW, KI, MINB>, (CW + 1) * 32, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+    }
+    int grid = num_sms * per_sm;
+    if (grid > p.n_walk) grid = p.n_walk;
+    ws_kernel<CW, KI, MINB><<<grid, (CW + 1) * 32, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// Variants of the warp-specialised kernel: consumer warps, i per consumer
+// thread, minimum CTAs per SM.
+cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant) {
+    switch (variant) {
+        case 0: return launch_ws_t<4, 3, 4>(p, s, num_sms);
+        case 1: return launch_ws_t<4, 2, 4>(p, s, num_sms);
+        case 2: return launch_ws_t<4, 2, 5>(p, s, num_sms);
+        case 3: return launch_ws_t<8, 2, 3>(p, s, num_sms);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace pgf

@@ -120,6 +120,9 @@ def load(build: bool = True) -> ctypes.CDLL:
         "pgf_retrieve": [ci, ci, vp, vp, vp],
         "pgf_set_walk_rcut2": [vp, ci],
         "pgf_recompute": [ci],
+        "pgf_set_kernel_variant": [ci],
+        "pgf_get_kernel_variant": [vp],
+        "pgf_autotune": [ci, ci, vp, vp],
         "pgf_wait": [ci],
         "pgf_get_profile": [vp],
         "pgf_clear_profile": [],
@@ -174,6 +177,23 @@ def set_walk_rcut2(walk_rcut2: np.ndarray | None) -> None:
     else:
         a = np.ascontiguousarray(walk_rcut2, dtype=np.float64)
         _check(load().pgf_set_walk_rcut2(a.ctypes.data, a.size))
+
+
+def set_kernel_variant(variant: int) -> None:
+    _check(load().pgf_set_kernel_variant(variant))
+
+
+def get_kernel_variant() -> int:
+    v = ctypes.c_int()
+    _check(load().pgf_get_kernel_variant(ctypes.byref(v)))
+    return v.value
+
+
+def autotune(tag: int = 0, repeats: int = 3) -> tuple[int, float]:
+    """Times every kernel variant on the tag's resident data; keeps the fastest."""
+    v, ms = ctypes.c_int(), ctypes.c_double()
+    _check(load().pgf_autotune(tag, repeats, ctypes.byref(v), ctypes.byref(ms)))
+    return v.value, ms.value
 
 
 def recompute(tag: int = 0) -> None:

@@ -215,3 +215,38 @@ def test_recompute_reproduces():
     b = gpuforce.retrieve(rec, tag=0).copy()
     np.testing.assert_array_equal(a["n_ngb"], b["n_ngb"])
     np.testing.assert_array_equal(a["acc"], b["acc"])
+
+
+@pytest.mark.parametrize("variant", list(range(1, 5)))
+@pytest.mark.parametrize("case", ["kernel_test_rsvar", "plummer2048_walks", "ragged", "binaries"])
+def test_kernel_variants(case, variant):
+    """Every mixed-precision kernel variant the autotuner may pick meets the
+    same parity bar (variant 0 is covered by the tests above)."""
+    if case == "ragged":
+        wb = _ragged_batch()
+    elif case == "binaries":
+        wb = walks.build_walks(ics.make_plummer_cluster(21, 20000, 0.004, binary_fraction=0.5))
+    else:
+        wb, _ = load_golden(case)
+    gpuforce.set_kernel_variant(variant)
+    try:
+        res = gpuforce.compute(wb, PGF_PRECISION_MIXED)
+    finally:
+        gpuforce.set_kernel_variant(0)
+    check(wb, res, PGF_PRECISION_MIXED, label=f"{case} v{variant}")
+
+
+def test_autotune_picks_a_variant_and_keeps_results():
+    wb = walks.build_walks(ics.make_plummer_cluster(22, 30000, 0.005, binary_fraction=0.3))
+    o = oracle.force(wb)
+    rec = gpuforce.Records(wb)
+    gpuforce.set_precision(PGF_PRECISION_MIXED)
+    gpuforce.dispatch(rec, tag=0)
+    gpuforce.retrieve(rec, tag=0)
+    best, ms = gpuforce.autotune(0, repeats=2)
+    assert 0 <= best < 5 and ms > 0
+    assert gpuforce.get_kernel_variant() == best
+    gpuforce.recompute(0)
+    f = gpuforce.retrieve(rec, tag=0)
+    check(wb, dict(acc=f["acc"], pot=f["pot"], nnb=f["n_ngb"]), PGF_PRECISION_MIXED, o=o, label="autotuned")
+    gpuforce.set_kernel_variant(0)

@@ -31,7 +31,7 @@ def _worker(rank, world, port, out):
 
 def test_two_rank_replica_aggregation():
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_worker, args=(2, port, out), nprocs=2, join=True)
         res = dict(out)
