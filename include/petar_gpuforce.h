@@ -106,11 +106,18 @@ int pgf_set_precision(int precision);
 
 /* Mixed-precision kernel variants: 0 is the CTA-synchronous tiled kernel;
  * 1..PGF_NUM_KERNEL_VARIANTS-1 are warp-specialised producer/consumer kernels
- * with different consumer-warp counts and i-particles per thread.  The
- * choice applies to later dispatches. */
-#define PGF_NUM_KERNEL_VARIANTS 5
+ * with different consumer-warp counts, i-particles per thread and scalar or
+ * packed FP32x2 arithmetic.  The choice applies to later dispatches. */
+#define PGF_NUM_KERNEL_VARIANTS 9
 int pgf_set_kernel_variant(int variant);
 int pgf_get_kernel_variant(int *variant);
+
+/* Index dispatches run as a pipeline of up to 8 stages over contiguous walk
+ * ranges (host packing, copies and kernels of successive stages overlap).
+ * 0 (default) picks the stage count from the id-list size, 1 disables the
+ * pipeline, 2..8 force that many stages (dispatches of fewer than 8 walks per
+ * stage use one).  Results do not depend on the stage count. */
+int pgf_set_dispatch_stages(int stages);
 
 /* Autotuner: times every kernel variant `repeats` times on the data of the
  * tag's last index dispatch (already on the device), keeps the fastest for

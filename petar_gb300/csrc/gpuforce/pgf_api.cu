@@ -29,6 +29,9 @@ namespace {
 using namespace pgf;
 
 constexpr int kMaxTags = 16;
+constexpr int kMaxChunks = 8;                       // pipeline stages of a large dispatch
+constexpr int64_t kChunkIdEntries = 12 << 20;       // about 48 MB of id lists per stage
+constexpr int kScratchInts = 8 + 2 * kMaxChunks;
 static_assert(PGF_NUM_KERNEL_VARIANTS == 1 + kNumWsVariants, "variant 0 plus the warp-specialised variants");
 constexpr int64_t kMaxRows = 0x7fffffff;
 
@@ -114,8 +117,12 @@ struct TagState {
     HostBuf<WalkDesc> h_walks;
     HostBuf<Accp> h_accp;
     HostBuf<int32_t> h_nnb;
-    HostBuf<int32_t> h_flags;  // err, n_retest
+    HostBuf<int32_t> h_flags;  // queue head, n_retest, err, re-tested records
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    // Pipelined dispatch, per stage: copy start/end, main kernel start/end,
+    // stage done (after the re-test kernel).
+    cudaEvent_t evc[kMaxChunks][5] = {};
+    int n_chunks = 0;  // stages of the last dispatch (0: a single launch)
     bool times_pending = false;  // kernel events recorded, not yet added to the profile
     Params params{};
 };
@@ -126,10 +133,13 @@ struct State {
     int num_sms = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // host-to-device copies of pipelined dispatches
+    cudaStream_t stage_stream[kMaxChunks] = {};  // kernels of pipeline stages
     bool user_stream = false;
     double eps2 = 0, rcut2 = 0, G = 1;
     int precision = PGF_PRECISION_MIXED;
     int variant = 0;  // mixed-precision kernel variant (pgf_set_kernel_variant)
+    int stages = 0;   // dispatch pipeline stages (pgf_set_dispatch_stages); 0 = by size
     // shared j data
     DevBuf<EpjMix> epj;
     DevBuf<double> epj_m64, epj_rs64;
@@ -142,7 +152,9 @@ struct State {
     int64_t n_epj_tot = 0, n_spj_tot = 0;
     bool j_sent = false;
     // scratch
-    DevBuf<int32_t> scratch;  // [0] queue head, [1] n_retest, [2] err
+    // [0] queue head, [1] n_retest (single launch), [2] err, [3] re-tested
+    // records, [8 + 2s], [9 + 2s]: queue head and n_retest of pipeline stage s
+    DevBuf<int32_t> scratch;
     DevBuf<Retest> retest;
     int retest_cap = 0;
     std::vector<double> walk_rcut2;
@@ -174,15 +186,20 @@ int setup_device(int rank) {
     PGF_CUDA(cudaSetDevice(g.device));
     PGF_CUDA(cudaDeviceGetAttribute(&g.num_sms, cudaDevAttrMultiProcessorCount, g.device));
     PGF_CUDA(cudaStreamCreateWithFlags(&g.own_stream, cudaStreamNonBlocking));
+    PGF_CUDA(cudaStreamCreateWithFlags(&g.copy_stream, cudaStreamNonBlocking));
+    for (auto& st : g.stage_stream) PGF_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     if (!g.user_stream) g.stream = g.own_stream;
     PGF_CUDA(cudaEventCreate(&g.ev_send0));
     PGF_CUDA(cudaEventCreate(&g.ev_send1));
-    for (auto& t : g.tags)
+    for (auto& t : g.tags) {
         for (auto& ev : t.ev) PGF_CUDA(cudaEventCreate(&ev));
-    PGF_CUDA(g.scratch.ensure(4));
+        for (auto& c : t.evc)
+            for (auto& ev : c) PGF_CUDA(cudaEventCreate(&ev));
+    }
+    PGF_CUDA(g.scratch.ensure(kScratchInts));
     g.retest_cap = 1 << 20;
     PGF_CUDA(g.retest.ensure((size_t)g.retest_cap));
-    PGF_CUDA(cudaMemset(g.scratch.d, 0, 4 * sizeof(int32_t)));
+    PGF_CUDA(cudaMemset(g.scratch.d, 0, kScratchInts * sizeof(int32_t)));
     g.init = true;
     return PGF_OK;
 }
@@ -288,26 +305,50 @@ int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, co
     return PGF_OK;
 }
 
-int launch_tag(TagState& t) {
-    Params& p = t.params;
-    p.queue_head = g.scratch.d;
-    p.n_retest = g.scratch.d + 1;
+// Scratch of a single launch (stage < 0) or of pipeline stage `stage` of
+// n_stages: its own queue cursor, re-test counter and slice of the re-test
+// records, so that the launches of different stages may overlap.
+void bind_scratch(Params& p, int stage = -1, int n_stages = 1) {
     p.err = g.scratch.d + 2;
-    p.retest = g.retest.d;
-    p.retest_cap = g.retest_cap;
-    PGF_CUDA(cudaEventRecord(t.ev[1], g.stream));
+    p.retest_total = g.scratch.d + 3;
+    if (stage < 0) {
+        p.queue_head = g.scratch.d;
+        p.n_retest = g.scratch.d + 1;
+        p.retest = g.retest.d;
+        p.retest_cap = g.retest_cap;
+    } else {
+        const int cap = g.retest_cap / n_stages;
+        p.queue_head = g.scratch.d + 8 + 2 * stage;
+        p.n_retest = g.scratch.d + 9 + 2 * stage;
+        p.retest = g.retest.d + (size_t)stage * cap;
+        p.retest_cap = cap;
+    }
+}
+
+// Main kernel of the tag's precision and variant on stream s, bracketed by two
+// events, then the FP64 neighbour re-test.
+int launch_kernels(const TagState& t, const Params& p, cudaStream_t s, cudaEvent_t ev_start, cudaEvent_t ev_end) {
+    PGF_CUDA(cudaEventRecord(ev_start, s));
     cudaError_t e;
     if (t.precision == PGF_PRECISION_FP64) {
-        e = launch_fp64(p, g.stream, g.num_sms);
-        if (e == cudaSuccess) e = cudaEventRecord(t.ev[2], g.stream);
-        if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), g.stream);
+        e = launch_fp64(p, s, g.num_sms);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_end, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), s);
     } else {
-        e = t.variant == 0 ? launch_mixed(p, g.stream, g.num_sms) : launch_ws(p, g.stream, g.num_sms, t.variant - 1);
-        if (e == cudaSuccess) e = cudaEventRecord(t.ev[2], g.stream);
-        if (e == cudaSuccess && p.n_walk > 0) e = launch_retest(p, g.stream, g.num_sms);
+        e = t.variant == 0 ? launch_mixed(p, s, g.num_sms) : launch_ws(p, s, g.num_sms, t.variant - 1);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_end, s);
+        if (e == cudaSuccess && p.n_walk > 0) e = launch_retest(p, s, g.num_sms);
     }
     if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+    return PGF_OK;
+}
+
+// One launch over all walks of the tag (recompute, small dispatches).
+int launch_tag(TagState& t) {
+    bind_scratch(t.params);
+    if (int r = launch_kernels(t, t.params, g.stream, t.ev[1], t.ev[2])) return r;
     PGF_CUDA(cudaEventRecord(t.ev[3], g.stream));
+    t.n_chunks = 0;
     t.dispatched = true;
     t.has_data = true;
     t.times_pending = true;
@@ -318,9 +359,22 @@ int launch_tag(TagState& t) {
 void harvest_times(TagState& t) {
     if (!t.times_pending) return;
     float ms_send = 0, ms_calc = 0, ms_main = 0;
-    cudaEventElapsedTime(&ms_send, t.ev[0], t.ev[1]);
-    cudaEventElapsedTime(&ms_calc, t.ev[1], t.ev[3]);
-    cudaEventElapsedTime(&ms_main, t.ev[1], t.ev[2]);
+    if (t.n_chunks > 0) {
+        // Stages overlap: the main-kernel time is the span from the first
+        // stage's start to the last main-kernel end.
+        cudaEventElapsedTime(&ms_calc, t.evc[0][2], t.ev[3]);
+        for (int c = 0; c < t.n_chunks; ++c) {
+            float a = 0, b = 0;
+            cudaEventElapsedTime(&a, t.evc[c][0], t.evc[c][1]);
+            cudaEventElapsedTime(&b, t.evc[0][2], t.evc[c][3]);
+            ms_send += a;
+            ms_main = std::max(ms_main, b);
+        }
+    } else {
+        cudaEventElapsedTime(&ms_calc, t.ev[1], t.ev[3]);
+        cudaEventElapsedTime(&ms_send, t.ev[0], t.ev[1]);
+        cudaEventElapsedTime(&ms_main, t.ev[1], t.ev[2]);
+    }
     g.prof.send += 1e-3 * ms_send;
     g.prof.calc += 1e-3 * ms_calc;
     g.prof.calc_main += 1e-3 * ms_main;
@@ -329,7 +383,88 @@ void harvest_times(TagState& t) {
     t.times_pending = false;
 }
 
-// Packs the walks of one index dispatch (src/force_gpu_cuda.cu:621-699).
+// Offsets of one walk in the packed (cost-sorted) layout.
+struct Slot3 {
+    int64_t i, e, s;
+};
+
+// Packs walk w of an index dispatch into position k of the tag's pinned
+// staging: its EPI rows, its id lists (validated against the sent arrays in
+// the same pass) and its descriptor.  Returns false if an id is out of range.
+bool pack_walk(TagState& t, int k, int w, const Slot3& o, const void* const* epi, const int* n_epi,
+               const pgf_epi_layout* il, const int* const* id_epj, const int* n_epj, const int* const* id_spj,
+               const int* n_spj) {
+    double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+    double rs_max = 0.0;
+    const char* base = reinterpret_cast<const char*>(epi[w]);
+    for (int i = 0; i < n_epi[w]; ++i) {
+        const char* r = base + (size_t)i * il->size;
+        const double* p = dptr(r, il->off_pos);
+        EpiDev e{p[0], p[1], p[2], *dptr(r, il->off_r_search)};
+        t.h_epi.h[o.i + i] = e;
+        rs_max = std::max(rs_max, e.rs);
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = std::min(lo[d], p[d]);
+            hi[d] = std::max(hi[d], p[d]);
+        }
+    }
+    unsigned bad = 0;
+    {
+        const int32_t* src = n_epj[w] ? id_epj[w] : nullptr;
+        int32_t* dst = t.h_id_epj.h + o.e;
+        const unsigned lim = (unsigned)g.n_epj_tot;
+        for (int q = 0; q < n_epj[w]; ++q) {
+            const int32_t v = src[q];
+            bad |= (unsigned)v >= lim;
+            dst[q] = v;
+        }
+    }
+    {
+        const int32_t* src = n_spj[w] ? id_spj[w] : nullptr;
+        int32_t* dst = t.h_id_spj.h + o.s;
+        const unsigned lim = (unsigned)g.n_spj_tot;
+        for (int q = 0; q < n_spj[w]; ++q) {
+            const int32_t v = src[q];
+            bad |= (unsigned)v >= lim;
+            dst[q] = v;
+        }
+    }
+    WalkDesc d;
+    d.epj_begin = o.e;
+    d.spj_begin = o.s;
+    d.i_begin = (int32_t)o.i;
+    d.n_i = n_epi[w];
+    d.n_epj = n_epj[w];
+    d.n_spj = n_spj[w];
+    if (n_epi[w] > 0) {
+        d.cx = 0.5 * (lo[0] + hi[0]);
+        d.cy = 0.5 * (lo[1] + hi[1]);
+        d.cz = 0.5 * (lo[2] + hi[2]);
+        // Half-extents about the centre and the largest r_search, rounded up
+        // so the kernel's far-field classification stays conservative.
+        d.hx = round_up(std::max(hi[0] - d.cx, d.cx - lo[0]));
+        d.hy = round_up(std::max(hi[1] - d.cy, d.cy - lo[1]));
+        d.hz = round_up(std::max(hi[2] - d.cz, d.cz - lo[2]));
+        d.rs_max = round_up(rs_max);
+    } else {
+        d.cx = d.cy = d.cz = 0.0;
+        d.hx = d.hy = d.hz = d.rs_max = 0.f;
+    }
+    d.pad[0] = d.pad[1] = d.pad[2] = d.pad[3] = 0.f;
+    d.rcut2 = g.walk_rcut2.empty() ? g.rcut2 : g.walk_rcut2[w];
+    t.h_walks.h[k] = d;
+    t.h_order.h[k] = k;
+    return bad == 0;
+}
+
+// Packs the walks of one index dispatch (src/force_gpu_cuda.cu:621-699) and
+// launches the kernels.  Walks are laid out in descending cost (EP-SP pairs
+// weighted by their larger instruction count), so the work queue is the
+// identity and the largest walks start first.  Large dispatches run as a
+// pipeline of up to kMaxChunks stages over contiguous ranges of that layout:
+// the host packs stage c + 1 while the copy stream moves stage c, and each
+// stage's kernels run on their own stream as soon as its copies land, so a
+// stage's tail overlaps the next stage's start.
 int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi, const pgf_epi_layout* il,
                    const int* const* id_epj, const int* n_epj, const int* const* id_spj, const int* n_spj) {
     TagState& t = g.tags[tag];
@@ -339,20 +474,28 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     if (!g.walk_rcut2.empty() && (int)g.walk_rcut2.size() != n_walk)
         return fail(PGF_ERR_ARG, "per-walk r_out^2 was set for %zu walks, dispatch has %d",
                     g.walk_rcut2.size(), n_walk);
-    // The previous dispatch of this tag may still be copying from staging.
+    // Earlier work of this tag may still read its staging or device buffers.
     if (t.dispatched) PGF_CUDA(cudaEventSynchronize(t.ev[3]));
     const double t0 = now_s();
-    std::vector<int64_t> idisp(n_walk + 1, 0), edisp(n_walk + 1, 0), sdisp(n_walk + 1, 0);
     for (int w = 0; w < n_walk; ++w) {
         if (n_epi[w] < 0 || n_epj[w] < 0 || n_spj[w] < 0) return fail(PGF_ERR_ARG, "negative count in walk %d", w);
         if ((n_epi[w] > 0 && !epi[w]) || (n_epj[w] > 0 && (!id_epj || !id_epj[w])) ||
             (n_spj[w] > 0 && (!id_spj || !id_spj[w])))
             return fail(PGF_ERR_ARG, "NULL array for walk %d", w);
-        idisp[w + 1] = idisp[w] + n_epi[w];
-        edisp[w + 1] = edisp[w] + n_epj[w];
-        sdisp[w + 1] = sdisp[w] + n_spj[w];
     }
-    const int64_t ni = idisp[n_walk], ne = edisp[n_walk], ns = sdisp[n_walk];
+    std::vector<int32_t> ord(n_walk);
+    std::iota(ord.begin(), ord.end(), 0);
+    auto cost = [&](int w) { return (double)n_epi[w] * ((double)n_epj[w] + 2.0 * (double)n_spj[w]); };
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return cost(a) > cost(b); });
+    std::vector<Slot3> off(n_walk + 1);
+    off[0] = Slot3{0, 0, 0};
+    t.epi_disp.assign(n_walk, 0);
+    for (int k = 0; k < n_walk; ++k) {
+        const int w = ord[k];
+        t.epi_disp[w] = off[k].i;
+        off[k + 1] = Slot3{off[k].i + n_epi[w], off[k].e + n_epj[w], off[k].s + n_spj[w]};
+    }
+    const int64_t ni = off[n_walk].i, ne = off[n_walk].e, ns = off[n_walk].s;
     if (ni > kMaxRows) return fail(PGF_ERR_CAPACITY, "%lld i-particles exceed 2^31-1", (long long)ni);
     if (ne > 0 && !g.j_sent) return fail(PGF_ERR_STATE, "EPJ ids given before the EPJ array was sent");
     PGF_CUDA(t.h_epi.ensure(ni));
@@ -367,87 +510,24 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     PGF_CUDA(t.order.ensure(n_walk));
     PGF_CUDA(t.accp.ensure(ni));
     PGF_CUDA(t.nnb.ensure(ni));
-    int bad_id = -1;
-#pragma omp parallel for schedule(dynamic, 4) reduction(max : bad_id)
-    for (int w = 0; w < n_walk; ++w) {
-        double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
-        double rs_max = 0.0;
-        const char* base = reinterpret_cast<const char*>(epi[w]);
-        for (int i = 0; i < n_epi[w]; ++i) {
-            const char* r = base + (size_t)i * il->size;
-            const double* p = dptr(r, il->off_pos);
-            EpiDev e{p[0], p[1], p[2], *dptr(r, il->off_r_search)};
-            t.h_epi.h[idisp[w] + i] = e;
-            rs_max = std::max(rs_max, e.rs);
-            for (int d = 0; d < 3; ++d) {
-                lo[d] = std::min(lo[d], p[d]);
-                hi[d] = std::max(hi[d], p[d]);
-            }
-        }
-        if (n_epj[w]) {
-            std::memcpy(t.h_id_epj.h + edisp[w], id_epj[w], sizeof(int32_t) * n_epj[w]);
-            for (int k = 0; k < n_epj[w]; ++k)
-                if ((unsigned)id_epj[w][k] >= (unsigned)g.n_epj_tot) bad_id = std::max(bad_id, w);
-        }
-        if (n_spj[w]) {
-            std::memcpy(t.h_id_spj.h + sdisp[w], id_spj[w], sizeof(int32_t) * n_spj[w]);
-            for (int k = 0; k < n_spj[w]; ++k)
-                if ((unsigned)id_spj[w][k] >= (unsigned)g.n_spj_tot) bad_id = std::max(bad_id, w);
-        }
-        WalkDesc d;
-        d.epj_begin = edisp[w];
-        d.spj_begin = sdisp[w];
-        d.i_begin = (int32_t)idisp[w];
-        d.n_i = n_epi[w];
-        d.n_epj = n_epj[w];
-        d.n_spj = n_spj[w];
-        if (n_epi[w] > 0) {
-            d.cx = 0.5 * (lo[0] + hi[0]);
-            d.cy = 0.5 * (lo[1] + hi[1]);
-            d.cz = 0.5 * (lo[2] + hi[2]);
-            // Half-extents about the centre and the largest r_search, rounded
-            // up so the kernel's far-field classification stays conservative.
-            d.hx = round_up(std::max(hi[0] - d.cx, d.cx - lo[0]));
-            d.hy = round_up(std::max(hi[1] - d.cy, d.cy - lo[1]));
-            d.hz = round_up(std::max(hi[2] - d.cz, d.cz - lo[2]));
-            d.rs_max = round_up(rs_max);
-        } else {
-            d.cx = d.cy = d.cz = 0.0;
-            d.hx = d.hy = d.hz = d.rs_max = 0.f;
-        }
-        d.pad[0] = d.pad[1] = d.pad[2] = d.pad[3] = 0.f;
-        d.rcut2 = g.walk_rcut2.empty() ? g.rcut2 : g.walk_rcut2[w];
-        t.h_walks.h[w] = d;
+
+    // Stages: contiguous ranges of the sorted layout with about equal numbers
+    // of list entries.
+    int n_chunks = g.stages > 0 ? g.stages : (int)std::min<int64_t>(kMaxChunks, (ne + ns) / kChunkIdEntries + 1);
+    if (n_walk < 8 * n_chunks) n_chunks = 1;
+    std::vector<int> cb(n_chunks + 1, n_walk);
+    cb[0] = 0;
+    for (int c = 1, k = 0; c < n_chunks; ++c) {
+        const int64_t target = (ne + ns) * c / n_chunks;
+        while (k < n_walk && off[k].e + off[k].s < target) ++k;
+        cb[c] = k;
     }
-    if (bad_id >= 0) return fail(PGF_ERR_ARG, "walk %d has an EPJ/SPJ id outside the sent arrays", bad_id);
-    // Work queue: walks by descending cost, EP-SP pairs weighted by their
-    // larger instruction count.
-    {
-        std::vector<int32_t> ord(n_walk);
-        std::iota(ord.begin(), ord.end(), 0);
-        std::vector<double> cost(n_walk);
-        for (int w = 0; w < n_walk; ++w)
-            cost[w] = (double)n_epi[w] * ((double)n_epj[w] + 2.0 * (double)n_spj[w]) + 1.0;
-        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-        std::memcpy(t.h_order.h, ord.data(), sizeof(int32_t) * n_walk);
-    }
+
     t.n_walk = n_walk;
     t.ni_tot = ni;
     t.n_epi.assign(n_epi, n_epi + n_walk);
-    t.epi_disp = idisp;
     t.precision = g.precision;
     t.variant = g.variant;
-    g.prof.copy += now_s() - t0;
-
-    cudaStream_t s = g.stream;
-    PGF_CUDA(cudaEventRecord(t.ev[0], s));
-    if (ni) PGF_CUDA(cudaMemcpyAsync(t.epi.d, t.h_epi.h, ni * sizeof(EpiDev), cudaMemcpyHostToDevice, s));
-    if (ne) PGF_CUDA(cudaMemcpyAsync(t.id_epj.d, t.h_id_epj.h, ne * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-    if (ns) PGF_CUDA(cudaMemcpyAsync(t.id_spj.d, t.h_id_spj.h, ns * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-    if (n_walk) {
-        PGF_CUDA(cudaMemcpyAsync(t.walks.d, t.h_walks.h, n_walk * sizeof(WalkDesc), cudaMemcpyHostToDevice, s));
-        PGF_CUDA(cudaMemcpyAsync(t.order.d, t.h_order.h, n_walk * sizeof(int32_t), cudaMemcpyHostToDevice, s));
-    }
     Params& p = t.params;
     p = Params{};
     p.epi = t.epi.d;
@@ -465,12 +545,101 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     p.G = g.G;
     p.out_accp = t.accp.d;
     p.out_nnb = t.nnb.d;
+    bind_scratch(p);
     g.prof.n_walk += n_walk;
     g.prof.n_epi += ni;
     g.prof.n_epj += ne;
     g.prof.n_spj += ns;
     g.prof.n_call += 1;
-    return launch_tag(t);
+
+    auto pack_range = [&](int k0, int k1) -> int {
+        int bad_walk = -1;
+#pragma omp parallel for schedule(dynamic, 4) reduction(max : bad_walk)
+        for (int k = k0; k < k1; ++k)
+            if (!pack_walk(t, k, ord[k], off[k], epi, n_epi, il, id_epj, n_epj, id_spj, n_spj))
+                bad_walk = std::max(bad_walk, ord[k]);
+        return bad_walk;
+    };
+    // Host-to-device copies of layout positions [k0, k1) on stream s.
+    auto copy_range = [&](int k0, int k1, cudaStream_t s) -> int {
+        const Slot3 a = off[k0], b = off[k1];
+        if (b.i > a.i)
+            PGF_CUDA(cudaMemcpyAsync(t.epi.d + a.i, t.h_epi.h + a.i, (b.i - a.i) * sizeof(EpiDev),
+                                     cudaMemcpyHostToDevice, s));
+        if (b.e > a.e)
+            PGF_CUDA(cudaMemcpyAsync(t.id_epj.d + a.e, t.h_id_epj.h + a.e, (b.e - a.e) * sizeof(int32_t),
+                                     cudaMemcpyHostToDevice, s));
+        if (b.s > a.s)
+            PGF_CUDA(cudaMemcpyAsync(t.id_spj.d + a.s, t.h_id_spj.h + a.s, (b.s - a.s) * sizeof(int32_t),
+                                     cudaMemcpyHostToDevice, s));
+        if (k1 > k0) {
+            PGF_CUDA(cudaMemcpyAsync(t.walks.d + k0, t.h_walks.h + k0, (k1 - k0) * sizeof(WalkDesc),
+                                     cudaMemcpyHostToDevice, s));
+            PGF_CUDA(cudaMemcpyAsync(t.order.d + k0, t.h_order.h + k0, (k1 - k0) * sizeof(int32_t),
+                                     cudaMemcpyHostToDevice, s));
+        }
+        return PGF_OK;
+    };
+
+    if (n_chunks == 1) {
+        const int bad_walk = pack_range(0, n_walk);
+        g.prof.copy += now_s() - t0;
+        if (bad_walk >= 0) return fail(PGF_ERR_ARG, "walk %d has an EPJ/SPJ id outside the sent arrays", bad_walk);
+        PGF_CUDA(cudaEventRecord(t.ev[0], g.stream));
+        if (int r = copy_range(0, n_walk, g.stream)) return r;
+        return launch_tag(t);
+    }
+
+    // Pipelined stages.  The copy stream starts after everything already
+    // queued on the compute stream (the EPJ/SPJ copies); the compute stream
+    // resumes after every stage is done.
+    cudaStream_t cs = g.copy_stream;
+    auto drain = [&]() {
+        cudaStreamSynchronize(cs);
+        for (int c = 0; c < n_chunks; ++c) cudaStreamSynchronize(g.stage_stream[c]);
+    };
+    PGF_CUDA(cudaEventRecord(t.ev[0], g.stream));
+    PGF_CUDA(cudaStreamWaitEvent(cs, t.ev[0], 0));
+    double pack_s = now_s() - t0;
+    for (int c = 0; c < n_chunks; ++c) {
+        const int k0 = cb[c], k1 = cb[c + 1];
+        const double tp = now_s();
+        const int bad_walk = pack_range(k0, k1);
+        pack_s += now_s() - tp;
+        if (bad_walk >= 0) {
+            // Stages already launched use valid data; let them finish before
+            // the caller may touch the staging buffers again.
+            drain();
+            g.prof.copy += pack_s;
+            return fail(PGF_ERR_ARG, "walk %d has an EPJ/SPJ id outside the sent arrays", bad_walk);
+        }
+        cudaStream_t sc = g.stage_stream[c];
+        int r = PGF_OK;
+        if (cudaEventRecord(t.evc[c][0], cs) != cudaSuccess || (r = copy_range(k0, k1, cs)) != PGF_OK ||
+            cudaEventRecord(t.evc[c][1], cs) != cudaSuccess || cudaStreamWaitEvent(sc, t.evc[c][1], 0) != cudaSuccess) {
+            drain();
+            return r ? r : fail(PGF_ERR_CUDA, "pipelined copy of stage %d failed", c);
+        }
+        Params pc = p;
+        pc.order = t.order.d + k0;
+        pc.n_walk = k1 - k0;
+        bind_scratch(pc, c, n_chunks);
+        if ((r = launch_kernels(t, pc, sc, t.evc[c][2], t.evc[c][3])) != PGF_OK) {
+            drain();
+            return r;
+        }
+        if (cudaEventRecord(t.evc[c][4], sc) != cudaSuccess || cudaStreamWaitEvent(g.stream, t.evc[c][4], 0) != cudaSuccess) {
+            drain();
+            return fail(PGF_ERR_CUDA, "stage %d event failed", c);
+        }
+    }
+    PGF_CUDA(cudaEventRecord(t.ev[3], g.stream));
+    g.prof.copy += pack_s;
+    t.n_chunks = n_chunks;
+    t.dispatched = true;
+    t.has_data = true;
+    t.times_pending = true;
+    return PGF_OK;
 }
 
 bool valid_tag(int tag) { return tag >= 0 && tag < kMaxTags; }
@@ -605,6 +774,13 @@ int pgf_set_kernel_variant(int variant) {
     return PGF_OK;
 }
 
+int pgf_set_dispatch_stages(int stages) {
+    if (stages < 0 || stages > kMaxChunks)
+        return fail(PGF_ERR_ARG, "dispatch stages %d outside [0, %d]", stages, kMaxChunks);
+    g.stages = stages;
+    return PGF_OK;
+}
+
 int pgf_get_kernel_variant(int* variant) {
     if (!variant) return fail(PGF_ERR_ARG, "NULL variant");
     *variant = g.variant;
@@ -669,7 +845,8 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
         PGF_CUDA(cudaMemcpyAsync(t.h_accp.h, t.accp.d, n * sizeof(Accp), cudaMemcpyDeviceToHost, s));
         PGF_CUDA(cudaMemcpyAsync(t.h_nnb.h, t.nnb.d, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     }
-    PGF_CUDA(cudaMemcpyAsync(t.h_flags.h, g.scratch.d, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    PGF_CUDA(cudaMemcpyAsync(t.h_flags.h, g.scratch.d, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    PGF_CUDA(cudaMemsetAsync(g.scratch.d + 2, 0, 2 * sizeof(int32_t), s));
     PGF_CUDA(cudaEventRecord(t.ev[5], s));
     PGF_CUDA(cudaEventSynchronize(t.ev[5]));
     t.dispatched = false;
@@ -677,7 +854,7 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
     float ms_recv = 0;
     cudaEventElapsedTime(&ms_recv, t.ev[4], t.ev[5]);
     g.prof.recv += 1e-3 * ms_recv;
-    g.prof.n_retest += t.h_flags.h[1];
+    g.prof.n_retest += t.h_flags.h[3];
     if (t.h_flags.h[2] != 0) return fail(PGF_ERR_DEVICE, "device error word %d", t.h_flags.h[2]);
     const double t0 = now_s();
 #pragma omp parallel for schedule(dynamic, 8)
@@ -730,6 +907,9 @@ int pgf_finalize(void) {
     if (!g.init) return PGF_OK;
     cudaSetDevice(g.device);
     cudaStreamSynchronize(g.stream);
+    if (g.copy_stream) cudaStreamSynchronize(g.copy_stream);
+    for (auto& st : g.stage_stream)
+        if (st) cudaStreamSynchronize(st);
     for (auto& t : g.tags) {
         t.epi.release();
         t.id_epj.release();
@@ -750,6 +930,12 @@ int pgf_finalize(void) {
             if (ev) cudaEventDestroy(ev);
             ev = nullptr;
         }
+        for (auto& c : t.evc)
+            for (auto& ev : c) {
+                if (ev) cudaEventDestroy(ev);
+                ev = nullptr;
+            }
+        t.n_chunks = 0;
         t.dispatched = t.has_data = false;
     }
     g.epj.release();
@@ -769,6 +955,12 @@ int pgf_finalize(void) {
     g.ev_send0 = g.ev_send1 = nullptr;
     if (g.own_stream) cudaStreamDestroy(g.own_stream);
     g.own_stream = nullptr;
+    if (g.copy_stream) cudaStreamDestroy(g.copy_stream);
+    g.copy_stream = nullptr;
+    for (auto& st : g.stage_stream) {
+        if (st) cudaStreamDestroy(st);
+        st = nullptr;
+    }
     if (!g.user_stream) g.stream = nullptr;
     g.j_sent = false;
     g.init = false;

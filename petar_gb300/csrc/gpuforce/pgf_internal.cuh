@@ -105,6 +105,7 @@ struct Params {
     int32_t retest_cap;
     int32_t pad1;
     int32_t* err;          // device error word (0 = ok)
+    int32_t* retest_total; // records re-tested since the host last read it (optional)
 };
 
 // Exact FP64 neighbour test of one pair, in the oracle's evaluation order
@@ -125,7 +126,7 @@ cudaError_t launch_fp64(const Params& p, cudaStream_t s, int num_sms);
 cudaError_t launch_mixed(const Params& p, cudaStream_t s, int num_sms);
 cudaError_t launch_retest(const Params& p, cudaStream_t s, int num_sms);
 // Warp-specialised kernel, variants 0..kNumWsVariants-1 (see pgf_kernels_ws.cu).
-constexpr int kNumWsVariants = 4;
+constexpr int kNumWsVariants = 8;
 cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant);
 
 }  // namespace pgf

@@ -518,6 +518,7 @@ __global__ __launch_bounds__(kThreads, PGF_MINB) void mixed_kernel(Params p) {
 // the neighbour count the interaction kernel wrote.
 __global__ __launch_bounds__(256) void retest_kernel(Params p) {
     const int n_rec = min(*p.n_retest, p.retest_cap);
+    if (p.retest_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(p.retest_total, *p.n_retest);
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;

@@ -110,6 +110,7 @@ __device__ __forceinline__ void consumers_sync(int n_threads) {
     asm volatile("bar.sync 1, %0;" ::"r"(n_threads) : "memory");
 }
 
+// Scalar tiles: one float4 record per j.
 struct SlotEP {
     float4 nh[kTileEP];  // near: hi x, y, z, m
     float4 nl[kTileEP];  // near: lo x, y, z, rs2
@@ -119,10 +120,29 @@ struct SlotEP {
 struct SlotSP {
     float4 sp[kTileSP][3];
 };
+// Packed tiles: far EPJ and SPJ as pairs of j, component-interleaved, so a
+// consumer reads (x0, x1), (y0, y1), ... as float2 operands of the FP32x2
+// instructions.  An odd last entry is paired with a massless dummy at 1e15.
+struct SlotEPx2 {
+    float4 nh[kTileEP];
+    float4 nl[kTileEP];
+    float4 fp[kTileEP / 2][2];  // (x0 x1 y0 y1), (z0 z1 m0 m1)
+    int nidx[kTileEP];
+};
+struct SlotSPx2 {
+    float4 sp[kTileSP / 2][6];  // x, y, z, m, -Qxx, -Qyy, -Qzz, -Qxy, -Qxz, -Qyz, -c (pairs), pad
+};
+template <bool PK>
 union Slot {
     SlotEP ep;
     SlotSP sp;
 };
+template <>
+union Slot<true> {
+    SlotEPx2 ep;
+    SlotSPx2 sp;
+};
+constexpr float kDummyPos = 1e15f;
 struct Hdr {
     int kind;
     int nn;     // near entries (EP), entries (SP)
@@ -133,9 +153,9 @@ struct Hdr {
     int64_t base;  // first list entry of the tile
 };
 
-template <int CW, int KI>
+template <int CW, int KI, bool PK>
 struct Smem {
-    Slot slot[kSlots];
+    Slot<PK> slot[kSlots];
     Hdr hdr[kSlots];
     uint64_t full[kSlots];
     uint64_t empty[kSlots];
@@ -145,8 +165,8 @@ struct Smem {
 
 // ---------------------------------------------------------------- producer
 
-template <int CW, int KI>
-__device__ void producer(const Params& p, Smem<CW, KI>& s, int lane) {
+template <int CW, int KI, bool PK>
+__device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
     constexpr int kMaxPass = CW * 32 * KI;
     const float eps2 = (float)p.eps2;
     unsigned item = 0;
@@ -210,7 +230,7 @@ __device__ void producer(const Params& p, Smem<CW, KI>& s, int lane) {
                     }
                 }
                 if (!acquire(sl)) return;
-                SlotEP& S = s.slot[sl].ep;
+                auto& S = s.slot[sl].ep;
                 int nn = 0, nf = 0;
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
@@ -250,10 +270,26 @@ __device__ void producer(const Params& p, Smem<CW, KI>& s, int lane) {
                         S.nl[pos] = make_float4(lx, ly, lz, rs2);
                         S.nidx[pos] = e;
                     } else if (valid) {
-                        S.fr[nf + __popc(bf & lt)] = make_float4(hx, hy, hz, m);
+                        const int pos = nf + __popc(bf & lt);
+                        if constexpr (PK) {
+                            float* f = reinterpret_cast<float*>(&S.fp[pos >> 1][0]) + (pos & 1);
+                            f[0] = hx;
+                            f[2] = hy;
+                            f[4] = hz;
+                            f[6] = m;
+                        } else {
+                            S.fr[pos] = make_float4(hx, hy, hz, m);
+                        }
                     }
                     nn += __popc(bn);
                     nf += __popc(bf);
+                }
+                if constexpr (PK) {
+                    if ((nf & 1) && lane == 0) {
+                        float* f = reinterpret_cast<float*>(&S.fp[nf >> 1][0]) + 1;
+                        f[0] = f[2] = f[4] = kDummyPos;
+                        f[6] = 0.f;
+                    }
                 }
                 if (lane == 0) {
                     s.hdr[sl].kind = kItemEP;
@@ -283,7 +319,7 @@ __device__ void producer(const Params& p, Smem<CW, KI>& s, int lane) {
                     }
                 }
                 if (!acquire(sl)) return;
-                SlotSP& S = s.slot[sl].sp;
+                auto& S = s.slot[sl].sp;
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {
                     const int e = q * 32 + lane;
@@ -291,11 +327,34 @@ __device__ void producer(const Params& p, Smem<CW, KI>& s, int lane) {
                         const float hx = (float)(as_double(r[q][0].x, r[q][0].y) - cx);
                         const float hy = (float)(as_double(r[q][0].z, r[q][0].w) - cy);
                         const float hz = (float)(as_double(r[q][1].x, r[q][1].y) - cz);
-                        S.sp[e][0] = make_float4(hx, hy, hz, __uint_as_float(r[q][1].z));
-                        S.sp[e][1] = make_float4(__uint_as_float(r[q][2].x), __uint_as_float(r[q][2].y),
-                                                 __uint_as_float(r[q][2].z), __uint_as_float(r[q][2].w));
-                        S.sp[e][2] = make_float4(__uint_as_float(r[q][3].x), __uint_as_float(r[q][3].y),
-                                                 -__uint_as_float(r[q][3].z) * eps2, 0.f);
+                        const float m = __uint_as_float(r[q][1].z);
+                        const float c = -__uint_as_float(r[q][3].z) * eps2;
+                        if constexpr (PK) {
+                            float* f = reinterpret_cast<float*>(&S.sp[e >> 1][0]) + (e & 1);
+                            f[0] = hx;
+                            f[2] = hy;
+                            f[4] = hz;
+                            f[6] = m;
+                            f[8] = -__uint_as_float(r[q][2].x);
+                            f[10] = -__uint_as_float(r[q][2].y);
+                            f[12] = -__uint_as_float(r[q][2].z);
+                            f[14] = -__uint_as_float(r[q][2].w);
+                            f[16] = -__uint_as_float(r[q][3].x);
+                            f[18] = -__uint_as_float(r[q][3].y);
+                            f[20] = -c;
+                        } else {
+                            S.sp[e][0] = make_float4(hx, hy, hz, m);
+                            S.sp[e][1] = make_float4(__uint_as_float(r[q][2].x), __uint_as_float(r[q][2].y),
+                                                     __uint_as_float(r[q][2].z), __uint_as_float(r[q][2].w));
+                            S.sp[e][2] = make_float4(__uint_as_float(r[q][3].x), __uint_as_float(r[q][3].y), c, 0.f);
+                        }
+                    }
+                }
+                if constexpr (PK) {
+                    if ((nt & 1) && lane == 0) {
+                        float* f = reinterpret_cast<float*>(&S.sp[nt >> 1][0]) + 1;
+                        f[0] = f[2] = f[4] = kDummyPos;
+                        for (int u = 6; u <= 20; u += 2) f[u] = 0.f;
                     }
                 }
                 if (lane == 0) {
@@ -315,8 +374,8 @@ __device__ void producer(const Params& p, Smem<CW, KI>& s, int lane) {
 
 // ---------------------------------------------------------------- consumer
 
-template <int CW, int KI>
-__device__ void consumer(const Params& p, Smem<CW, KI>& s, int ct) {
+template <int CW, int KI, bool PK>
+__device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
     constexpr int CT = CW * 32;
     constexpr int kMaxPass = CT * KI;
     const double eps2d = p.eps2;
@@ -332,6 +391,10 @@ __device__ void consumer(const Params& p, Smem<CW, KI>& s, int ct) {
     int kb[KI], gi[KI], cnt[KI];
     bool valid[KI];
     float a[KI][4];
+    // Packed path: (-x_i, -x_i) operands and pair accumulators: b[0..2] the
+    // acceleration, b[3] minus the potential.
+    float2 nx2[KI], ny2[KI], nz2[KI];
+    float2 b[KI][4];
     int since = 0;
 #pragma unroll
     for (int k = 0; k < KI; ++k) {
@@ -339,16 +402,28 @@ __device__ void consumer(const Params& p, Smem<CW, KI>& s, int ct) {
         kb[k] = gi[k] = cnt[k] = 0;
         valid[k] = false;
         a[k][0] = a[k][1] = a[k][2] = a[k][3] = 0.f;
+        nx2[k] = ny2[k] = nz2[k] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) b[k][q] = make_float2(0.f, 0.f);
     }
 
     auto flush = [&]() {
 #pragma unroll
-        for (int k = 0; k < KI; ++k)
+        for (int k = 0; k < KI; ++k) {
+            if constexpr (PK) {
+                a[k][0] += b[k][0].x + b[k][0].y;
+                a[k][1] += b[k][1].x + b[k][1].y;
+                a[k][2] += b[k][2].x + b[k][2].y;
+                a[k][3] -= b[k][3].x + b[k][3].y;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) b[k][q] = make_float2(0.f, 0.f);
+            }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 s.acc[k][q][ct] += (double)a[k][q];
                 a[k][q] = 0.f;
             }
+        }
         since = 0;
     };
     auto push_retest = [&](int k, int64_t jidx) -> int {
@@ -402,6 +477,11 @@ __device__ void consumer(const Params& p, Smem<CW, KI>& s, int ct) {
                     rsi2[k] = (float)(e.rs * e.rs);
                     kb[k] = kband_near(fmax(fabs(dx), fmax(fabs(dy), fabs(dz))), e.rs, eps2d);
                 }
+                nx2[k] = make_float2(-xih[k], -xih[k]);
+                ny2[k] = make_float2(-yih[k], -yih[k]);
+                nz2[k] = make_float2(-zih[k], -zih[k]);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) b[k][q] = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     a[k][q] = 0.f;
@@ -411,7 +491,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI>& s, int ct) {
             since = 0;
         } else if (h.kind == kItemEP) {
             if (active) {
-                const SlotEP& T = s.slot[sl].ep;
+                const auto& T = s.slot[sl].ep;
                 int c[KI];
 #pragma unroll
                 for (int k = 0; k < KI; ++k) c[k] = 0;
@@ -443,37 +523,120 @@ __device__ void consumer(const Params& p, Smem<CW, KI>& s, int ct) {
                         a[k][3] -= mri;
                     }
                 }
-                const int pf = (h.nf + n_js - 1) / n_js;
-                const int f0 = min(h.nf, js * pf);
-                const int f1 = min(h.nf, f0 + pf);
-#pragma unroll 4
-                for (int j = f0; j < f1; ++j) {
-                    const float4 hh = T.fr[j];
+                int nfar;
+                if constexpr (PK) {
+                    // far pairs of j, two per FP32x2 instruction
+                    const int np = (h.nf + 1) >> 1;
+                    const int pp = (np + n_js - 1) / n_js;
+                    const int f0 = min(np, js * pp);
+                    const int f1 = min(np, f0 + pp);
+                    const float2 e2 = make_float2(eps2, eps2);
+#pragma unroll 2
+                    for (int j = f0; j < f1; ++j) {
+                        const float4 u = T.fp[j][0];
+                        const float4 v = T.fp[j][1];
+                        const float2 X = make_float2(u.x, u.y), Y = make_float2(u.z, u.w);
+                        const float2 Z = make_float2(v.x, v.y), M = make_float2(v.z, v.w);
 #pragma unroll
-                    for (int k = 0; k < KI; ++k) {
-                        const float dx = hh.x - xih[k];
-                        const float dy = hh.y - yih[k];
-                        const float dz = hh.z - zih[k];
-                        float r2 = fmaf(dx, dx, eps2);
-                        r2 = fmaf(dy, dy, r2);
-                        r2 = fmaf(dz, dz, r2);
-                        const float ri = rsqrt_approx(r2);
-                        const float mri = hh.w * ri;
-                        const float mri3 = mri * (ri * ri);
-                        a[k][0] = fmaf(mri3, dx, a[k][0]);
-                        a[k][1] = fmaf(mri3, dy, a[k][1]);
-                        a[k][2] = fmaf(mri3, dz, a[k][2]);
-                        a[k][3] -= mri;
+                        for (int k = 0; k < KI; ++k) {
+                            const float2 dx = __fadd2_rn(X, nx2[k]);
+                            const float2 dy = __fadd2_rn(Y, ny2[k]);
+                            const float2 dz = __fadd2_rn(Z, nz2[k]);
+                            float2 r2 = __ffma2_rn(dx, dx, e2);
+                            r2 = __ffma2_rn(dy, dy, r2);
+                            r2 = __ffma2_rn(dz, dz, r2);
+                            const float2 ri = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+                            const float2 mri = __fmul2_rn(M, ri);
+                            const float2 mri3 = __fmul2_rn(mri, __fmul2_rn(ri, ri));
+                            b[k][0] = __ffma2_rn(mri3, dx, b[k][0]);
+                            b[k][1] = __ffma2_rn(mri3, dy, b[k][1]);
+                            b[k][2] = __ffma2_rn(mri3, dz, b[k][2]);
+                            b[k][3] = __fadd2_rn(b[k][3], mri);
+                        }
                     }
+                    nfar = 2 * (f1 - f0);
+                } else {
+                    const int pf = (h.nf + n_js - 1) / n_js;
+                    const int f0 = min(h.nf, js * pf);
+                    const int f1 = min(h.nf, f0 + pf);
+#pragma unroll 4
+                    for (int j = f0; j < f1; ++j) {
+                        const float4 hh = T.fr[j];
+#pragma unroll
+                        for (int k = 0; k < KI; ++k) {
+                            const float dx = hh.x - xih[k];
+                            const float dy = hh.y - yih[k];
+                            const float dz = hh.z - zih[k];
+                            float r2 = fmaf(dx, dx, eps2);
+                            r2 = fmaf(dy, dy, r2);
+                            r2 = fmaf(dz, dz, r2);
+                            const float ri = rsqrt_approx(r2);
+                            const float mri = hh.w * ri;
+                            const float mri3 = mri * (ri * ri);
+                            a[k][0] = fmaf(mri3, dx, a[k][0]);
+                            a[k][1] = fmaf(mri3, dy, a[k][1]);
+                            a[k][2] = fmaf(mri3, dz, a[k][2]);
+                            a[k][3] -= mri;
+                        }
+                    }
+                    nfar = f1 - f0;
                 }
 #pragma unroll
                 for (int k = 0; k < KI; ++k) cnt[k] += c[k];
-                since += (j1 - j0) + (f1 - f0);
+                since += (j1 - j0) + nfar;
                 if (since >= kFlush) flush();
             }
         } else if (h.kind == kItemSP) {
             if (active) {
-                const SlotSP& T = s.slot[sl].sp;
+              if constexpr (PK) {
+                const auto& T = s.slot[sl].sp;
+                const int np = (h.nn + 1) >> 1;
+                const int pp = (np + n_js - 1) / n_js;
+                const int j0 = min(np, js * pp);
+                const int j1 = min(np, j0 + pp);
+                const float2 e2 = make_float2(eps2, eps2);
+#pragma unroll 1
+                for (int j = j0; j < j1; ++j) {
+                    const float4 w0 = T.sp[j][0], w1 = T.sp[j][1], w2 = T.sp[j][2];
+                    const float4 w3 = T.sp[j][3], w4 = T.sp[j][4], w5 = T.sp[j][5];
+                    const float2 X = make_float2(w0.x, w0.y), Y = make_float2(w0.z, w0.w);
+                    const float2 Z = make_float2(w1.x, w1.y), M = make_float2(w1.z, w1.w);
+                    // nQ = -Q and nC = -c, so that the terms below need no negation:
+                    // with u = d.(-Q).d - c = -(d.Q.d + c) and t = u / r^5,
+                    // acc += (m/r^3 - 2.5 t/r^2) d + (-Q).d / r^5 and
+                    // -pot += m/r - 0.5 t.
+                    const float2 Qxx = make_float2(w2.x, w2.y), Qyy = make_float2(w2.z, w2.w);
+                    const float2 Qzz = make_float2(w3.x, w3.y), Qxy = make_float2(w3.z, w3.w);
+                    const float2 Qxz = make_float2(w4.x, w4.y), Qyz = make_float2(w4.z, w4.w);
+                    const float2 C = make_float2(w5.x, w5.y);
+                    const float2 km25 = make_float2(-2.5f, -2.5f), km05 = make_float2(-0.5f, -0.5f);
+#pragma unroll
+                    for (int k = 0; k < KI; ++k) {
+                        const float2 dx = __fadd2_rn(X, nx2[k]);
+                        const float2 dy = __fadd2_rn(Y, ny2[k]);
+                        const float2 dz = __fadd2_rn(Z, nz2[k]);
+                        float2 r2 = __ffma2_rn(dx, dx, e2);
+                        r2 = __ffma2_rn(dy, dy, r2);
+                        r2 = __ffma2_rn(dz, dz, r2);
+                        const float2 ri = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+                        const float2 qdx = __ffma2_rn(Qxx, dx, __ffma2_rn(Qxy, dy, __fmul2_rn(Qxz, dz)));
+                        const float2 qdy = __ffma2_rn(Qxy, dx, __ffma2_rn(Qyy, dy, __fmul2_rn(Qyz, dz)));
+                        const float2 qdz = __ffma2_rn(Qxz, dx, __ffma2_rn(Qyz, dy, __fmul2_rn(Qzz, dz)));
+                        const float2 sq = __ffma2_rn(qdx, dx, __ffma2_rn(qdy, dy, __ffma2_rn(qdz, dz, C)));
+                        const float2 ri2 = __fmul2_rn(ri, ri);
+                        const float2 ri3 = __fmul2_rn(ri2, ri);
+                        const float2 ri5 = __fmul2_rn(ri3, ri2);
+                        const float2 tq = __fmul2_rn(sq, ri5);
+                        const float2 A = __ffma2_rn(__fmul2_rn(tq, ri2), km25, __fmul2_rn(M, ri3));
+                        b[k][0] = __ffma2_rn(A, dx, __ffma2_rn(ri5, qdx, b[k][0]));
+                        b[k][1] = __ffma2_rn(A, dy, __ffma2_rn(ri5, qdy, b[k][1]));
+                        b[k][2] = __ffma2_rn(A, dz, __ffma2_rn(ri5, qdz, b[k][2]));
+                        b[k][3] = __ffma2_rn(tq, km05, __ffma2_rn(M, ri, b[k][3]));
+                    }
+                }
+                since += 2 * (j1 - j0);
+              } else {
+                const auto& T = s.slot[sl].sp;
                 const int ps = (h.nn + n_js - 1) / n_js;
                 const int j0 = min(h.nn, js * ps);
                 const int j1 = min(h.nn, j0 + ps);
@@ -507,7 +670,8 @@ __device__ void consumer(const Params& p, Smem<CW, KI>& s, int ct) {
                     }
                 }
                 since += j1 - j0;
-                if (since >= kFlush) flush();
+              }
+              if (since >= kFlush) flush();
             }
         } else {  // kItemEnd: reduce the j-slices of the pass and write
             if (active) {
@@ -540,10 +704,10 @@ __device__ void consumer(const Params& p, Smem<CW, KI>& s, int ct) {
     }
 }
 
-template <int CW, int KI, int MINB>
+template <int CW, int KI, int MINB, bool PK>
 __global__ __launch_bounds__((CW + 1) * 32, MINB) void ws_kernel(Params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    Smem<CW, KI>& s = *reinterpret_cast<Smem<CW, KI>*>(smem_raw);
+    Smem<CW, KI, PK>& s = *reinterpret_cast<Smem<CW, KI, PK>*>(smem_raw);
     const int tid = threadIdx.x;
     if (tid == 0) {
         for (int i = 0; i < kSlots; ++i) {
@@ -553,29 +717,30 @@ __global__ __launch_bounds__((CW + 1) * 32, MINB) void ws_kernel(Params p) {
     }
     __syncthreads();
     if (tid >= CW * 32)
-        producer<CW, KI>(p, s, tid - CW * 32);
+        producer<CW, KI, PK>(p, s, tid - CW * 32);
     else
-        consumer<CW, KI>(p, s, tid);
+        consumer<CW, KI, PK>(p, s, tid);
 }
 
-template <int CW, int KI, int MINB>
+template <int CW, int KI, int MINB, bool PK>
 cudaError_t launch_ws_t(const Params& p, cudaStream_t st, int num_sms) {
     cudaError_t e = cudaMemsetAsync(p.queue_head, 0, sizeof(int32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), st);
     if (e != cudaSuccess) return e;
     if (p.n_walk <= 0) return cudaSuccess;
     static int per_sm = 0;
-    const size_t smem = sizeof(Smem<CW, KI>);
+    const size_t smem = sizeof(Smem<CW, KI, PK>);
     if (per_sm == 0) {
-        e = cudaFuncSetAttribute(ws_kernel<CW, KI, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(ws_kernel<CW, KI, MINB, PK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ws_kernel<CW, KI, MINB>, (CW + 1) * 32, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ws_kernel<CW, KI, MINB, PK>, (CW + 1) * 32, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
     int grid = num_sms * per_sm;
     if (grid > p.n_walk) grid = p.n_walk;
-    ws_kernel<CW, KI, MINB><<<grid, (CW + 1) * 32, smem, st>>>(p);
+    ws_kernel<CW, KI, MINB, PK><<<grid, (CW + 1) * 32, smem, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -585,10 +750,14 @@ cudaError_t launch_ws_t(const Params& p, cudaStream_t st, int num_sms) {
 // thread, minimum CTAs per SM.
 cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant) {
     switch (variant) {
-        case 0: return launch_ws_t<4, 3, 4>(p, s, num_sms);
-        case 1: return launch_ws_t<4, 2, 4>(p, s, num_sms);
-        case 2: return launch_ws_t<4, 2, 5>(p, s, num_sms);
-        case 3: return launch_ws_t<8, 2, 3>(p, s, num_sms);
+        case 0: return launch_ws_t<4, 3, 4, false>(p, s, num_sms);
+        case 1: return launch_ws_t<4, 2, 4, false>(p, s, num_sms);
+        case 2: return launch_ws_t<4, 2, 5, false>(p, s, num_sms);
+        case 3: return launch_ws_t<8, 2, 3, false>(p, s, num_sms);
+        case 4: return launch_ws_t<4, 2, 4, true>(p, s, num_sms);
+        case 5: return launch_ws_t<4, 2, 5, true>(p, s, num_sms);
+        case 6: return launch_ws_t<4, 1, 5, true>(p, s, num_sms);
+        case 7: return launch_ws_t<8, 2, 3, true>(p, s, num_sms);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -121,6 +121,7 @@ def load(build: bool = True) -> ctypes.CDLL:
         "pgf_set_walk_rcut2": [vp, ci],
         "pgf_recompute": [ci],
         "pgf_set_kernel_variant": [ci],
+        "pgf_set_dispatch_stages": [ci],
         "pgf_get_kernel_variant": [vp],
         "pgf_autotune": [ci, ci, vp, vp],
         "pgf_wait": [ci],
@@ -181,6 +182,11 @@ def set_walk_rcut2(walk_rcut2: np.ndarray | None) -> None:
 
 def set_kernel_variant(variant: int) -> None:
     _check(load().pgf_set_kernel_variant(variant))
+
+
+def set_dispatch_stages(stages: int) -> None:
+    """Pipeline stages of index dispatches (0: by size, 1: none, 2..8: forced)."""
+    _check(load().pgf_set_dispatch_stages(stages))
 
 
 def get_kernel_variant() -> int:

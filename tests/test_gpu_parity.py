@@ -217,7 +217,7 @@ def test_recompute_reproduces():
     np.testing.assert_array_equal(a["acc"], b["acc"])
 
 
-@pytest.mark.parametrize("variant", list(range(1, 5)))
+@pytest.mark.parametrize("variant", list(range(1, 9)))
 @pytest.mark.parametrize("case", ["kernel_test_rsvar", "plummer2048_walks", "ragged", "binaries"])
 def test_kernel_variants(case, variant):
     """Every mixed-precision kernel variant the autotuner may pick meets the
@@ -244,9 +244,67 @@ def test_autotune_picks_a_variant_and_keeps_results():
     gpuforce.dispatch(rec, tag=0)
     gpuforce.retrieve(rec, tag=0)
     best, ms = gpuforce.autotune(0, repeats=2)
-    assert 0 <= best < 5 and ms > 0
+    assert 0 <= best < 9 and ms > 0
     assert gpuforce.get_kernel_variant() == best
     gpuforce.recompute(0)
     f = gpuforce.retrieve(rec, tag=0)
     check(wb, dict(acc=f["acc"], pot=f["pot"], nnb=f["n_ngb"]), PGF_PRECISION_MIXED, o=o, label="autotuned")
     gpuforce.set_kernel_variant(0)
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+def test_pipelined_dispatch_matches_single_launch(variant):
+    """A dispatch split into pipeline stages (overlapped packing, copies and
+    kernels over contiguous walk ranges) gives bit-identical forces, counts
+    and re-test totals to one launch over all walks, and so does the globally
+    ordered recompute after it."""
+    wb = walks.build_walks(ics.make_plummer_cluster(23, 30000, 0.004, binary_fraction=0.5))
+    rec = gpuforce.Records(wb)
+    gpuforce.set_precision(PGF_PRECISION_MIXED)
+    gpuforce.set_kernel_variant(variant)
+    out = {}
+    try:
+        for stages in (1, 2, 3, 8):
+            gpuforce.set_dispatch_stages(stages)
+            gpuforce.clear_profile()
+            gpuforce.dispatch(rec, tag=0)
+            f = gpuforce.retrieve(rec, tag=0).copy()
+            out[stages] = (f, gpuforce.get_profile()["n_retest"])
+        gpuforce.set_dispatch_stages(8)
+        gpuforce.dispatch(rec, tag=0)
+        gpuforce.retrieve(rec, tag=0)
+        gpuforce.recompute(0)
+        out["recompute"] = (gpuforce.retrieve(rec, tag=0).copy(), None)
+    finally:
+        gpuforce.set_dispatch_stages(0)
+        gpuforce.set_kernel_variant(0)
+    f1, r1 = out[1]
+    for key in (2, 3, 8, "recompute"):
+        f, r = out[key]
+        np.testing.assert_array_equal(f["n_ngb"], f1["n_ngb"])
+        np.testing.assert_array_equal(f["acc"], f1["acc"])
+        np.testing.assert_array_equal(f["pot"], f1["pot"])
+        if r is not None:
+            assert r == r1, (key, r, r1)
+    check(wb, dict(acc=f1["acc"], pot=f1["pot"], nnb=f1["n_ngb"]), PGF_PRECISION_MIXED, label="stages")
+
+
+def test_pipelined_dispatch_rejects_bad_id_in_late_stage():
+    """An out-of-range id in the last stage is reported after earlier stages
+    were launched; the library stays usable."""
+    wb, _ = load_golden("plummer2048_walks")
+    bad = wb.id_epj.copy()
+    bad[-1] = wb.epj_mass.size
+    good_ids = wb.id_epj
+    gpuforce.set_dispatch_stages(3)  # 27 walks: three stages of nine
+    try:
+        wb.id_epj = bad
+        with pytest.raises(gpuforce.GpuForceError) as e:
+            gpuforce.compute(wb)
+        assert e.value.code == 1
+        wb.id_epj = good_ids
+        res = gpuforce.compute(wb)
+    finally:
+        gpuforce.set_dispatch_stages(0)
+        wb.id_epj = good_ids
+    check(wb, res, PGF_PRECISION_MIXED, label="after bad id")
