@@ -145,6 +145,8 @@ struct State {
     DevBuf<double> epj_m64, epj_rs64;
     DevBuf<SpjMix> spj;
     DevBuf<SpjQ64> spj_q64;
+    DevBuf<EpjF32> epj32;  // (hi, lo) FP32 copies built on the device
+    DevBuf<SpjF32> spj32;
     HostBuf<EpjMix> h_epj;
     HostBuf<double> h_epj_m64, h_epj_rs64;
     HostBuf<SpjMix> h_spj;
@@ -161,6 +163,7 @@ struct State {
     TagState tags[kMaxTags];
     pgf_profile prof{};
     cudaEvent_t ev_send0 = nullptr, ev_send1 = nullptr;
+    bool send_pending = false;  // j copies queued, time not yet in the profile
 };
 
 State g;
@@ -215,6 +218,17 @@ inline const double* dptr(const void* base, size_t off) {
     return reinterpret_cast<const double*>(reinterpret_cast<const char*>(base) + off);
 }
 
+// Adds the time of the last j send to the profile once its copies are done.
+void harvest_send(bool wait = false) {
+    if (!g.send_pending) return;
+    if (wait) cudaEventSynchronize(g.ev_send1);
+    if (cudaEventQuery(g.ev_send1) != cudaSuccess) return;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, g.ev_send0, g.ev_send1);
+    g.prof.send += 1e-3 * ms;
+    g.send_pending = false;
+}
+
 // Packs the shared EPJ / SPJ arrays (the send_flag phase,
 // src/force_gpu_cuda.cu:577-619).
 int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, const void* spj,
@@ -226,6 +240,7 @@ int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, co
     // pending copies may still read the pinned staging: finish them before
     // either is reused or reallocated.
     PGF_CUDA(cudaStreamSynchronize(g.stream));
+    harvest_send();
     const double t0 = now_s();
     PGF_CUDA(g.h_epj.ensure(n_epj));
     PGF_CUDA(g.h_epj_m64.ensure(n_epj));
@@ -237,6 +252,8 @@ int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, co
     PGF_CUDA(g.epj_rs64.ensure(n_epj));
     PGF_CUDA(g.spj.ensure(n_spj));
     PGF_CUDA(g.spj_q64.ensure(n_spj));
+    PGF_CUDA(g.epj32.ensure(n_epj));
+    PGF_CUDA(g.spj32.ensure(n_spj));
 #pragma omp parallel for schedule(static)
     for (int64_t j = 0; j < n_epj; ++j) {
         const char* r = reinterpret_cast<const char*>(epj) + j * el->size;
@@ -294,11 +311,14 @@ int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, co
         PGF_CUDA(cudaMemcpyAsync(g.spj_q64.d, g.h_spj_q64.h, n_spj * sizeof(SpjQ64), cudaMemcpyHostToDevice,
                                  g.stream));
     }
+    {
+        const cudaError_t e = launch_split_j(g.epj.d, n_epj, g.epj32.d, g.spj.d, n_spj, g.spj32.d, g.stream);
+        if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "j split kernel failed: %s", cudaGetErrorString(e));
+    }
+    // The copies run behind the caller's next steps (walk packing); the
+    // staging is not written again before the next send, which waits first.
     PGF_CUDA(cudaEventRecord(g.ev_send1, g.stream));
-    PGF_CUDA(cudaEventSynchronize(g.ev_send1));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, g.ev_send0, g.ev_send1);
-    g.prof.send += 1e-3 * ms;
+    g.send_pending = true;
     g.n_epj_tot = n_epj;
     g.n_spj_tot = n_spj;
     g.j_sent = true;
@@ -536,6 +556,8 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     p.epj_rs64 = g.epj_rs64.d;
     p.spj = g.spj.d;
     p.spj_q64 = g.spj_q64.d;
+    p.epj32 = g.epj32.d;
+    p.spj32 = g.spj32.d;
     p.id_epj = t.id_epj.d;
     p.id_spj = t.id_spj.d;
     p.walks = t.walks.d;
@@ -851,6 +873,7 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
     PGF_CUDA(cudaEventSynchronize(t.ev[5]));
     t.dispatched = false;
     harvest_times(t);
+    harvest_send();
     float ms_recv = 0;
     cudaEventElapsedTime(&ms_recv, t.ev[4], t.ev[5]);
     g.prof.recv += 1e-3 * ms_recv;
@@ -887,11 +910,13 @@ int pgf_wait(int tag) {
     PGF_CUDA(cudaSetDevice(g.device));
     PGF_CUDA(cudaEventSynchronize(t.ev[3]));
     harvest_times(t);
+    harvest_send();
     return PGF_OK;
 }
 
 int pgf_get_profile(pgf_profile* out) {
     if (!out) return fail(PGF_ERR_ARG, "NULL profile");
+    if (g.init) harvest_send();
     *out = g.prof;
     return PGF_OK;
 }
@@ -943,6 +968,8 @@ int pgf_finalize(void) {
     g.epj_rs64.release();
     g.spj.release();
     g.spj_q64.release();
+    g.epj32.release();
+    g.spj32.release();
     g.h_epj.release();
     g.h_epj_m64.release();
     g.h_epj_rs64.release();

@@ -7,6 +7,10 @@
 //   SpjMix[n_spj_tot]    64 B: FP64 position, FP32 mass, FP32 traceless
 //                              quadrupole Q = 3q - tr(q) I and tr(q)
 //   SpjQ64[n_spj_tot]    64 B: FP64 mass and raw quadrupole (plain FP64 kernel)
+//   EpjF32[n_epj_tot]    32 B: position as an FP32 (hi, lo) pair, FP32 mass
+//                              and r_search^2 (warp-specialised kernels)
+//   SpjF32[n_spj_tot]    64 B: position as an FP32 (hi, lo) pair, FP32 mass,
+//                              traceless quadrupole and tr(q)
 //   EpiDev[ni_tot]       32 B: FP64 position and r_search
 //   id_epj / id_spj      int32 per list entry, walks concatenated
 //   WalkDesc[n_walk]     96 B: list offsets, walk centre (FP64), box
@@ -39,6 +43,24 @@ struct __align__(32) SpjMix {
     float pad1;
 };
 static_assert(sizeof(SpjMix) == 64, "SpjMix layout");
+
+// Positions split into FP32 hi = fl(x) and lo = fl(x - hi), so hi + lo holds x
+// to about 2^-48 |x|.  Built on the device from EpjMix / SpjMix; they let the
+// warp-specialised kernels form walk-relative coordinates in FP32 arithmetic
+// (the FP64 pipe of GB300 runs at 1/64 of the FP32 rate).
+struct __align__(32) EpjF32 {
+    float xh, yh, zh, m;
+    float xl, yl, zl, rs2;
+};
+static_assert(sizeof(EpjF32) == 32, "EpjF32 layout");
+
+struct __align__(32) SpjF32 {
+    float xh, yh, zh, m;
+    float xl, yl, zl, tr;
+    float Q[6];  // traceless 3q - tr(q) I
+    float pad[2];
+};
+static_assert(sizeof(SpjF32) == 64, "SpjF32 layout");
 
 struct __align__(16) SpjQ64 {
     double m;
@@ -88,6 +110,8 @@ struct Params {
     const double* epj_rs64;
     const SpjMix* spj;
     const SpjQ64* spj_q64;
+    const EpjF32* epj32;
+    const SpjF32* spj32;
     const int32_t* id_epj;
     const int32_t* id_spj;
     const WalkDesc* walks;
@@ -125,6 +149,9 @@ __device__ __forceinline__ int exact_neighbour(double xi, double yi, double zi, 
 cudaError_t launch_fp64(const Params& p, cudaStream_t s, int num_sms);
 cudaError_t launch_mixed(const Params& p, cudaStream_t s, int num_sms);
 cudaError_t launch_retest(const Params& p, cudaStream_t s, int num_sms);
+// Builds the (hi, lo) FP32 copies of the EPJ / SPJ arrays.
+cudaError_t launch_split_j(const EpjMix* epj, int64_t n_epj, EpjF32* epj32, const SpjMix* spj, int64_t n_spj,
+                           SpjF32* spj32, cudaStream_t s);
 // Warp-specialised kernel, variants 0..kNumWsVariants-1 (see pgf_kernels_ws.cu).
 constexpr int kNumWsVariants = 8;
 cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant);

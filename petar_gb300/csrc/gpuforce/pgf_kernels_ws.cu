@@ -17,6 +17,14 @@
 //   needs (mbarrier "full") and releases it when done (mbarrier "empty").  The
 //   producer therefore runs ahead, across walk boundaries, by up to kSlots
 //   items.
+// * The producer works in FP32 only.  j positions arrive as (hi, lo) FP32
+//   pairs (EpjF32 / SpjF32); x - c is (x_hi - c_hi) + (x_lo - c_lo), and for
+//   near entries an error-free two-sum gives the walk-relative (hi, lo) pair.
+//   GB300 runs FP64 at 1/64 of the FP32 rate, so FP64 conversion in the
+//   producer would throttle it on small walks.
+// * Consumers flush their FP32 partial sums into (hi, lo) FP32 accumulators
+//   in shared memory with a two-sum (no FP64 in the pair loops either); the
+//   j-slices are combined in FP64 once per pass.
 // * Ambiguous neighbour pairs (within the guard band of r_search) are pushed
 //   one by one as Retest records with their own list index, so no thread has
 //   to coordinate its counts with another.
@@ -51,8 +59,11 @@ __device__ __forceinline__ int kband_near(double D, double rs, double eps2) {
     return k >= double(kKMax) ? kKMax : int(k) + 1;
 }
 
-__device__ __forceinline__ double as_double(unsigned lo, unsigned hi) {
-    return __hiloint2double((int)hi, (int)lo);
+// Error-free sum: s + e == a + b exactly (round-to-nearest, no reassociation).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
 }
 
 __device__ __forceinline__ unsigned long long globaltimer() {
@@ -159,7 +170,7 @@ struct Smem {
     Hdr hdr[kSlots];
     uint64_t full[kSlots];
     uint64_t empty[kSlots];
-    double acc[KI][4][CW * 32];
+    float2 acc[KI][4][CW * 32];  // (hi, lo) FP32 accumulators of the flushed partials
     int cnt[KI][CW * 32];
 };
 
@@ -193,7 +204,10 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
         }
         const int widx = p.order[w_q];
         const WalkDesc wd = p.walks[widx];
-        const double cx = wd.cx, cy = wd.cy, cz = wd.cz;
+        // Walk centre as an FP32 (hi, lo) pair.
+        const float chx = (float)wd.cx, chy = (float)wd.cy, chz = (float)wd.cz;
+        const float clx = (float)(wd.cx - (double)chx), cly = (float)(wd.cy - (double)chy),
+                    clz = (float)(wd.cz - (double)chz);
         const float rcut2 = (float)wd.rcut2;
         const float rsmax2 = wd.rs_max * wd.rs_max;
         const float hmax = fmaxf(wd.hx, fmaxf(wd.hy, wd.hz));
@@ -213,7 +227,7 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
                 const int64_t base = wd.epj_begin + (int64_t)t * kTileEP;
                 const int nt = min(kTileEP, wd.n_epj - t * kTileEP);
                 int id[4];
-                uint4 r0[4], r1[4];
+                float4 r0[4], r1[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const int e = q * 32 + lane;
@@ -222,11 +236,11 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     if (id[q] >= 0) {
-                        const uint4* src = reinterpret_cast<const uint4*>(p.epj + id[q]);
+                        const float4* src = reinterpret_cast<const float4*>(p.epj32 + id[q]);
                         r0[q] = __ldg(src);
                         r1[q] = __ldg(src + 1);
                     } else {
-                        r0[q] = r1[q] = make_uint4(0, 0, 0, 0);
+                        r0[q] = r1[q] = make_float4(0.f, 0.f, 0.f, 0.f);
                     }
                 }
                 if (!acquire(sl)) return;
@@ -239,14 +253,14 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
                     bool near = false;
                     float hx = 0.f, hy = 0.f, hz = 0.f, m = 0.f, rs2 = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
                     if (valid) {
-                        const double dx = as_double(r0[q].x, r0[q].y) - cx;
-                        const double dy = as_double(r0[q].z, r0[q].w) - cy;
-                        const double dz = as_double(r1[q].x, r1[q].y) - cz;
-                        hx = (float)dx;
-                        hy = (float)dy;
-                        hz = (float)dz;
-                        m = __uint_as_float(r1[q].z);
-                        rs2 = __uint_as_float(r1[q].w);
+                        // x - c to within about 1 ulp; exact (hi, lo) below for near entries
+                        const float sx = r0[q].x - chx, sy = r0[q].y - chy, sz = r0[q].z - chz;
+                        const float tx = r1[q].x - clx, ty = r1[q].y - cly, tz = r1[q].z - clz;
+                        hx = sx + tx;
+                        hy = sy + ty;
+                        hz = sz + tz;
+                        m = r0[q].w;
+                        rs2 = r1[q].w;
                         const float ex = fmaxf(fabsf(hx) - wd.hx, 0.f);
                         const float ey = fmaxf(fabsf(hy) - wd.hy, 0.f);
                         const float ez = fmaxf(fabsf(hz) - wd.hz, 0.f);
@@ -256,9 +270,15 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
                         const float Rm = R * 1.001f + 1e-6f * (dmax + hmax);
                         near = !(dist2 > Rm * Rm);
                         if (near) {
-                            lx = (float)(dx - (double)hx);
-                            ly = (float)(dy - (double)hy);
-                            lz = (float)(dz - (double)hz);
+                            // (x_hi - c_hi) exactly as s + e, then (s, e + x_lo - c_lo)
+                            // renormalised: hi + lo = x - c to about 2^-48 |x|.
+                            float s_, e_;
+                            two_sum(r0[q].x, -chx, s_, e_);
+                            two_sum(s_, e_ + tx, hx, lx);
+                            two_sum(r0[q].y, -chy, s_, e_);
+                            two_sum(s_, e_ + ty, hy, ly);
+                            two_sum(r0[q].z, -chz, s_, e_);
+                            two_sum(s_, e_ + tz, hz, lz);
                         }
                     }
                     const unsigned bn = __ballot_sync(0xffffffffu, valid && near);
@@ -304,7 +324,7 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
                 const int64_t base = wd.spj_begin + (int64_t)t * kTileSP;
                 const int nt = min(kTileSP, wd.n_spj - t * kTileSP);
                 int id[2];
-                uint4 r[2][4];
+                float4 r[2][4];
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {
                     const int e = q * 32 + lane;
@@ -313,7 +333,7 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {
                     if (id[q] >= 0) {
-                        const uint4* src = reinterpret_cast<const uint4*>(p.spj + id[q]);
+                        const float4* src = reinterpret_cast<const float4*>(p.spj32 + id[q]);
 #pragma unroll
                         for (int u = 0; u < 4; ++u) r[q][u] = __ldg(src + u);
                     }
@@ -324,29 +344,29 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
                 for (int q = 0; q < 2; ++q) {
                     const int e = q * 32 + lane;
                     if (e < nt) {
-                        const float hx = (float)(as_double(r[q][0].x, r[q][0].y) - cx);
-                        const float hy = (float)(as_double(r[q][0].z, r[q][0].w) - cy);
-                        const float hz = (float)(as_double(r[q][1].x, r[q][1].y) - cz);
-                        const float m = __uint_as_float(r[q][1].z);
-                        const float c = -__uint_as_float(r[q][3].z) * eps2;
+                        // SpjF32: (xh yh zh m) (xl yl zl tr) (Qxx Qyy Qzz Qxy) (Qxz Qyz pad pad)
+                        const float hx = (r[q][0].x - chx) + (r[q][1].x - clx);
+                        const float hy = (r[q][0].y - chy) + (r[q][1].y - cly);
+                        const float hz = (r[q][0].z - chz) + (r[q][1].z - clz);
+                        const float m = r[q][0].w;
+                        const float c = -r[q][1].w * eps2;
                         if constexpr (PK) {
                             float* f = reinterpret_cast<float*>(&S.sp[e >> 1][0]) + (e & 1);
                             f[0] = hx;
                             f[2] = hy;
                             f[4] = hz;
                             f[6] = m;
-                            f[8] = -__uint_as_float(r[q][2].x);
-                            f[10] = -__uint_as_float(r[q][2].y);
-                            f[12] = -__uint_as_float(r[q][2].z);
-                            f[14] = -__uint_as_float(r[q][2].w);
-                            f[16] = -__uint_as_float(r[q][3].x);
-                            f[18] = -__uint_as_float(r[q][3].y);
+                            f[8] = -r[q][2].x;
+                            f[10] = -r[q][2].y;
+                            f[12] = -r[q][2].z;
+                            f[14] = -r[q][2].w;
+                            f[16] = -r[q][3].x;
+                            f[18] = -r[q][3].y;
                             f[20] = -c;
                         } else {
                             S.sp[e][0] = make_float4(hx, hy, hz, m);
-                            S.sp[e][1] = make_float4(__uint_as_float(r[q][2].x), __uint_as_float(r[q][2].y),
-                                                     __uint_as_float(r[q][2].z), __uint_as_float(r[q][2].w));
-                            S.sp[e][2] = make_float4(__uint_as_float(r[q][3].x), __uint_as_float(r[q][3].y), c, 0.f);
+                            S.sp[e][1] = r[q][2];
+                            S.sp[e][2] = make_float4(r[q][3].x, r[q][3].y, c, 0.f);
                         }
                     }
                 }
@@ -374,18 +394,37 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
 
 // ---------------------------------------------------------------- consumer
 
+template <int N>
+struct IntC {
+    static constexpr int value = N;
+};
+
+// Issue cost per j entry of a pass of nip i-particles with ku i per thread on
+// ct_threads consumer threads: warps that issue, times the pairs each thread
+// runs per j, plus a small charge for the shared-memory load each j costs a
+// thread, divided by the j-slices the pass splits a tile into.
+__device__ __forceinline__ float pass_cost(int nip, int ku, int ct_threads) {
+    const int S = (nip + ku - 1) / ku;
+    const int n_js = ct_threads / S;
+    if (n_js == 0) return 3.0e38f;
+    const int warps = (n_js * S + 31) >> 5;
+    return (float)warps * ((float)ku + 0.15f) / (float)n_js;
+}
+
 template <int CW, int KI, bool PK>
 __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
     constexpr int CT = CW * 32;
     constexpr int kMaxPass = CT * KI;
+    constexpr int KA = KI > 1 ? KI - 1 : 1;  // the other i-per-thread count a pass may use
     const double eps2d = p.eps2;
     const float eps2 = (float)p.eps2;
     unsigned item = 0;
 
-    // Pass state.
+    // Pass state.  A pass runs ku (KA or KI) i-particles per thread, whichever
+    // leaves fewer lanes idle; the tile bodies are instantiated for both.
     WalkDesc wd{};
     float rcut2 = 0.f;
-    int nip = 0, S = 1, n_js = 1, js = 0, slot = 0;
+    int nip = 0, S = 1, n_js = 1, js = 0, slot = 0, ku = KI;
     bool active = false;
     float xih[KI], yih[KI], zih[KI], xil[KI], yil[KI], zil[KI], rsi2[KI];
     int kb[KI], gi[KI], cnt[KI];
@@ -410,6 +449,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
     auto flush = [&]() {
 #pragma unroll
         for (int k = 0; k < KI; ++k) {
+            if (k >= ku) continue;
             if constexpr (PK) {
                 a[k][0] += b[k][0].x + b[k][0].y;
                 a[k][1] += b[k][1].x + b[k][1].y;
@@ -420,7 +460,11 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
             }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                s.acc[k][q][ct] += (double)a[k][q];
+                float2 v = s.acc[k][q][ct];
+                float e;
+                two_sum(v.x, a[k][q], v.x, e);
+                v.y += e;
+                s.acc[k][q][ct] = v;
                 a[k][q] = 0.f;
             }
         }
@@ -442,6 +486,191 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
         return exact_neighbour(ei.x, ei.y, ei.z, ei.rs, e.x, e.y, e.z, p.epj_rs64[id], p.eps2);
     };
 
+    // One EPJ tile with KU i-particles per thread.
+    auto ep_tile = [&](auto ku_c, const Hdr& h, int sl) {
+        constexpr int KU = decltype(ku_c)::value;
+        const auto& T = s.slot[sl].ep;
+        int c[KU];
+#pragma unroll
+        for (int k = 0; k < KU; ++k) c[k] = 0;
+        const int pn = (h.nn + n_js - 1) / n_js;
+        const int j0 = min(h.nn, js * pn);
+        const int j1 = min(h.nn, j0 + pn);
+#pragma unroll 2
+        for (int j = j0; j < j1; ++j) {
+            const float4 hh = T.nh[j];
+            const float4 ll = T.nl[j];
+#pragma unroll
+            for (int k = 0; k < KU; ++k) {
+                const float dx = (hh.x - xih[k]) + (ll.x - xil[k]);
+                const float dy = (hh.y - yih[k]) + (ll.y - yil[k]);
+                const float dz = (hh.z - zih[k]) + (ll.z - zil[k]);
+                float r2 = fmaf(dx, dx, eps2);
+                r2 = fmaf(dy, dy, r2);
+                r2 = fmaf(dz, dz, r2);
+                const float rs2 = fmaxf(rsi2[k], ll.w);
+                const int e = __float_as_int(r2) - __float_as_int(rs2) + kb[k];
+                c[k] += (int)((unsigned)e >> 31);
+                if ((unsigned)e < (unsigned)(2 * kb[k]) && valid[k]) c[k] += push_retest(k, h.base + T.nidx[j]);
+                const float ri = rsqrt_approx(fmaxf(r2, rcut2));
+                const float mri = hh.w * ri;
+                const float mri3 = mri * (ri * ri);
+                a[k][0] = fmaf(mri3, dx, a[k][0]);
+                a[k][1] = fmaf(mri3, dy, a[k][1]);
+                a[k][2] = fmaf(mri3, dz, a[k][2]);
+                a[k][3] -= mri;
+            }
+        }
+        int nfar;
+        if constexpr (PK) {
+            // far pairs of j, two per FP32x2 instruction
+            const int np = (h.nf + 1) >> 1;
+            const int pp = (np + n_js - 1) / n_js;
+            const int f0 = min(np, js * pp);
+            const int f1 = min(np, f0 + pp);
+            const float2 e2 = make_float2(eps2, eps2);
+#pragma unroll 2
+            for (int j = f0; j < f1; ++j) {
+                const float4 u = T.fp[j][0];
+                const float4 v = T.fp[j][1];
+                const float2 X = make_float2(u.x, u.y), Y = make_float2(u.z, u.w);
+                const float2 Z = make_float2(v.x, v.y), M = make_float2(v.z, v.w);
+#pragma unroll
+                for (int k = 0; k < KU; ++k) {
+                    const float2 dx = __fadd2_rn(X, nx2[k]);
+                    const float2 dy = __fadd2_rn(Y, ny2[k]);
+                    const float2 dz = __fadd2_rn(Z, nz2[k]);
+                    float2 r2 = __ffma2_rn(dx, dx, e2);
+                    r2 = __ffma2_rn(dy, dy, r2);
+                    r2 = __ffma2_rn(dz, dz, r2);
+                    const float2 ri = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+                    const float2 mri = __fmul2_rn(M, ri);
+                    const float2 mri3 = __fmul2_rn(mri, __fmul2_rn(ri, ri));
+                    b[k][0] = __ffma2_rn(mri3, dx, b[k][0]);
+                    b[k][1] = __ffma2_rn(mri3, dy, b[k][1]);
+                    b[k][2] = __ffma2_rn(mri3, dz, b[k][2]);
+                    b[k][3] = __fadd2_rn(b[k][3], mri);
+                }
+            }
+            nfar = 2 * (f1 - f0);
+        } else {
+            const int pf = (h.nf + n_js - 1) / n_js;
+            const int f0 = min(h.nf, js * pf);
+            const int f1 = min(h.nf, f0 + pf);
+#pragma unroll 4
+            for (int j = f0; j < f1; ++j) {
+                const float4 hh = T.fr[j];
+#pragma unroll
+                for (int k = 0; k < KU; ++k) {
+                    const float dx = hh.x - xih[k];
+                    const float dy = hh.y - yih[k];
+                    const float dz = hh.z - zih[k];
+                    float r2 = fmaf(dx, dx, eps2);
+                    r2 = fmaf(dy, dy, r2);
+                    r2 = fmaf(dz, dz, r2);
+                    const float ri = rsqrt_approx(r2);
+                    const float mri = hh.w * ri;
+                    const float mri3 = mri * (ri * ri);
+                    a[k][0] = fmaf(mri3, dx, a[k][0]);
+                    a[k][1] = fmaf(mri3, dy, a[k][1]);
+                    a[k][2] = fmaf(mri3, dz, a[k][2]);
+                    a[k][3] -= mri;
+                }
+            }
+            nfar = f1 - f0;
+        }
+#pragma unroll
+        for (int k = 0; k < KU; ++k) cnt[k] += c[k];
+        since += (j1 - j0) + nfar;
+    };
+
+    // One SPJ tile with KU i-particles per thread.
+    auto sp_tile = [&](auto ku_c, const Hdr& h, int sl) {
+        constexpr int KU = decltype(ku_c)::value;
+        const auto& T = s.slot[sl].sp;
+        if constexpr (PK) {
+            const int np = (h.nn + 1) >> 1;
+            const int pp = (np + n_js - 1) / n_js;
+            const int j0 = min(np, js * pp);
+            const int j1 = min(np, j0 + pp);
+            const float2 e2 = make_float2(eps2, eps2);
+#pragma unroll 1
+            for (int j = j0; j < j1; ++j) {
+                const float4 w0 = T.sp[j][0], w1 = T.sp[j][1], w2 = T.sp[j][2];
+                const float4 w3 = T.sp[j][3], w4 = T.sp[j][4], w5 = T.sp[j][5];
+                const float2 X = make_float2(w0.x, w0.y), Y = make_float2(w0.z, w0.w);
+                const float2 Z = make_float2(w1.x, w1.y), M = make_float2(w1.z, w1.w);
+                // nQ = -Q and nC = -c, so that the terms below need no negation:
+                // with u = d.(-Q).d - c = -(d.Q.d + c) and t = u / r^5,
+                // acc += (m/r^3 - 2.5 t/r^2) d + (-Q).d / r^5 and
+                // -pot += m/r - 0.5 t.
+                const float2 Qxx = make_float2(w2.x, w2.y), Qyy = make_float2(w2.z, w2.w);
+                const float2 Qzz = make_float2(w3.x, w3.y), Qxy = make_float2(w3.z, w3.w);
+                const float2 Qxz = make_float2(w4.x, w4.y), Qyz = make_float2(w4.z, w4.w);
+                const float2 C = make_float2(w5.x, w5.y);
+                const float2 km25 = make_float2(-2.5f, -2.5f), km05 = make_float2(-0.5f, -0.5f);
+#pragma unroll
+                for (int k = 0; k < KU; ++k) {
+                    const float2 dx = __fadd2_rn(X, nx2[k]);
+                    const float2 dy = __fadd2_rn(Y, ny2[k]);
+                    const float2 dz = __fadd2_rn(Z, nz2[k]);
+                    float2 r2 = __ffma2_rn(dx, dx, e2);
+                    r2 = __ffma2_rn(dy, dy, r2);
+                    r2 = __ffma2_rn(dz, dz, r2);
+                    const float2 ri = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+                    const float2 qdx = __ffma2_rn(Qxx, dx, __ffma2_rn(Qxy, dy, __fmul2_rn(Qxz, dz)));
+                    const float2 qdy = __ffma2_rn(Qxy, dx, __ffma2_rn(Qyy, dy, __fmul2_rn(Qyz, dz)));
+                    const float2 qdz = __ffma2_rn(Qxz, dx, __ffma2_rn(Qyz, dy, __fmul2_rn(Qzz, dz)));
+                    const float2 sq = __ffma2_rn(qdx, dx, __ffma2_rn(qdy, dy, __ffma2_rn(qdz, dz, C)));
+                    const float2 ri2 = __fmul2_rn(ri, ri);
+                    const float2 ri3 = __fmul2_rn(ri2, ri);
+                    const float2 ri5 = __fmul2_rn(ri3, ri2);
+                    const float2 tq = __fmul2_rn(sq, ri5);
+                    const float2 A = __ffma2_rn(__fmul2_rn(tq, ri2), km25, __fmul2_rn(M, ri3));
+                    b[k][0] = __ffma2_rn(A, dx, __ffma2_rn(ri5, qdx, b[k][0]));
+                    b[k][1] = __ffma2_rn(A, dy, __ffma2_rn(ri5, qdy, b[k][1]));
+                    b[k][2] = __ffma2_rn(A, dz, __ffma2_rn(ri5, qdz, b[k][2]));
+                    b[k][3] = __ffma2_rn(tq, km05, __ffma2_rn(M, ri, b[k][3]));
+                }
+            }
+            since += 2 * (j1 - j0);
+        } else {
+            const int ps = (h.nn + n_js - 1) / n_js;
+            const int j0 = min(h.nn, js * ps);
+            const int j1 = min(h.nn, j0 + ps);
+#pragma unroll 2
+            for (int j = j0; j < j1; ++j) {
+                const float4 q0 = T.sp[j][0];
+                const float4 qa = T.sp[j][1];
+                const float4 qb = T.sp[j][2];
+#pragma unroll
+                for (int k = 0; k < KU; ++k) {
+                    const float dx = q0.x - xih[k];
+                    const float dy = q0.y - yih[k];
+                    const float dz = q0.z - zih[k];
+                    float r2 = fmaf(dx, dx, eps2);
+                    r2 = fmaf(dy, dy, r2);
+                    r2 = fmaf(dz, dz, r2);
+                    const float ri = rsqrt_approx(r2);
+                    const float qdx = fmaf(qa.x, dx, fmaf(qa.w, dy, qb.x * dz));
+                    const float qdy = fmaf(qa.w, dx, fmaf(qa.y, dy, qb.y * dz));
+                    const float qdz = fmaf(qb.x, dx, fmaf(qb.y, dy, qa.z * dz));
+                    const float sq = fmaf(qdx, dx, fmaf(qdy, dy, fmaf(qdz, dz, qb.z)));
+                    const float ri2 = ri * ri;
+                    const float ri3 = ri2 * ri;
+                    const float ri5 = ri3 * ri2;
+                    const float tq = sq * ri5;
+                    const float A = fmaf(tq * ri2, 2.5f, q0.w * ri3);
+                    a[k][0] = fmaf(A, dx, fmaf(-ri5, qdx, a[k][0]));
+                    a[k][1] = fmaf(A, dy, fmaf(-ri5, qdy, a[k][1]));
+                    a[k][2] = fmaf(A, dz, fmaf(-ri5, qdz, a[k][2]));
+                    a[k][3] = fmaf(-0.5f, tq, fmaf(-q0.w, ri, a[k][3]));
+                }
+            }
+            since += j1 - j0;
+        }
+    };
+
     for (;;) {
         const int sl = item % kSlots;
         if (!mbar_wait(&s.full[sl], (item / kSlots) & 1u, p.err)) return;
@@ -451,7 +680,11 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
             wd = p.walks[h.walk];
             rcut2 = (float)wd.rcut2;
             nip = min(kMaxPass, wd.n_i - h.ipass);
-            S = (nip + KI - 1) / KI;
+            ku = KI;
+            if constexpr (KA < KI) {
+                if (pass_cost(nip, KA, CT) < pass_cost(nip, KI, CT)) ku = KA;
+            }
+            S = (nip + ku - 1) / ku;
             n_js = CT / S;
             js = ct / S;
             slot = ct - js * S;
@@ -459,7 +692,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
 #pragma unroll
             for (int k = 0; k < KI; ++k) {
                 const int li = slot + k * S;
-                valid[k] = active && li < nip;
+                valid[k] = active && k < ku && li < nip;
                 gi[k] = wd.i_begin + h.ipass + li;
                 xih[k] = yih[k] = zih[k] = xil[k] = yil[k] = zil[k] = 0.f;
                 rsi2[k] = 0.f;
@@ -485,193 +718,25 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     a[k][q] = 0.f;
-                    s.acc[k][q][ct] = 0.0;
+                    s.acc[k][q][ct] = make_float2(0.f, 0.f);
                 }
             }
             since = 0;
         } else if (h.kind == kItemEP) {
             if (active) {
-                const auto& T = s.slot[sl].ep;
-                int c[KI];
-#pragma unroll
-                for (int k = 0; k < KI; ++k) c[k] = 0;
-                const int pn = (h.nn + n_js - 1) / n_js;
-                const int j0 = min(h.nn, js * pn);
-                const int j1 = min(h.nn, j0 + pn);
-#pragma unroll 2
-                for (int j = j0; j < j1; ++j) {
-                    const float4 hh = T.nh[j];
-                    const float4 ll = T.nl[j];
-#pragma unroll
-                    for (int k = 0; k < KI; ++k) {
-                        const float dx = (hh.x - xih[k]) + (ll.x - xil[k]);
-                        const float dy = (hh.y - yih[k]) + (ll.y - yil[k]);
-                        const float dz = (hh.z - zih[k]) + (ll.z - zil[k]);
-                        float r2 = fmaf(dx, dx, eps2);
-                        r2 = fmaf(dy, dy, r2);
-                        r2 = fmaf(dz, dz, r2);
-                        const float rs2 = fmaxf(rsi2[k], ll.w);
-                        const int e = __float_as_int(r2) - __float_as_int(rs2) + kb[k];
-                        c[k] += (int)((unsigned)e >> 31);
-                        if ((unsigned)e < (unsigned)(2 * kb[k]) && valid[k]) c[k] += push_retest(k, h.base + T.nidx[j]);
-                        const float ri = rsqrt_approx(fmaxf(r2, rcut2));
-                        const float mri = hh.w * ri;
-                        const float mri3 = mri * (ri * ri);
-                        a[k][0] = fmaf(mri3, dx, a[k][0]);
-                        a[k][1] = fmaf(mri3, dy, a[k][1]);
-                        a[k][2] = fmaf(mri3, dz, a[k][2]);
-                        a[k][3] -= mri;
-                    }
-                }
-                int nfar;
-                if constexpr (PK) {
-                    // far pairs of j, two per FP32x2 instruction
-                    const int np = (h.nf + 1) >> 1;
-                    const int pp = (np + n_js - 1) / n_js;
-                    const int f0 = min(np, js * pp);
-                    const int f1 = min(np, f0 + pp);
-                    const float2 e2 = make_float2(eps2, eps2);
-#pragma unroll 2
-                    for (int j = f0; j < f1; ++j) {
-                        const float4 u = T.fp[j][0];
-                        const float4 v = T.fp[j][1];
-                        const float2 X = make_float2(u.x, u.y), Y = make_float2(u.z, u.w);
-                        const float2 Z = make_float2(v.x, v.y), M = make_float2(v.z, v.w);
-#pragma unroll
-                        for (int k = 0; k < KI; ++k) {
-                            const float2 dx = __fadd2_rn(X, nx2[k]);
-                            const float2 dy = __fadd2_rn(Y, ny2[k]);
-                            const float2 dz = __fadd2_rn(Z, nz2[k]);
-                            float2 r2 = __ffma2_rn(dx, dx, e2);
-                            r2 = __ffma2_rn(dy, dy, r2);
-                            r2 = __ffma2_rn(dz, dz, r2);
-                            const float2 ri = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
-                            const float2 mri = __fmul2_rn(M, ri);
-                            const float2 mri3 = __fmul2_rn(mri, __fmul2_rn(ri, ri));
-                            b[k][0] = __ffma2_rn(mri3, dx, b[k][0]);
-                            b[k][1] = __ffma2_rn(mri3, dy, b[k][1]);
-                            b[k][2] = __ffma2_rn(mri3, dz, b[k][2]);
-                            b[k][3] = __fadd2_rn(b[k][3], mri);
-                        }
-                    }
-                    nfar = 2 * (f1 - f0);
-                } else {
-                    const int pf = (h.nf + n_js - 1) / n_js;
-                    const int f0 = min(h.nf, js * pf);
-                    const int f1 = min(h.nf, f0 + pf);
-#pragma unroll 4
-                    for (int j = f0; j < f1; ++j) {
-                        const float4 hh = T.fr[j];
-#pragma unroll
-                        for (int k = 0; k < KI; ++k) {
-                            const float dx = hh.x - xih[k];
-                            const float dy = hh.y - yih[k];
-                            const float dz = hh.z - zih[k];
-                            float r2 = fmaf(dx, dx, eps2);
-                            r2 = fmaf(dy, dy, r2);
-                            r2 = fmaf(dz, dz, r2);
-                            const float ri = rsqrt_approx(r2);
-                            const float mri = hh.w * ri;
-                            const float mri3 = mri * (ri * ri);
-                            a[k][0] = fmaf(mri3, dx, a[k][0]);
-                            a[k][1] = fmaf(mri3, dy, a[k][1]);
-                            a[k][2] = fmaf(mri3, dz, a[k][2]);
-                            a[k][3] -= mri;
-                        }
-                    }
-                    nfar = f1 - f0;
-                }
-#pragma unroll
-                for (int k = 0; k < KI; ++k) cnt[k] += c[k];
-                since += (j1 - j0) + nfar;
+                if (ku == KI)
+                    ep_tile(IntC<KI>{}, h, sl);
+                else if constexpr (KA < KI)
+                    ep_tile(IntC<KA>{}, h, sl);
                 if (since >= kFlush) flush();
             }
         } else if (h.kind == kItemSP) {
             if (active) {
-              if constexpr (PK) {
-                const auto& T = s.slot[sl].sp;
-                const int np = (h.nn + 1) >> 1;
-                const int pp = (np + n_js - 1) / n_js;
-                const int j0 = min(np, js * pp);
-                const int j1 = min(np, j0 + pp);
-                const float2 e2 = make_float2(eps2, eps2);
-#pragma unroll 1
-                for (int j = j0; j < j1; ++j) {
-                    const float4 w0 = T.sp[j][0], w1 = T.sp[j][1], w2 = T.sp[j][2];
-                    const float4 w3 = T.sp[j][3], w4 = T.sp[j][4], w5 = T.sp[j][5];
-                    const float2 X = make_float2(w0.x, w0.y), Y = make_float2(w0.z, w0.w);
-                    const float2 Z = make_float2(w1.x, w1.y), M = make_float2(w1.z, w1.w);
-                    // nQ = -Q and nC = -c, so that the terms below need no negation:
-                    // with u = d.(-Q).d - c = -(d.Q.d + c) and t = u / r^5,
-                    // acc += (m/r^3 - 2.5 t/r^2) d + (-Q).d / r^5 and
-                    // -pot += m/r - 0.5 t.
-                    const float2 Qxx = make_float2(w2.x, w2.y), Qyy = make_float2(w2.z, w2.w);
-                    const float2 Qzz = make_float2(w3.x, w3.y), Qxy = make_float2(w3.z, w3.w);
-                    const float2 Qxz = make_float2(w4.x, w4.y), Qyz = make_float2(w4.z, w4.w);
-                    const float2 C = make_float2(w5.x, w5.y);
-                    const float2 km25 = make_float2(-2.5f, -2.5f), km05 = make_float2(-0.5f, -0.5f);
-#pragma unroll
-                    for (int k = 0; k < KI; ++k) {
-                        const float2 dx = __fadd2_rn(X, nx2[k]);
-                        const float2 dy = __fadd2_rn(Y, ny2[k]);
-                        const float2 dz = __fadd2_rn(Z, nz2[k]);
-                        float2 r2 = __ffma2_rn(dx, dx, e2);
-                        r2 = __ffma2_rn(dy, dy, r2);
-                        r2 = __ffma2_rn(dz, dz, r2);
-                        const float2 ri = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
-                        const float2 qdx = __ffma2_rn(Qxx, dx, __ffma2_rn(Qxy, dy, __fmul2_rn(Qxz, dz)));
-                        const float2 qdy = __ffma2_rn(Qxy, dx, __ffma2_rn(Qyy, dy, __fmul2_rn(Qyz, dz)));
-                        const float2 qdz = __ffma2_rn(Qxz, dx, __ffma2_rn(Qyz, dy, __fmul2_rn(Qzz, dz)));
-                        const float2 sq = __ffma2_rn(qdx, dx, __ffma2_rn(qdy, dy, __ffma2_rn(qdz, dz, C)));
-                        const float2 ri2 = __fmul2_rn(ri, ri);
-                        const float2 ri3 = __fmul2_rn(ri2, ri);
-                        const float2 ri5 = __fmul2_rn(ri3, ri2);
-                        const float2 tq = __fmul2_rn(sq, ri5);
-                        const float2 A = __ffma2_rn(__fmul2_rn(tq, ri2), km25, __fmul2_rn(M, ri3));
-                        b[k][0] = __ffma2_rn(A, dx, __ffma2_rn(ri5, qdx, b[k][0]));
-                        b[k][1] = __ffma2_rn(A, dy, __ffma2_rn(ri5, qdy, b[k][1]));
-                        b[k][2] = __ffma2_rn(A, dz, __ffma2_rn(ri5, qdz, b[k][2]));
-                        b[k][3] = __ffma2_rn(tq, km05, __ffma2_rn(M, ri, b[k][3]));
-                    }
-                }
-                since += 2 * (j1 - j0);
-              } else {
-                const auto& T = s.slot[sl].sp;
-                const int ps = (h.nn + n_js - 1) / n_js;
-                const int j0 = min(h.nn, js * ps);
-                const int j1 = min(h.nn, j0 + ps);
-#pragma unroll 2
-                for (int j = j0; j < j1; ++j) {
-                    const float4 q0 = T.sp[j][0];
-                    const float4 qa = T.sp[j][1];
-                    const float4 qb = T.sp[j][2];
-#pragma unroll
-                    for (int k = 0; k < KI; ++k) {
-                        const float dx = q0.x - xih[k];
-                        const float dy = q0.y - yih[k];
-                        const float dz = q0.z - zih[k];
-                        float r2 = fmaf(dx, dx, eps2);
-                        r2 = fmaf(dy, dy, r2);
-                        r2 = fmaf(dz, dz, r2);
-                        const float ri = rsqrt_approx(r2);
-                        const float qdx = fmaf(qa.x, dx, fmaf(qa.w, dy, qb.x * dz));
-                        const float qdy = fmaf(qa.w, dx, fmaf(qa.y, dy, qb.y * dz));
-                        const float qdz = fmaf(qb.x, dx, fmaf(qb.y, dy, qa.z * dz));
-                        const float sq = fmaf(qdx, dx, fmaf(qdy, dy, fmaf(qdz, dz, qb.z)));
-                        const float ri2 = ri * ri;
-                        const float ri3 = ri2 * ri;
-                        const float ri5 = ri3 * ri2;
-                        const float tq = sq * ri5;
-                        const float A = fmaf(tq * ri2, 2.5f, q0.w * ri3);
-                        a[k][0] = fmaf(A, dx, fmaf(-ri5, qdx, a[k][0]));
-                        a[k][1] = fmaf(A, dy, fmaf(-ri5, qdy, a[k][1]));
-                        a[k][2] = fmaf(A, dz, fmaf(-ri5, qdz, a[k][2]));
-                        a[k][3] = fmaf(-0.5f, tq, fmaf(-q0.w, ri, a[k][3]));
-                    }
-                }
-                since += j1 - j0;
-              }
-              if (since >= kFlush) flush();
+                if (ku == KI)
+                    sp_tile(IntC<KI>{}, h, sl);
+                else if constexpr (KA < KI)
+                    sp_tile(IntC<KA>{}, h, sl);
+                if (since >= kFlush) flush();
             }
         } else {  // kItemEnd: reduce the j-slices of the pass and write
             if (active) {
@@ -690,7 +755,10 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
                     for (int q = 0; q < n_js; ++q) {
                         const int src = q * S + slot;
 #pragma unroll
-                        for (int c = 0; c < 4; ++c) r[c] += s.acc[k][c][src];
+                        for (int c = 0; c < 4; ++c) {
+                            const float2 v = s.acc[k][c][src];
+                            r[c] += (double)v.x + (double)v.y;
+                        }
                         n += s.cnt[k][src];
                     }
                     p.out_accp[gi[k]] = Accp{G * r[0], G * r[1], G * r[2], G * r[3]};
@@ -744,7 +812,52 @@ cudaError_t launch_ws_t(const Params& p, cudaStream_t st, int num_sms) {
     return cudaGetLastError();
 }
 
+__global__ __launch_bounds__(256) void split_j_kernel(const EpjMix* __restrict__ epj, int64_t n_epj,
+                                                      EpjF32* __restrict__ epj32, const SpjMix* __restrict__ spj,
+                                                      int64_t n_spj, SpjF32* __restrict__ spj32) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_epj; i += stride) {
+        const EpjMix e = epj[i];
+        EpjF32 o;
+        o.xh = (float)e.x;
+        o.yh = (float)e.y;
+        o.zh = (float)e.z;
+        o.xl = (float)(e.x - (double)o.xh);
+        o.yl = (float)(e.y - (double)o.yh);
+        o.zl = (float)(e.z - (double)o.zh);
+        o.m = e.m;
+        o.rs2 = e.rs2;
+        epj32[i] = o;
+    }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_spj; i += stride) {
+        const SpjMix e = spj[i];
+        SpjF32 o;
+        o.xh = (float)e.x;
+        o.yh = (float)e.y;
+        o.zh = (float)e.z;
+        o.xl = (float)(e.x - (double)o.xh);
+        o.yl = (float)(e.y - (double)o.yh);
+        o.zl = (float)(e.z - (double)o.zh);
+        o.m = e.m;
+        o.tr = e.tr;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) o.Q[c] = e.Q[c];
+        o.pad[0] = o.pad[1] = 0.f;
+        spj32[i] = o;
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_split_j(const EpjMix* epj, int64_t n_epj, EpjF32* epj32, const SpjMix* spj, int64_t n_spj,
+                           SpjF32* spj32, cudaStream_t s) {
+    const int64_t n = n_epj > n_spj ? n_epj : n_spj;
+    if (n <= 0) return cudaSuccess;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    split_j_kernel<<<(int)blocks, 256, 0, s>>>(epj, n_epj, epj32, spj, n_spj, spj32);
+    return cudaGetLastError();
+}
 
 // Variants of the warp-specialised kernel: consumer warps, i per consumer
 // thread, minimum CTAs per SM.
@@ -752,10 +865,10 @@ cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant)
     switch (variant) {
         case 0: return launch_ws_t<4, 3, 4, false>(p, s, num_sms);
         case 1: return launch_ws_t<4, 2, 4, false>(p, s, num_sms);
-        case 2: return launch_ws_t<4, 2, 5, false>(p, s, num_sms);
+        case 2: return launch_ws_t<8, 3, 2, false>(p, s, num_sms);
         case 3: return launch_ws_t<8, 2, 3, false>(p, s, num_sms);
         case 4: return launch_ws_t<4, 2, 4, true>(p, s, num_sms);
-        case 5: return launch_ws_t<4, 2, 5, true>(p, s, num_sms);
+        case 5: return launch_ws_t<8, 3, 2, true>(p, s, num_sms);
         case 6: return launch_ws_t<4, 1, 5, true>(p, s, num_sms);
         case 7: return launch_ws_t<8, 2, 3, true>(p, s, num_sms);
         default: return cudaErrorInvalidValue;
