@@ -47,6 +47,7 @@ sys.path.insert(0, str(ROOT))
 
 WORKLOADS = {
     "plummer1m_bin50": dict(seed=3, n_cm=1048576, r_out=0.003, binary_fraction=0.5, theta=0.3),
+    "plummer256k_bin50": dict(seed=4, n_cm=262144, r_out=0.0048, binary_fraction=0.5, theta=0.3),
     "plummer65k": dict(seed=2, n_cm=65536, r_out=0.008, binary_fraction=0.0, theta=0.3),
     "plummer2k": dict(seed=1, n_cm=2048, r_out=0.02, binary_fraction=0.0, theta=0.3),
 }
@@ -363,14 +364,19 @@ def run_ours(args):
     # The library's autotuner picks the kernel variant on this workload; each
     # variant's time is also recorded for the report.
     variant_ms = {}
-    for v in range(9):
-        gpuforce.set_kernel_variant(v)
-        gpuforce.recompute(0)
-        gpuforce.wait(0)
-        gpuforce.recompute(0)
-        gpuforce.wait(0)
-        variant_ms[v] = 1e3 * gpuforce.get_profile()["last_calc_main"]
-    best_variant, _ = gpuforce.autotune(0, repeats=2)
+    if args.variant >= 0:
+        # fixed variant (profiling runs): no sweep, no autotuner
+        gpuforce.set_kernel_variant(args.variant)
+        best_variant = args.variant
+    else:
+        for v in range(gpuforce.NUM_KERNEL_VARIANTS):
+            gpuforce.set_kernel_variant(v)
+            gpuforce.recompute(0)
+            gpuforce.wait(0)
+            gpuforce.recompute(0)
+            gpuforce.wait(0)
+            variant_ms[v] = 1e3 * gpuforce.get_profile()["last_calc_main"]
+        best_variant, _ = gpuforce.autotune(0, repeats=2)
     gpuforce.recompute(0)
     f_mixed = gpuforce.retrieve(rec, tag=0).copy()
     for _ in range(args.warmup):
@@ -504,6 +510,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="use this kernel variant instead of the autotuner's choice")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         log("note: fewer than 3 warm-up steps")

@@ -865,10 +865,10 @@ cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant)
     switch (variant) {
         case 0: return launch_ws_t<4, 3, 4, false>(p, s, num_sms);
         case 1: return launch_ws_t<4, 2, 4, false>(p, s, num_sms);
-        case 2: return launch_ws_t<8, 3, 2, false>(p, s, num_sms);
+        case 2: return launch_ws_t<4, 4, 4, false>(p, s, num_sms);
         case 3: return launch_ws_t<8, 2, 3, false>(p, s, num_sms);
         case 4: return launch_ws_t<4, 2, 4, true>(p, s, num_sms);
-        case 5: return launch_ws_t<8, 3, 2, true>(p, s, num_sms);
+        case 5: return launch_ws_t<4, 3, 4, true>(p, s, num_sms);
         case 6: return launch_ws_t<4, 1, 5, true>(p, s, num_sms);
         case 7: return launch_ws_t<8, 2, 3, true>(p, s, num_sms);
         default: return cudaErrorInvalidValue;

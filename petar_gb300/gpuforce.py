@@ -26,6 +26,7 @@ import numpy as np
 PGF_OK = 0
 PGF_PRECISION_MIXED = 0
 PGF_PRECISION_FP64 = 1
+NUM_KERNEL_VARIANTS = 9  # PGF_NUM_KERNEL_VARIANTS
 
 # PeTar's EPISoft (src/soft_ptcl.hpp:271-308): id, pos, r_search, rank_org, type.
 EPI_DTYPE = np.dtype([("id", "<i8"), ("pos", "<f8", 3), ("r_search", "<f8"), ("rank_org", "<i4"),

@@ -67,3 +67,10 @@ def test_record_layouts_match_petar():
     assert (jl.off_mass, jl.off_pos, jl.off_r_search) == (8, 16, 80)
     assert (sl.off_mass, sl.off_pos, sl.off_quad, sl.has_quad) == (0, 8, 32, 1)
     assert (fl.size, fl.off_acc, fl.off_pot, fl.off_n_ngb, fl.n_ngb_bytes) == (40, 0, 24, 32, 8)
+
+
+def test_variant_count_matches_header():
+    import re
+    text = (ROOT / "include" / "petar_gpuforce.h").read_text()
+    n = int(re.search(r"#define PGF_NUM_KERNEL_VARIANTS (\d+)", text).group(1))
+    assert n == gpuforce.NUM_KERNEL_VARIANTS

@@ -217,7 +217,7 @@ def test_recompute_reproduces():
     np.testing.assert_array_equal(a["acc"], b["acc"])
 
 
-@pytest.mark.parametrize("variant", list(range(1, 9)))
+@pytest.mark.parametrize("variant", list(range(1, gpuforce.NUM_KERNEL_VARIANTS)))
 @pytest.mark.parametrize("case", ["kernel_test_rsvar", "plummer2048_walks", "ragged", "binaries"])
 def test_kernel_variants(case, variant):
     """Every mixed-precision kernel variant the autotuner may pick meets the
@@ -244,7 +244,7 @@ def test_autotune_picks_a_variant_and_keeps_results():
     gpuforce.dispatch(rec, tag=0)
     gpuforce.retrieve(rec, tag=0)
     best, ms = gpuforce.autotune(0, repeats=2)
-    assert 0 <= best < 9 and ms > 0
+    assert 0 <= best < gpuforce.NUM_KERNEL_VARIANTS and ms > 0
     assert gpuforce.get_kernel_variant() == best
     gpuforce.recompute(0)
     f = gpuforce.retrieve(rec, tag=0)
