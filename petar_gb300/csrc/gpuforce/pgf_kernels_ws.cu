@@ -171,7 +171,9 @@ struct Smem {
     uint64_t full[kSlots];
     uint64_t empty[kSlots];
     float2 acc[KI][4][CW * 32];  // (hi, lo) FP32 accumulators of the flushed partials
-    int cnt[KI][CW * 32];
+    int cnt[KI][CW * 32];        // neighbour counts
+    float4 nlo[KI][CW * 32];     // near-pair data of each i: lo x, y, z and r_search^2
+    int nkb[KI][CW * 32];        // guard band of each i (ulps)
 };
 
 // ---------------------------------------------------------------- producer
@@ -411,6 +413,10 @@ __device__ __forceinline__ float pass_cost(int nip, int ku, int ct_threads) {
     return (float)warps * ((float)ku + 0.15f) / (float)n_js;
 }
 
+// Consumer registers hold only what the far and SP loops need: the i hi
+// coordinates and the pair accumulators.  The near-only data of each i (lo
+// coordinates, r_search^2, guard band) and the neighbour counts live in
+// shared memory and are read once per tile that has near entries.
 template <int CW, int KI, bool PK>
 __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
     constexpr int CT = CW * 32;
@@ -422,65 +428,93 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
 
     // Pass state.  A pass runs ku (KA or KI) i-particles per thread, whichever
     // leaves fewer lanes idle; the tile bodies are instantiated for both.
-    WalkDesc wd{};
     float rcut2 = 0.f;
-    int nip = 0, S = 1, n_js = 1, js = 0, slot = 0, ku = KI;
+    int nip = 0, S = 1, n_js = 1, js = 0, slot = 0, ku = KI, gbase = 0;
     bool active = false;
-    float xih[KI], yih[KI], zih[KI], xil[KI], yil[KI], zil[KI], rsi2[KI];
-    int kb[KI], gi[KI], cnt[KI];
-    bool valid[KI];
-    float a[KI][4];
-    // Packed path: (-x_i, -x_i) operands and pair accumulators: b[0..2] the
-    // acceleration, b[3] minus the potential.
-    float2 nx2[KI], ny2[KI], nz2[KI];
-    float2 b[KI][4];
+    // Scalar path: i coordinates and accumulators a[0..2] acceleration, a[3]
+    // potential.  Packed path: (-x_i, -x_i) operands and pair accumulators
+    // b[0..2] acceleration, b[3] minus the potential.
+    float xih[PK ? 1 : KI], yih[PK ? 1 : KI], zih[PK ? 1 : KI];
+    float a[PK ? 1 : KI][4];
+    float2 nx2[PK ? KI : 1], ny2[PK ? KI : 1], nz2[PK ? KI : 1];
+    float2 b[PK ? KI : 1][4];
     int since = 0;
+    auto xi = [&](int k) -> float {
+        if constexpr (PK) return -nx2[k].x; else return xih[k];
+    };
+    auto yi = [&](int k) -> float {
+        if constexpr (PK) return -ny2[k].x; else return yih[k];
+    };
+    auto zi = [&](int k) -> float {
+        if constexpr (PK) return -nz2[k].x; else return zih[k];
+    };
+    // Scalar accumulation used by the near loop in both paths.
+    auto acc4 = [&](int k, float mri3, float dx, float dy, float dz, float mri) {
+        if constexpr (PK) {
+            b[k][0].x = fmaf(mri3, dx, b[k][0].x);
+            b[k][1].x = fmaf(mri3, dy, b[k][1].x);
+            b[k][2].x = fmaf(mri3, dz, b[k][2].x);
+            b[k][3].x += mri;
+        } else {
+            a[k][0] = fmaf(mri3, dx, a[k][0]);
+            a[k][1] = fmaf(mri3, dy, a[k][1]);
+            a[k][2] = fmaf(mri3, dz, a[k][2]);
+            a[k][3] -= mri;
+        }
+    };
+    auto clear_acc = [&]() {
 #pragma unroll
-    for (int k = 0; k < KI; ++k) {
-        xih[k] = yih[k] = zih[k] = xil[k] = yil[k] = zil[k] = rsi2[k] = 0.f;
-        kb[k] = gi[k] = cnt[k] = 0;
-        valid[k] = false;
-        a[k][0] = a[k][1] = a[k][2] = a[k][3] = 0.f;
-        nx2[k] = ny2[k] = nz2[k] = make_float2(0.f, 0.f);
+        for (int k = 0; k < KI; ++k) {
+            if constexpr (PK) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) b[k][q] = make_float2(0.f, 0.f);
-    }
+                for (int q = 0; q < 4; ++q) b[k][q] = make_float2(0.f, 0.f);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) a[k][q] = 0.f;
+            }
+        }
+    };
+    clear_acc();
+#pragma unroll
+    for (int k = 0; k < (PK ? 1 : KI); ++k) xih[k] = yih[k] = zih[k] = 0.f;
+#pragma unroll
+    for (int k = 0; k < (PK ? KI : 1); ++k) nx2[k] = ny2[k] = nz2[k] = make_float2(0.f, 0.f);
 
     auto flush = [&]() {
 #pragma unroll
         for (int k = 0; k < KI; ++k) {
             if (k >= ku) continue;
-            if constexpr (PK) {
-                a[k][0] += b[k][0].x + b[k][0].y;
-                a[k][1] += b[k][1].x + b[k][1].y;
-                a[k][2] += b[k][2].x + b[k][2].y;
-                a[k][3] -= b[k][3].x + b[k][3].y;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) b[k][q] = make_float2(0.f, 0.f);
-            }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
+                float x;
+                if constexpr (PK) {
+                    x = b[k][q].x + b[k][q].y;
+                    if (q == 3) x = -x;
+                } else {
+                    x = a[k][q];
+                }
                 float2 v = s.acc[k][q][ct];
                 float e;
-                two_sum(v.x, a[k][q], v.x, e);
+                two_sum(v.x, x, v.x, e);
                 v.y += e;
                 s.acc[k][q][ct] = v;
-                a[k][q] = 0.f;
             }
         }
+        clear_acc();
         since = 0;
     };
     auto push_retest = [&](int k, int64_t jidx) -> int {
+        const int gi = gbase + k * S;
         const int r = atomicAdd(p.n_retest, 1);
         if (r < p.retest_cap) {
             Retest rr;
             rr.j_begin = jidx;
-            rr.i = gi[k];
+            rr.i = gi;
             rr.n = 1;
             p.retest[r] = rr;
             return 0;
         }
-        const EpiDev ei = p.epi[gi[k]];
+        const EpiDev ei = p.epi[gi];
         const int id = p.id_epj[jidx];
         const EpjMix e = p.epj[id];
         return exact_neighbour(ei.x, ei.y, ei.z, ei.rs, e.x, e.y, e.z, p.epj_rs64[id], p.eps2);
@@ -490,36 +524,43 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
     auto ep_tile = [&](auto ku_c, const Hdr& h, int sl) {
         constexpr int KU = decltype(ku_c)::value;
         const auto& T = s.slot[sl].ep;
-        int c[KU];
-#pragma unroll
-        for (int k = 0; k < KU; ++k) c[k] = 0;
         const int pn = (h.nn + n_js - 1) / n_js;
         const int j0 = min(h.nn, js * pn);
         const int j1 = min(h.nn, j0 + pn);
-#pragma unroll 2
-        for (int j = j0; j < j1; ++j) {
-            const float4 hh = T.nh[j];
-            const float4 ll = T.nl[j];
+        if (j1 > j0) {
+            float4 lo[KU];
+            int kb[KU], c[KU];
+            bool vk[KU];
 #pragma unroll
             for (int k = 0; k < KU; ++k) {
-                const float dx = (hh.x - xih[k]) + (ll.x - xil[k]);
-                const float dy = (hh.y - yih[k]) + (ll.y - yil[k]);
-                const float dz = (hh.z - zih[k]) + (ll.z - zil[k]);
-                float r2 = fmaf(dx, dx, eps2);
-                r2 = fmaf(dy, dy, r2);
-                r2 = fmaf(dz, dz, r2);
-                const float rs2 = fmaxf(rsi2[k], ll.w);
-                const int e = __float_as_int(r2) - __float_as_int(rs2) + kb[k];
-                c[k] += (int)((unsigned)e >> 31);
-                if ((unsigned)e < (unsigned)(2 * kb[k]) && valid[k]) c[k] += push_retest(k, h.base + T.nidx[j]);
-                const float ri = rsqrt_approx(fmaxf(r2, rcut2));
-                const float mri = hh.w * ri;
-                const float mri3 = mri * (ri * ri);
-                a[k][0] = fmaf(mri3, dx, a[k][0]);
-                a[k][1] = fmaf(mri3, dy, a[k][1]);
-                a[k][2] = fmaf(mri3, dz, a[k][2]);
-                a[k][3] -= mri;
+                lo[k] = s.nlo[k][ct];
+                kb[k] = s.nkb[k][ct];
+                c[k] = 0;
+                vk[k] = slot + k * S < nip;
             }
+#pragma unroll 1
+            for (int j = j0; j < j1; ++j) {
+                const float4 hh = T.nh[j];
+                const float4 ll = T.nl[j];
+#pragma unroll
+                for (int k = 0; k < KU; ++k) {
+                    const float dx = (hh.x - xi(k)) + (ll.x - lo[k].x);
+                    const float dy = (hh.y - yi(k)) + (ll.y - lo[k].y);
+                    const float dz = (hh.z - zi(k)) + (ll.z - lo[k].z);
+                    float r2 = fmaf(dx, dx, eps2);
+                    r2 = fmaf(dy, dy, r2);
+                    r2 = fmaf(dz, dz, r2);
+                    const float rs2 = fmaxf(lo[k].w, ll.w);
+                    const int e = __float_as_int(r2) - __float_as_int(rs2) + kb[k];
+                    c[k] += (int)((unsigned)e >> 31);
+                    if ((unsigned)e < (unsigned)(2 * kb[k]) && vk[k]) c[k] += push_retest(k, h.base + T.nidx[j]);
+                    const float ri = rsqrt_approx(fmaxf(r2, rcut2));
+                    const float mri = hh.w * ri;
+                    acc4(k, mri * (ri * ri), dx, dy, dz, mri);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < KU; ++k) s.cnt[k][ct] += c[k];
         }
         int nfar;
         if constexpr (PK) {
@@ -579,8 +620,6 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
             }
             nfar = f1 - f0;
         }
-#pragma unroll
-        for (int k = 0; k < KU; ++k) cnt[k] += c[k];
         since += (j1 - j0) + nfar;
     };
 
@@ -677,7 +716,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
         const Hdr h = s.hdr[sl];
         if (h.kind == kItemExit) return;
         if (h.kind == kItemBegin) {
-            wd = p.walks[h.walk];
+            const WalkDesc wd = p.walks[h.walk];
             rcut2 = (float)wd.rcut2;
             nip = min(kMaxPass, wd.n_i - h.ipass);
             ku = KI;
@@ -689,38 +728,39 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
             js = ct / S;
             slot = ct - js * S;
             active = js < n_js;
+            gbase = wd.i_begin + h.ipass + slot;
 #pragma unroll
             for (int k = 0; k < KI; ++k) {
-                const int li = slot + k * S;
-                valid[k] = active && k < ku && li < nip;
-                gi[k] = wd.i_begin + h.ipass + li;
-                xih[k] = yih[k] = zih[k] = xil[k] = yil[k] = zil[k] = 0.f;
-                rsi2[k] = 0.f;
-                kb[k] = 0;
-                cnt[k] = 0;
-                if (valid[k]) {
-                    const EpiDev e = p.epi[gi[k]];
+                const bool valid = active && k < ku && slot + k * S < nip;
+                float hx = 0.f, hy = 0.f, hz = 0.f;
+                float4 lo = make_float4(0.f, 0.f, 0.f, 0.f);
+                int kb = 0;
+                if (valid) {
+                    const EpiDev e = p.epi[gbase + k * S];
                     const double dx = e.x - wd.cx, dy = e.y - wd.cy, dz = e.z - wd.cz;
-                    xih[k] = (float)dx;
-                    yih[k] = (float)dy;
-                    zih[k] = (float)dz;
-                    xil[k] = (float)(dx - (double)xih[k]);
-                    yil[k] = (float)(dy - (double)yih[k]);
-                    zil[k] = (float)(dz - (double)zih[k]);
-                    rsi2[k] = (float)(e.rs * e.rs);
-                    kb[k] = kband_near(fmax(fabs(dx), fmax(fabs(dy), fabs(dz))), e.rs, eps2d);
+                    hx = (float)dx;
+                    hy = (float)dy;
+                    hz = (float)dz;
+                    lo = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz),
+                                     (float)(e.rs * e.rs));
+                    kb = kband_near(fmax(fabs(dx), fmax(fabs(dy), fabs(dz))), e.rs, eps2d);
                 }
-                nx2[k] = make_float2(-xih[k], -xih[k]);
-                ny2[k] = make_float2(-yih[k], -yih[k]);
-                nz2[k] = make_float2(-zih[k], -zih[k]);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) b[k][q] = make_float2(0.f, 0.f);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    a[k][q] = 0.f;
-                    s.acc[k][q][ct] = make_float2(0.f, 0.f);
+                if constexpr (PK) {
+                    nx2[k] = make_float2(-hx, -hx);
+                    ny2[k] = make_float2(-hy, -hy);
+                    nz2[k] = make_float2(-hz, -hz);
+                } else {
+                    xih[k] = hx;
+                    yih[k] = hy;
+                    zih[k] = hz;
                 }
+                s.nlo[k][ct] = lo;
+                s.nkb[k][ct] = kb;
+                s.cnt[k][ct] = 0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) s.acc[k][q][ct] = make_float2(0.f, 0.f);
             }
+            clear_acc();
             since = 0;
         } else if (h.kind == kItemEP) {
             if (active) {
@@ -739,17 +779,13 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
                 if (since >= kFlush) flush();
             }
         } else {  // kItemEnd: reduce the j-slices of the pass and write
-            if (active) {
-                flush();
-#pragma unroll
-                for (int k = 0; k < KI; ++k) s.cnt[k][ct] = cnt[k];
-            }
+            if (active) flush();
             consumers_sync(CT);
             if (active && js == 0) {
                 const double G = p.G;
 #pragma unroll
                 for (int k = 0; k < KI; ++k) {
-                    if (!valid[k]) continue;
+                    if (!(k < ku && slot + k * S < nip)) continue;
                     double r[4] = {0.0, 0.0, 0.0, 0.0};
                     int n = 0;
                     for (int q = 0; q < n_js; ++q) {
@@ -761,8 +797,9 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
                         }
                         n += s.cnt[k][src];
                     }
-                    p.out_accp[gi[k]] = Accp{G * r[0], G * r[1], G * r[2], G * r[3]};
-                    p.out_nnb[gi[k]] = n;
+                    const int gi = gbase + k * S;
+                    p.out_accp[gi] = Accp{G * r[0], G * r[1], G * r[2], G * r[3]};
+                    p.out_nnb[gi] = n;
                 }
             }
             consumers_sync(CT);
