@@ -225,10 +225,12 @@ def fp32_peak_tflops() -> dict:
 def traffic_from_profiles() -> float | None:
     """DRAM bytes per launch of the main kernel from the committed ncu summary
     (a line 'dram_bytes_per_launch_scaled: <bytes>'), or None."""
-    for name in ("mixed_kernel_plummer1m_bin50.md", "mixed_kernel_plummer65k.md"):
+    # A capture of the 1M workload itself, else a smaller capture scaled to it.
+    for name, key in (("ws_kernel_plummer1m_bin50.md", "dram_bytes_per_launch"),
+                      ("ws_kernel_plummer256k_bin50.md", "dram_bytes_per_launch_scaled")):
         p = ROOT / "profiles" / name
         if p.exists():
-            m = re.search(r"dram_bytes_per_launch(?:_scaled)?:\s*([0-9.eE+]+)", p.read_text())
+            m = re.search(key + r":\s*([0-9.eE+]+)", p.read_text())
             if m:
                 return float(m.group(1))
     return None
@@ -465,11 +467,12 @@ def run_ours(args):
     peak = max(v for v in peaks.values() if v) if any(peaks.values()) else None
     main_s = statistics.mean(main_ms) / 1e3
     achieved = flops / main_s / 1e12
+    kernel_name = "mixed_kernel" if best_variant == 0 else f"ws_kernel (variant {best_variant})"
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak if peak else None, "traffic": traffic_from_profiles(),
             "peak_source": "FP32 FMA loops measured in this run, the faster of scalar and packed FP32x2 "
                            "(MEASURED_PEAKS.json has no FP32 figure)", "peaks_measured": peaks,
-            "flops_per_launch": flops, "kernel": "mixed_kernel", "launch_ms": 1e3 * main_s,
+            "flops_per_launch": flops, "kernel": kernel_name, "launch_ms": 1e3 * main_s,
             "flop_model": "19 per EP-EP, 54 per EP-SP interaction"}
 
     cpu = None

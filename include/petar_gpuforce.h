@@ -52,6 +52,14 @@ enum {
     PGF_PRECISION_FP64 = 1   /* plain FP64 throughout */
 };
 
+/* What an index dispatch computes (pgf_set_mode). */
+enum {
+    PGF_MODE_FORCE = 0,           /* soft force: acc, pot and n_ngb (default) */
+    PGF_MODE_NEIGHBOR_SEARCH = 1  /* n_ngb only, as SearchNeighborEpEpNoSimd
+                                     (src/soft_force.hpp:11-34): r^2 < max(rs_i, rs_j)^2
+                                     without softening; SPJ lists are ignored */
+};
+
 /* Record layouts (sizes and byte offsets). */
 typedef struct pgf_epi_layout {
     size_t size;         /* sizeof(EPISoft) */
@@ -103,6 +111,13 @@ int pgf_initialize(int rank, double eps2, double rcut2, double G);
 
 /* Chooses the kernel used by later dispatches (PGF_PRECISION_*). */
 int pgf_set_precision(int precision);
+
+/* Selects what later dispatches compute (PGF_MODE_*).  Each tag keeps the
+ * mode of its dispatch; retrieve of a neighbour-search dispatch overwrites
+ * n_ngb only and leaves acc and pot as they are.  The GPU counterpart of the
+ * reference's CPU search functor SearchNeighborEpEpNoSimd
+ * (src/soft_force.hpp:11-34); counts are exact as in the force mode. */
+int pgf_set_mode(int mode);
 
 /* Mixed-precision kernel variants: 0 is the CTA-synchronous tiled kernel;
  * 1..PGF_NUM_KERNEL_VARIANTS-1 are warp-specialised producer/consumer kernels

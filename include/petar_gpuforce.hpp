@@ -88,6 +88,7 @@ struct CalcForceWithLinearCutoffCUDAMultiWalk {
                        const bool send_flag) {
         using namespace petar_gpuforce;
         check(pgf_initialize(my_rank, eps2, rcut2, G), "pgf_initialize");
+        check(pgf_set_mode(PGF_MODE_FORCE), "pgf_set_mode");
         const pgf_epi_layout il = epi_layout<EPISoft>();
         const pgf_epj_layout jl = epj_layout<EPJSoft>();
         const pgf_spj_layout sl = spj_layout<SPJSoft>();
@@ -121,6 +122,7 @@ struct CalcForceWithLinearCutoffCUDA {
                        const EPJSoft* epj[], const PS::S32 n_epj[], const SPJSoft* spj[], const PS::S32 n_spj[]) {
         using namespace petar_gpuforce;
         check(pgf_initialize(my_rank, eps2, rcut2, G), "pgf_initialize");
+        check(pgf_set_mode(PGF_MODE_FORCE), "pgf_set_mode");
         const pgf_epi_layout il = epi_layout<EPISoft>();
         const pgf_epj_layout jl = epj_layout<EPJSoft>();
         const pgf_spj_layout sl = spj_layout<SPJSoft>();
@@ -128,6 +130,39 @@ struct CalcForceWithLinearCutoffCUDA {
                            reinterpret_cast<const void* const*>(epj), n_epj, &jl,
                            reinterpret_cast<const void* const*>(spj), n_spj, &sl),
               "pgf_dispatch");
+        return 0;
+    }
+};
+
+// Multi-walk GPU form of SearchNeighborEpEpNoSimd (src/soft_force.hpp:11-34):
+// the same dispatch signature as the force functor; RetrieveForceCUDA then
+// overwrites n_ngb only.  Counts use r^2 < max(rs_i, rs_j)^2 without
+// softening; SPJ lists are ignored.
+struct SearchNeighborEpEpCUDAMultiWalk {
+    PS::S32 my_rank;
+    PS::F64 eps2;
+    PS::F64 rcut2;
+    PS::F64 G;
+
+    SearchNeighborEpEpCUDAMultiWalk() {}
+    SearchNeighborEpEpCUDAMultiWalk(PS::S32 _rank, PS::F64 _eps2, PS::F64 _rcut2, PS::F64 _G)
+        : my_rank(_rank), eps2(_eps2), rcut2(_rcut2), G(_G) {}
+
+    PS::S32 operator()(const PS::S32 tag, const PS::S32 n_walk, const EPISoft** epi, const PS::S32* n_epi,
+                       const PS::S32** id_epj, const PS::S32* n_epj, const PS::S32** id_spj, const PS::S32* n_spj,
+                       const EPJSoft* epj, const PS::S32 n_epj_tot, const SPJSoft* spj, const PS::S32 n_spj_tot,
+                       const bool send_flag) {
+        using namespace petar_gpuforce;
+        check(pgf_initialize(my_rank, eps2, rcut2, G), "pgf_initialize");
+        check(pgf_set_mode(PGF_MODE_NEIGHBOR_SEARCH), "pgf_set_mode");
+        const pgf_epi_layout il = epi_layout<EPISoft>();
+        const pgf_epj_layout jl = epj_layout<EPJSoft>();
+        const pgf_spj_layout sl = spj_layout<SPJSoft>();
+        check(pgf_dispatch_index(tag, n_walk, reinterpret_cast<const void* const*>(epi), n_epi, &il,
+                                 reinterpret_cast<const int* const*>(id_epj), n_epj,
+                                 reinterpret_cast<const int* const*>(id_spj), n_spj, epj, n_epj_tot, &jl, spj,
+                                 n_spj_tot, &sl, send_flag ? 1 : 0),
+              "pgf_dispatch_index");
         return 0;
     }
 };

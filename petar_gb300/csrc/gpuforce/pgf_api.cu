@@ -105,6 +105,7 @@ struct TagState {
     int64_t ni_tot = 0;
     int precision = PGF_PRECISION_MIXED;
     int variant = 0;
+    int mode = PGF_MODE_FORCE;
     std::vector<int> n_epi;
     std::vector<int64_t> epi_disp;
     DevBuf<EpiDev> epi;
@@ -140,6 +141,7 @@ struct State {
     int precision = PGF_PRECISION_MIXED;
     int variant = 0;  // mixed-precision kernel variant (pgf_set_kernel_variant)
     int stages = 0;   // dispatch pipeline stages (pgf_set_dispatch_stages); 0 = by size
+    int mode = PGF_MODE_FORCE;
     // shared j data
     DevBuf<EpjMix> epj;
     DevBuf<double> epj_m64, epj_rs64;
@@ -350,7 +352,11 @@ void bind_scratch(Params& p, int stage = -1, int n_stages = 1) {
 int launch_kernels(const TagState& t, const Params& p, cudaStream_t s, cudaEvent_t ev_start, cudaEvent_t ev_end) {
     PGF_CUDA(cudaEventRecord(ev_start, s));
     cudaError_t e;
-    if (t.precision == PGF_PRECISION_FP64) {
+    if (t.mode == PGF_MODE_NEIGHBOR_SEARCH) {
+        e = launch_ws_search(p, s, g.num_sms);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_end, s);
+        if (e == cudaSuccess && p.n_walk > 0) e = launch_retest(p, s, g.num_sms);
+    } else if (t.precision == PGF_PRECISION_FP64) {
         e = launch_fp64(p, s, g.num_sms);
         if (e == cudaSuccess) e = cudaEventRecord(ev_end, s);
         if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), s);
@@ -548,6 +554,7 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     t.n_epi.assign(n_epi, n_epi + n_walk);
     t.precision = g.precision;
     t.variant = g.variant;
+    t.mode = g.mode;
     Params& p = t.params;
     p = Params{};
     p.epi = t.epi.d;
@@ -563,7 +570,9 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     p.walks = t.walks.d;
     p.order = t.order.d;
     p.n_walk = n_walk;
-    p.eps2 = g.eps2;
+    // The neighbour search tests r^2 < max(rs_i, rs_j)^2 without softening
+    // (src/soft_force.hpp:11-34); the force kernels include eps^2.
+    p.eps2 = t.mode == PGF_MODE_NEIGHBOR_SEARCH ? 0.0 : g.eps2;
     p.G = g.G;
     p.out_accp = t.accp.d;
     p.out_nnb = t.nnb.d;
@@ -796,6 +805,12 @@ int pgf_set_kernel_variant(int variant) {
     return PGF_OK;
 }
 
+int pgf_set_mode(int mode) {
+    if (mode != PGF_MODE_FORCE && mode != PGF_MODE_NEIGHBOR_SEARCH) return fail(PGF_ERR_ARG, "unknown mode %d", mode);
+    g.mode = mode;
+    return PGF_OK;
+}
+
 int pgf_set_dispatch_stages(int stages) {
     if (stages < 0 || stages > kMaxChunks)
         return fail(PGF_ERR_ARG, "dispatch stages %d outside [0, %d]", stages, kMaxChunks);
@@ -886,12 +901,14 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
         const int64_t o = t.epi_disp[w];
         for (int i = 0; i < ni[w]; ++i) {
             char* r = base + (size_t)i * fl->size;
-            const Accp a = t.h_accp.h[o + i];
-            double* acc = reinterpret_cast<double*>(r + fl->off_acc);
-            acc[0] = a.x;
-            acc[1] = a.y;
-            acc[2] = a.z;
-            *reinterpret_cast<double*>(r + fl->off_pot) = a.w;
+            if (t.mode == PGF_MODE_FORCE) {
+                const Accp a = t.h_accp.h[o + i];
+                double* acc = reinterpret_cast<double*>(r + fl->off_acc);
+                acc[0] = a.x;
+                acc[1] = a.y;
+                acc[2] = a.z;
+                *reinterpret_cast<double*>(r + fl->off_pot) = a.w;
+            }
             if (fl->n_ngb_bytes == 8)
                 *reinterpret_cast<int64_t*>(r + fl->off_n_ngb) = t.h_nnb.h[o + i];
             else

@@ -155,5 +155,7 @@ cudaError_t launch_split_j(const EpjMix* epj, int64_t n_epj, EpjF32* epj32, cons
 // Warp-specialised kernel, variants 0..kNumWsVariants-1 (see pgf_kernels_ws.cu).
 constexpr int kNumWsVariants = 8;
 cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant);
+// Neighbour search (counts only, SPJ lists ignored) with the warp-specialised kernel.
+cudaError_t launch_ws_search(const Params& p, cudaStream_t s, int num_sms);
 
 }  // namespace pgf

@@ -15,7 +15,7 @@
 // * CW consumer warps take the items in order.  They never stage data and
 //   never wait for each other inside a pass: each waits only for the slot it
 //   needs (mbarrier "full") and releases it when done (mbarrier "empty").  The
-//   producer therefore runs ahead, across walk boundaries, by up to kSlots
+//   producer therefore runs ahead, across walk boundaries, by up to NS
 //   items.
 // * The producer works in FP32 only.  j positions arrive as (hi, lo) FP32
 //   pairs (EpjF32 / SpjF32); x - c is (x_hi - c_hi) + (x_lo - c_lo), and for
@@ -35,9 +35,9 @@
 namespace pgf {
 namespace {
 
-constexpr int kTileEP = 128;  // EPJ entries per tile (4 per producer lane)
-constexpr int kTileSP = 64;   // SPJ entries per tile (2 per producer lane)
-constexpr int kSlots = 4;     // ring depth
+// Ring geometry is a template parameter of each variant: TE EPJ entries per
+// EP tile (TE / 32 per producer lane), TE / 2 SPJ entries per SP tile, NS ring
+// slots.
 constexpr int kFlush = 256;   // pairs per consumer thread between FP64 flushes
 constexpr int kKMax = 1 << 22;
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;
@@ -57,6 +57,21 @@ __device__ __forceinline__ int kband_near(double D, double rs, double eps2) {
     if (!(r2ref > 0.0)) return kKMax;
     const double k = 48.0 + 1e-5 * D / sqrt(r2ref);
     return k >= double(kKMax) ? kKMax : int(k) + 1;
+}
+
+// L2 policy for data read once per launch (the id lists): evicted before
+// lines loaded with the default policy, so the streamed ids do not push the
+// EPJ/SPJ records (re-read by every walk) out of L2.
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ int ld_streamed(const int32_t* a, uint64_t pol) {
+    int v;
+    asm volatile("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    return v;
 }
 
 // Error-free sum: s + e == a + b exactly (round-to-nearest, no reassociation).
@@ -122,36 +137,40 @@ __device__ __forceinline__ void consumers_sync(int n_threads) {
 }
 
 // Scalar tiles: one float4 record per j.
+template <int TE>
 struct SlotEP {
-    float4 nh[kTileEP];  // near: hi x, y, z, m
-    float4 nl[kTileEP];  // near: lo x, y, z, rs2
-    float4 fr[kTileEP];  // far:  hi x, y, z, m
-    int nidx[kTileEP];   // near: entry index in the tile (for re-tests)
+    float4 nh[TE];  // near: hi x, y, z, m
+    float4 nl[TE];  // near: lo x, y, z, rs2
+    float4 fr[TE];  // far:  hi x, y, z, m
+    int nidx[TE];   // near: entry index in the tile (for re-tests)
 };
+template <int TE>
 struct SlotSP {
-    float4 sp[kTileSP][3];
+    float4 sp[TE / 2][3];
 };
 // Packed tiles: far EPJ and SPJ as pairs of j, component-interleaved, so a
 // consumer reads (x0, x1), (y0, y1), ... as float2 operands of the FP32x2
 // instructions.  An odd last entry is paired with a massless dummy at 1e15.
+template <int TE>
 struct SlotEPx2 {
-    float4 nh[kTileEP];
-    float4 nl[kTileEP];
-    float4 fp[kTileEP / 2][2];  // (x0 x1 y0 y1), (z0 z1 m0 m1)
-    int nidx[kTileEP];
+    float4 nh[TE];
+    float4 nl[TE];
+    float4 fp[TE / 2][2];  // (x0 x1 y0 y1), (z0 z1 m0 m1)
+    int nidx[TE];
 };
+template <int TE>
 struct SlotSPx2 {
-    float4 sp[kTileSP / 2][6];  // x, y, z, m, -Qxx, -Qyy, -Qzz, -Qxy, -Qxz, -Qyz, -c (pairs), pad
+    float4 sp[TE / 4][6];  // x, y, z, m, -Qxx, -Qyy, -Qzz, -Qxy, -Qxz, -Qyz, -c (pairs), pad
 };
-template <bool PK>
+template <bool PK, int TE>
 union Slot {
-    SlotEP ep;
-    SlotSP sp;
+    SlotEP<TE> ep;
+    SlotSP<TE> sp;
 };
-template <>
-union Slot<true> {
-    SlotEPx2 ep;
-    SlotSPx2 sp;
+template <int TE>
+union Slot<true, TE> {
+    SlotEPx2<TE> ep;
+    SlotSPx2<TE> sp;
 };
 constexpr float kDummyPos = 1e15f;
 struct Hdr {
@@ -164,12 +183,12 @@ struct Hdr {
     int64_t base;  // first list entry of the tile
 };
 
-template <int CW, int KI, bool PK>
+template <int CW, int KI, bool PK, int TE, int NS>
 struct Smem {
-    Slot<PK> slot[kSlots];
-    Hdr hdr[kSlots];
-    uint64_t full[kSlots];
-    uint64_t empty[kSlots];
+    Slot<PK, TE> slot[NS];
+    Hdr hdr[NS];
+    uint64_t full[NS];
+    uint64_t empty[NS];
     float2 acc[KI][4][CW * 32];  // (hi, lo) FP32 accumulators of the flushed partials
     int cnt[KI][CW * 32];        // neighbour counts
     float4 nlo[KI][CW * 32];     // near-pair data of each i: lo x, y, z and r_search^2
@@ -178,10 +197,16 @@ struct Smem {
 
 // ---------------------------------------------------------------- producer
 
-template <int CW, int KI, bool PK>
-__device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
+// SR (neighbour search): EPJ tiles only, near entries only; far entries can
+// hold no neighbour and SPJ lists are skipped.
+template <int CW, int KI, bool PK, bool SR, int TE, int NS>
+__device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int lane) {
     constexpr int kMaxPass = CW * 32 * KI;
+    constexpr int kTileEP = TE, kTileSP = TE / 2, kSlots = NS;
+    constexpr int QE = TE / 32, QS = TE / 64;  // EPJ and SPJ entries per lane and tile
+    static_assert(QS >= 1 && TE % 64 == 0, "EP tiles of a multiple of 64 entries");
     const float eps2 = (float)p.eps2;
+    const uint64_t stream_pol = l2_evict_first_policy();
     unsigned item = 0;
     auto acquire = [&](int& sl) -> bool {
         sl = item % kSlots;
@@ -214,7 +239,7 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
         const float rsmax2 = wd.rs_max * wd.rs_max;
         const float hmax = fmaxf(wd.hx, fmaxf(wd.hy, wd.hz));
         const int n_ept = (wd.n_epj + kTileEP - 1) / kTileEP;
-        const int n_spt = (wd.n_spj + kTileSP - 1) / kTileSP;
+        const int n_spt = SR ? 0 : (wd.n_spj + kTileSP - 1) / kTileSP;
         for (int ipass = 0; ipass < wd.n_i; ipass += kMaxPass) {
             int sl;
             if (!acquire(sl)) return;
@@ -228,15 +253,15 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
             for (int t = 0; t < n_ept; ++t) {
                 const int64_t base = wd.epj_begin + (int64_t)t * kTileEP;
                 const int nt = min(kTileEP, wd.n_epj - t * kTileEP);
-                int id[4];
-                float4 r0[4], r1[4];
+                int id[QE];
+                float4 r0[QE], r1[QE];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
+                for (int q = 0; q < QE; ++q) {
                     const int e = q * 32 + lane;
-                    id[q] = e < nt ? __ldg(p.id_epj + base + e) : -1;
+                    id[q] = e < nt ? ld_streamed(p.id_epj + base + e, stream_pol) : -1;
                 }
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
+                for (int q = 0; q < QE; ++q) {
                     if (id[q] >= 0) {
                         const float4* src = reinterpret_cast<const float4*>(p.epj32 + id[q]);
                         r0[q] = __ldg(src);
@@ -249,7 +274,7 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
                 auto& S = s.slot[sl].ep;
                 int nn = 0, nf = 0;
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
+                for (int q = 0; q < QE; ++q) {
                     const int e = q * 32 + lane;
                     const bool valid = e < nt;
                     bool near = false;
@@ -284,14 +309,14 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
                         }
                     }
                     const unsigned bn = __ballot_sync(0xffffffffu, valid && near);
-                    const unsigned bf = __ballot_sync(0xffffffffu, valid && !near);
+                    const unsigned bf = __ballot_sync(0xffffffffu, valid && !near && !SR);
                     const unsigned lt = (1u << lane) - 1u;
                     if (valid && near) {
                         const int pos = nn + __popc(bn & lt);
                         S.nh[pos] = make_float4(hx, hy, hz, m);
                         S.nl[pos] = make_float4(lx, ly, lz, rs2);
                         S.nidx[pos] = e;
-                    } else if (valid) {
+                    } else if (valid && !SR) {
                         const int pos = nf + __popc(bf & lt);
                         if constexpr (PK) {
                             float* f = reinterpret_cast<float*>(&S.fp[pos >> 1][0]) + (pos & 1);
@@ -306,7 +331,7 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
                     nn += __popc(bn);
                     nf += __popc(bf);
                 }
-                if constexpr (PK) {
+                if constexpr (PK && !SR) {
                     if ((nf & 1) && lane == 0) {
                         float* f = reinterpret_cast<float*>(&S.fp[nf >> 1][0]) + 1;
                         f[0] = f[2] = f[4] = kDummyPos;
@@ -325,15 +350,15 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
             for (int t = 0; t < n_spt; ++t) {
                 const int64_t base = wd.spj_begin + (int64_t)t * kTileSP;
                 const int nt = min(kTileSP, wd.n_spj - t * kTileSP);
-                int id[2];
-                float4 r[2][4];
+                int id[QS];
+                float4 r[QS][4];
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
+                for (int q = 0; q < QS; ++q) {
                     const int e = q * 32 + lane;
-                    id[q] = e < nt ? __ldg(p.id_spj + base + e) : -1;
+                    id[q] = e < nt ? ld_streamed(p.id_spj + base + e, stream_pol) : -1;
                 }
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
+                for (int q = 0; q < QS; ++q) {
                     if (id[q] >= 0) {
                         const float4* src = reinterpret_cast<const float4*>(p.spj32 + id[q]);
 #pragma unroll
@@ -343,7 +368,7 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK>& s, int lane) {
                 if (!acquire(sl)) return;
                 auto& S = s.slot[sl].sp;
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
+                for (int q = 0; q < QS; ++q) {
                     const int e = q * 32 + lane;
                     if (e < nt) {
                         // SpjF32: (xh yh zh m) (xl yl zl tr) (Qxx Qyy Qzz Qxy) (Qxz Qyz pad pad)
@@ -417,8 +442,9 @@ __device__ __forceinline__ float pass_cost(int nip, int ku, int ct_threads) {
 // coordinates and the pair accumulators.  The near-only data of each i (lo
 // coordinates, r_search^2, guard band) and the neighbour counts live in
 // shared memory and are read once per tile that has near entries.
-template <int CW, int KI, bool PK>
-__device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
+template <int CW, int KI, bool PK, bool SR, int TE, int NS>
+__device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int ct) {
+    constexpr int kSlots = NS;
     constexpr int CT = CW * 32;
     constexpr int kMaxPass = CT * KI;
     constexpr int KA = KI > 1 ? KI - 1 : 1;  // the other i-per-thread count a pass may use
@@ -439,6 +465,16 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
     float2 nx2[PK ? KI : 1], ny2[PK ? KI : 1], nz2[PK ? KI : 1];
     float2 b[PK ? KI : 1][4];
     int since = 0;
+#pragma unroll
+    for (int k = 0; k < (PK ? 1 : KI); ++k) {
+        xih[k] = yih[k] = zih[k] = 0.f;
+        a[k][0] = a[k][1] = a[k][2] = a[k][3] = 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < (PK ? KI : 1); ++k) {
+        nx2[k] = ny2[k] = nz2[k] = make_float2(0.f, 0.f);
+        b[k][0] = b[k][1] = b[k][2] = b[k][3] = make_float2(0.f, 0.f);
+    }
     auto xi = [&](int k) -> float {
         if constexpr (PK) return -nx2[k].x; else return xih[k];
     };
@@ -474,11 +510,6 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
             }
         }
     };
-    clear_acc();
-#pragma unroll
-    for (int k = 0; k < (PK ? 1 : KI); ++k) xih[k] = yih[k] = zih[k] = 0.f;
-#pragma unroll
-    for (int k = 0; k < (PK ? KI : 1); ++k) nx2[k] = ny2[k] = nz2[k] = make_float2(0.f, 0.f);
 
     auto flush = [&]() {
 #pragma unroll
@@ -554,16 +585,20 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
                     const int e = __float_as_int(r2) - __float_as_int(rs2) + kb[k];
                     c[k] += (int)((unsigned)e >> 31);
                     if ((unsigned)e < (unsigned)(2 * kb[k]) && vk[k]) c[k] += push_retest(k, h.base + T.nidx[j]);
-                    const float ri = rsqrt_approx(fmaxf(r2, rcut2));
-                    const float mri = hh.w * ri;
-                    acc4(k, mri * (ri * ri), dx, dy, dz, mri);
+                    if constexpr (!SR) {
+                        const float ri = rsqrt_approx(fmaxf(r2, rcut2));
+                        const float mri = hh.w * ri;
+                        acc4(k, mri * (ri * ri), dx, dy, dz, mri);
+                    }
                 }
             }
 #pragma unroll
             for (int k = 0; k < KU; ++k) s.cnt[k][ct] += c[k];
         }
-        int nfar;
-        if constexpr (PK) {
+        int nfar = 0;
+        if constexpr (SR) {
+            // no far entries in a neighbour search
+        } else if constexpr (PK) {
             // far pairs of j, two per FP32x2 instruction
             const int np = (h.nf + 1) >> 1;
             const int pp = (np + n_js - 1) / n_js;
@@ -798,7 +833,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
                         n += s.cnt[k][src];
                     }
                     const int gi = gbase + k * S;
-                    p.out_accp[gi] = Accp{G * r[0], G * r[1], G * r[2], G * r[3]};
+                    if constexpr (!SR) p.out_accp[gi] = Accp{G * r[0], G * r[1], G * r[2], G * r[3]};
                     p.out_nnb[gi] = n;
                 }
             }
@@ -809,43 +844,43 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK>& s, int ct) {
     }
 }
 
-template <int CW, int KI, int MINB, bool PK>
+template <int CW, int KI, int MINB, bool PK, bool SR, int TE, int NS>
 __global__ __launch_bounds__((CW + 1) * 32, MINB) void ws_kernel(Params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    Smem<CW, KI, PK>& s = *reinterpret_cast<Smem<CW, KI, PK>*>(smem_raw);
+    Smem<CW, KI, PK, TE, NS>& s = *reinterpret_cast<Smem<CW, KI, PK, TE, NS>*>(smem_raw);
     const int tid = threadIdx.x;
     if (tid == 0) {
-        for (int i = 0; i < kSlots; ++i) {
+        for (int i = 0; i < NS; ++i) {
             mbar_init(&s.full[i], 32);
             mbar_init(&s.empty[i], CW * 32);
         }
     }
     __syncthreads();
     if (tid >= CW * 32)
-        producer<CW, KI, PK>(p, s, tid - CW * 32);
+        producer<CW, KI, PK, SR, TE, NS>(p, s, tid - CW * 32);
     else
-        consumer<CW, KI, PK>(p, s, tid);
+        consumer<CW, KI, PK, SR, TE, NS>(p, s, tid);
 }
 
-template <int CW, int KI, int MINB, bool PK>
+template <int CW, int KI, int MINB, bool PK, bool SR = false, int TE = 128, int NS = 4>
 cudaError_t launch_ws_t(const Params& p, cudaStream_t st, int num_sms) {
     cudaError_t e = cudaMemsetAsync(p.queue_head, 0, sizeof(int32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), st);
     if (e != cudaSuccess) return e;
     if (p.n_walk <= 0) return cudaSuccess;
     static int per_sm = 0;
-    const size_t smem = sizeof(Smem<CW, KI, PK>);
+    const size_t smem = sizeof(Smem<CW, KI, PK, TE, NS>);
     if (per_sm == 0) {
-        e = cudaFuncSetAttribute(ws_kernel<CW, KI, MINB, PK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(ws_kernel<CW, KI, MINB, PK, SR, TE, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ws_kernel<CW, KI, MINB, PK>, (CW + 1) * 32, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ws_kernel<CW, KI, MINB, PK, SR, TE, NS>, (CW + 1) * 32, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
     int grid = num_sms * per_sm;
     if (grid > p.n_walk) grid = p.n_walk;
-    ws_kernel<CW, KI, MINB, PK><<<grid, (CW + 1) * 32, smem, st>>>(p);
+    ws_kernel<CW, KI, MINB, PK, SR, TE, NS><<<grid, (CW + 1) * 32, smem, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -897,19 +932,24 @@ cudaError_t launch_split_j(const EpjMix* epj, int64_t n_epj, EpjF32* epj32, cons
 }
 
 // Variants of the warp-specialised kernel: consumer warps, i per consumer
-// thread, minimum CTAs per SM.
+// thread, minimum CTAs per SM, packed FP32x2, and the ring geometry (EP tile
+// entries, slots).
 cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant) {
     switch (variant) {
         case 0: return launch_ws_t<4, 3, 4, false>(p, s, num_sms);
-        case 1: return launch_ws_t<4, 2, 4, false>(p, s, num_sms);
-        case 2: return launch_ws_t<4, 4, 4, false>(p, s, num_sms);
-        case 3: return launch_ws_t<8, 2, 3, false>(p, s, num_sms);
+        case 1: return launch_ws_t<4, 3, 4, false, false, 64, 8>(p, s, num_sms);
+        case 2: return launch_ws_t<4, 3, 4, true, false, 64, 8>(p, s, num_sms);
+        case 3: return launch_ws_t<4, 2, 4, true, false, 64, 8>(p, s, num_sms);
         case 4: return launch_ws_t<4, 2, 4, true>(p, s, num_sms);
         case 5: return launch_ws_t<4, 3, 4, true>(p, s, num_sms);
-        case 6: return launch_ws_t<4, 1, 5, true>(p, s, num_sms);
-        case 7: return launch_ws_t<8, 2, 3, true>(p, s, num_sms);
+        case 6: return launch_ws_t<4, 4, 4, false, false, 64, 8>(p, s, num_sms);
+        case 7: return launch_ws_t<4, 3, 3, true, false, 128, 6>(p, s, num_sms);
         default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_ws_search(const Params& p, cudaStream_t s, int num_sms) {
+    return launch_ws_t<4, 3, 4, false, true>(p, s, num_sms);
 }
 
 }  // namespace pgf

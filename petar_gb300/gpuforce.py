@@ -27,6 +27,8 @@ PGF_OK = 0
 PGF_PRECISION_MIXED = 0
 PGF_PRECISION_FP64 = 1
 NUM_KERNEL_VARIANTS = 9  # PGF_NUM_KERNEL_VARIANTS
+PGF_MODE_FORCE = 0
+PGF_MODE_NEIGHBOR_SEARCH = 1
 
 # PeTar's EPISoft (src/soft_ptcl.hpp:271-308): id, pos, r_search, rank_org, type.
 EPI_DTYPE = np.dtype([("id", "<i8"), ("pos", "<f8", 3), ("r_search", "<f8"), ("rank_org", "<i4"),
@@ -123,6 +125,7 @@ def load(build: bool = True) -> ctypes.CDLL:
         "pgf_recompute": [ci],
         "pgf_set_kernel_variant": [ci],
         "pgf_set_dispatch_stages": [ci],
+        "pgf_set_mode": [ci],
         "pgf_get_kernel_variant": [vp],
         "pgf_autotune": [ci, ci, vp, vp],
         "pgf_wait": [ci],
@@ -183,6 +186,11 @@ def set_walk_rcut2(walk_rcut2: np.ndarray | None) -> None:
 
 def set_kernel_variant(variant: int) -> None:
     _check(load().pgf_set_kernel_variant(variant))
+
+
+def set_mode(mode: int) -> None:
+    """PGF_MODE_FORCE (default) or PGF_MODE_NEIGHBOR_SEARCH for later dispatches."""
+    _check(load().pgf_set_mode(mode))
 
 
 def set_dispatch_stages(stages: int) -> None:
@@ -366,3 +374,17 @@ def compute(batch, precision: int = PGF_PRECISION_MIXED, rec: Records | None = N
     dispatch(rec)
     f = retrieve(rec)
     return dict(acc=f["acc"].copy(), pot=f["pot"].copy(), nnb=f["n_ngb"].copy())
+
+
+def search_neighbors(batch, rec: Records | None = None) -> np.ndarray:
+    """n_ngb of every EPI row of a WalkBatch in neighbour-search mode
+    (SearchNeighborEpEpNoSimd semantics: no softening in the test, SPJ lists
+    ignored).  acc and pot of the records are left as they were."""
+    rec = rec if rec is not None else Records(batch)
+    set_mode(PGF_MODE_NEIGHBOR_SEARCH)
+    try:
+        dispatch(rec)
+        f = retrieve(rec)
+    finally:
+        set_mode(PGF_MODE_FORCE)
+    return f["n_ngb"].copy()

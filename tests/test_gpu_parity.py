@@ -308,3 +308,31 @@ def test_pipelined_dispatch_rejects_bad_id_in_late_stage():
         gpuforce.set_dispatch_stages(0)
         wb.id_epj = good_ids
     check(wb, res, PGF_PRECISION_MIXED, label="after bad id")
+
+
+@pytest.mark.parametrize("case", ["kernel_test", "kernel_test_rsvar", "plummer2048_walks"])
+def test_neighbor_search_matches_reference_search_functor(case):
+    """Neighbour-search mode against the reference's SearchNeighborEpEpNoSimd
+    (compiled from its sources into the golden fixtures): bit-exact."""
+    wb, d = load_golden(case)
+    n = gpuforce.search_neighbors(wb)
+    np.testing.assert_array_equal(n, d["nosimd__nnb_search"])
+
+
+def test_neighbor_search_binaries_leaves_acc_and_pot():
+    """Binary-rich lists with softening: search counts follow the unsoftened
+    test, retrieve leaves acc and pot untouched, and the force mode is back
+    afterwards."""
+    wb = walks.build_walks(ics.make_plummer_cluster(24, 20000, 0.004, binary_fraction=0.5))
+    wb.eps2 = 1e-6
+    rec = gpuforce.Records(wb)
+    rec.force["acc"] = 7.0
+    rec.force["pot"] = -3.0
+    n = gpuforce.search_neighbors(wb, rec)
+    o_search = oracle.force(wb, nnb_with_eps=False)
+    o_force = oracle.force(wb)
+    np.testing.assert_array_equal(n, o_search["nnb"])
+    assert (o_search["nnb"] != o_force["nnb"]).any()  # softening changes some counts
+    assert (rec.force["acc"] == 7.0).all() and (rec.force["pot"] == -3.0).all()
+    res = gpuforce.compute(wb, PGF_PRECISION_MIXED)
+    check(wb, res, PGF_PRECISION_MIXED, o=o_force, label="force after search")
