@@ -44,6 +44,13 @@ def _lib():
         lib.oracle_nnb_global.argtypes = [ctypes.c_int64, vp, vp, ctypes.c_double, vp]
         lib.oracle_direct.restype = None
         lib.oracle_direct.argtypes = [ctypes.c_int64, vp, ctypes.c_int64, vp, vp] + [ctypes.c_double] * 3 + [vp, vp]
+        lib.oracle_co_w.restype = None
+        lib.oracle_co_w.argtypes = [ctypes.c_int64] + [vp] * 5
+        lib.oracle_co_w_two.restype = None
+        lib.oracle_co_w_two.argtypes = [ctypes.c_int64] + [vp] * 7
+        lib.oracle_force_changeover.restype = None
+        lib.oracle_force_changeover.argtypes = ([ctypes.c_int64] + [vp] * 13 + [ctypes.c_double] * 3 + [vp]
+                                                + [vp] * 9 + [vp] * 4)
         _LIB = lib
     return _LIB
 
@@ -79,6 +86,49 @@ def force(batch, nnb_with_eps: bool = True, parts: bool = False) -> dict:
         float(batch.eps2), float(batch.rcut2), float(batch.G), _p(wr), int(bool(nnb_with_eps)),
         _p(out["acc"]), _p(out["pot"]), _p(out["nnb"]), _p(out.get("acc_ep")), _p(out.get("pot_ep")),
         _p(out.get("acc_sp")), _p(out.get("pot_sp")))
+    return out
+
+
+def co_w(r_in, r_out, dr):
+    """(W_acc, W_pot) of changeovers (r_in, r_out) at separations dr
+    (src/changeover.hpp:294-334)."""
+    r_in, r_out, dr = (_c(a, np.float64) for a in (r_in, r_out, dr))
+    a = np.zeros(dr.size)
+    p = np.zeros(dr.size)
+    _lib().oracle_co_w(dr.size, _p(r_in), _p(r_out), _p(dr), _p(a), _p(p))
+    return a, p
+
+
+def co_w_two(r_in1, r_out1, r_in2, r_out2, dr):
+    """The pair forms: W of the changeover with the larger r_out."""
+    arrs = [_c(a, np.float64) for a in (r_in1, r_out1, r_in2, r_out2, dr)]
+    n = arrs[-1].size
+    a = np.zeros(n)
+    p = np.zeros(n)
+    _lib().oracle_co_w_two(n, *[_p(x) for x in arrs], _p(a), _p(p))
+    return a, p
+
+
+def force_changeover(batch, co) -> dict:
+    """acc, pot_tot, pot_soft and nnb of every EPI row with the changeover
+    correction of its neighbours applied (see oracle_force_changeover).
+    ``co`` holds per-EPI id, r_in, r_out, self_mass and per-EPJ id, r_in,
+    r_out, mass_backup, status arrays (petar_gb300.walks.ChangeoverSet)."""
+    lib = _lib()
+    ni = batch.epi_rs.size
+    arrs = [_c(batch.epi_disp, np.int64), _c(batch.epi_pos, np.float64), _c(batch.epi_rs, np.float64),
+            _c(batch.epj_pos, np.float64), _c(batch.epj_mass, np.float64), _c(batch.epj_rs, np.float64),
+            _c(batch.spj_pos, np.float64), _c(batch.spj_mass, np.float64), _c(batch.spj_quad, np.float64),
+            _c(batch.epj_disp, np.int64), _c(batch.id_epj, np.int32), _c(batch.spj_disp, np.int64),
+            _c(batch.id_spj, np.int32)]
+    wr = None if batch.walk_rcut2 is None else _c(batch.walk_rcut2, np.float64)
+    coa = [_c(co.epi_id, np.int64), _c(co.epi_r_in, np.float64), _c(co.epi_r_out, np.float64),
+           _c(co.epi_self_mass, np.float64), _c(co.epj_id, np.int64), _c(co.epj_r_in, np.float64),
+           _c(co.epj_r_out, np.float64), _c(co.epj_mass_backup, np.float64), _c(co.epj_status, np.float64)]
+    out = dict(acc=np.zeros((ni, 3)), pot=np.zeros(ni), pot_soft=np.zeros(ni), nnb=np.zeros(ni, np.int64))
+    lib.oracle_force_changeover(batch.n_walk, *[_p(a) for a in arrs], float(batch.eps2), float(batch.rcut2),
+                                float(batch.G), _p(wr), *[_p(a) for a in coa], _p(out["acc"]), _p(out["pot"]),
+                                _p(out["pot_soft"]), _p(out["nnb"]))
     return out
 
 

@@ -184,3 +184,164 @@ void oracle_direct(int64_t n_target, const int64_t *target, int64_t n, const dou
         pot[t] = G * p;
     }
 }
+
+/* ---- Changeover functions (src/changeover.hpp, default build: the
+ * potential-based W of the #else branch, INTEGRATED_CUTOFF_FUNCTION unset) ---- */
+typedef struct {
+    double r_in, r_out, norm, coff, pot_off;
+} co_t;
+
+/* ChangeOver::setR(r_in, r_out), src/changeover.hpp:64-75. */
+static co_t co_make(double r_in, double r_out) {
+    co_t c;
+    c.r_in = r_in;
+    c.r_out = r_out;
+    c.norm = 1.0 / (r_out - r_in);
+    c.coff = (r_out - r_in) / (r_out + r_in);
+    c.pot_off = (1.0 + c.coff) / r_out;
+    return c;
+}
+
+/* calcPotW, src/changeover.hpp:294-309. */
+static double co_potw(const co_t *c, double dr) {
+    const double x = (dr - c->r_in) * c->norm;
+    double k = 1.0;
+    if (x >= 1.0) {
+        k = c->pot_off * dr;
+    } else if (x > 0.0) {
+        const double x2 = x * x;
+        const double x3 = x2 * x;
+        const double x5 = x2 * x3;
+        k -= c->coff * x5 * (5.0 * x3 - 20.0 * x2 + 28.0 * x - 14.0);
+    }
+    return k;
+}
+
+/* calcAcc0W, src/changeover.hpp:318-334. */
+static double co_acc0w(const co_t *c, double dr) {
+    double x = (dr - c->r_in) * c->norm;
+    x = (x < 1.0) ? x : 1.0;
+    x = (x > 0.0) ? x : 0.0;
+    const double x_1 = x - 1;
+    const double x_2 = x_1 * x_1;
+    const double x_4 = x_2 * x_2;
+    const double x2 = x * x;
+    const double x3 = x2 * x;
+    const double x4 = x2 * x2;
+    return x_4 * (1.0 + 4.0 * x + 10.0 * x2 + 20.0 * x3 + 35.0 * c->coff * x4);
+}
+
+/* calcAcc0WTwo / calcPotWTwo pick the changeover with the larger r_out, the
+ * second one on a tie (src/changeover.hpp:364-375). */
+static const co_t *co_pick(const co_t *a, const co_t *b) { return a->r_out > b->r_out ? a : b; }
+
+void oracle_co_w(int64_t n, const double *r_in, const double *r_out, const double *dr, double *acc0w,
+                 double *potw) {
+    for (int64_t i = 0; i < n; ++i) {
+        const co_t c = co_make(r_in[i], r_out[i]);
+        acc0w[i] = co_acc0w(&c, dr[i]);
+        potw[i] = co_potw(&c, dr[i]);
+    }
+}
+
+void oracle_co_w_two(int64_t n, const double *r_in1, const double *r_out1, const double *r_in2,
+                     const double *r_out2, const double *dr, double *acc0w, double *potw) {
+    for (int64_t i = 0; i < n; ++i) {
+        const co_t a = co_make(r_in1[i], r_out1[i]);
+        const co_t b = co_make(r_in2[i], r_out2[i]);
+        const co_t *c = co_pick(&a, &b);
+        acc0w[i] = co_acc0w(c, dr[i]);
+        potw[i] = co_potw(c, dr[i]);
+    }
+}
+
+/* Soft force of each EPI with the changeover correction of its tree
+ * neighbours applied, as PeTar composes it for one force evaluation:
+ *   1. the linear-cutoff EP-EP and EP-SP sums (oracle_force); FPSoft copies
+ *      ForceSoft.pot into pot_tot and pot_soft (src/soft_ptcl.hpp:84-95);
+ *   2. the self-potential G m / r_out for particles with a self term
+ *      (src/hard.hpp:1663-1674; self_mass is that mass, 0 for none);
+ *   3. for every other EPJ of the walk's list within the neighbour radius
+ *      (the count's test: |dx|^2 + eps2 < max(rs_i, rs_j)^2, which is the tree
+ *      search's for eps = 0), calcAccPotShortWithLinearCutoff for EPJSoft,
+ *      FP64 branch (src/hard.hpp:1404-1480): the cutoff term is replaced by
+ *      the changeover force k = 1 - W_acc(r) of the pair's larger r_out, and
+ *      the potentials follow the artificial-particle status of j (single:
+ *      status == 0 and mass_backup == 0; member: status < 0, potential from
+ *      mass_backup; otherwise the pair's potential is removed).
+ * r_out of the correction is the walk's cutoff radius (EPISoft::r_out). */
+void oracle_force_changeover(int64_t n_walk, const int64_t *epi_disp, const double *epi_pos,
+                             const double *epi_rs, const double *epj_pos, const double *epj_mass,
+                             const double *epj_rs, const double *spj_pos, const double *spj_mass,
+                             const double *spj_quad, const int64_t *epj_disp, const int32_t *id_epj,
+                             const int64_t *spj_disp, const int32_t *id_spj, double eps2, double rcut2, double G,
+                             const double *walk_rcut2, const int64_t *epi_id, const double *epi_rin,
+                             const double *epi_rout, const double *epi_mself, const int64_t *epj_id,
+                             const double *epj_rin, const double *epj_rout, const double *epj_mbk,
+                             const double *epj_status, double *acc, double *pot_tot, double *pot_soft,
+                             int64_t *nnb) {
+    oracle_force(n_walk, epi_disp, epi_pos, epi_rs, epj_pos, epj_mass, epj_rs, spj_pos, spj_mass, spj_quad,
+                 epj_disp, id_epj, spj_disp, id_spj, eps2, rcut2, G, walk_rcut2, 1, acc, pot_tot, nnb, 0, 0, 0, 0);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t w = 0; w < n_walk; ++w) {
+        const double r_out2 = walk_rcut2 ? walk_rcut2[w] : rcut2;
+        const double r_out = sqrt(r_out2);
+        for (int64_t i = epi_disp[w]; i < epi_disp[w + 1]; ++i) {
+            const double *xi = epi_pos + 3 * i;
+            const co_t ci = co_make(epi_rin[i], epi_rout[i]);
+            double ax = acc[3 * i + 0], ay = acc[3 * i + 1], az = acc[3 * i + 2];
+            double pt = pot_tot[i], ps = pot_tot[i];
+            if (epi_mself[i] != 0.0) {
+                const double pot_cor = G * epi_mself[i] / r_out;
+                pt += pot_cor;
+                ps += pot_cor;
+            }
+            for (int64_t k = epj_disp[w]; k < epj_disp[w + 1]; ++k) {
+                const int64_t j = id_epj[k];
+                if (epj_id[j] == epi_id[i]) continue;
+                const double rx = xi[0] - epj_pos[3 * j + 0];
+                const double ry = xi[1] - epj_pos[3 * j + 1];
+                const double rz = xi[2] - epj_pos[3 * j + 2];
+                const double dr2 = rx * rx + ry * ry + rz * rz;
+                const double dr2_eps = dr2 + eps2;
+                const double r_search = dmax(epi_rs[i], epj_rs[j]);
+                if (!(dr2_eps < r_search * r_search)) continue;
+                const double drinv = 1.0 / sqrt(dr2_eps);
+                double gmor = G * epj_mass[j] * drinv;
+                const double drinv2 = drinv * drinv;
+                const double gmor3 = gmor * drinv2;
+                const double dr_eps = drinv * dr2_eps;
+                const co_t cj = co_make(epj_rin[j], epj_rout[j]);
+                const co_t *c = co_pick(&ci, &cj);
+                const double kacc = 1.0 - co_acc0w(c, dr_eps);
+                const double dr2_max = (dr2_eps > r_out2) ? dr2_eps : r_out2;
+                const double drinv_max = 1.0 / sqrt(dr2_max);
+                const double gmor_max = G * epj_mass[j] * drinv_max;
+                const double drinv2_max = drinv_max * drinv_max;
+                const double gmor3_max = gmor_max * drinv2_max;
+                const double s = gmor3 * kacc - gmor3_max;
+                ax -= s * rx;
+                ay -= s * ry;
+                az -= s * rz;
+                const double kpot = 1.0 - co_potw(c, dr_eps);
+                const double status = epj_status[j], mbk = epj_mbk[j];
+                if (status == 0.0 && mbk == 0.0) {
+                    ps -= gmor * kpot - gmor_max;
+                    pt -= (gmor - gmor_max);
+                } else if (status < 0.0) {
+                    gmor = G * mbk * drinv;
+                    ps -= gmor * kpot - gmor_max;
+                    pt -= (gmor - gmor_max);
+                } else {
+                    ps += gmor_max;
+                    pt += gmor_max;
+                }
+            }
+            acc[3 * i + 0] = ax;
+            acc[3 * i + 1] = ay;
+            acc[3 * i + 2] = az;
+            pot_tot[i] = pt;
+            pot_soft[i] = ps;
+        }
+    }
+}

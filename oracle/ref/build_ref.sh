@@ -7,6 +7,8 @@
 #                      (RSQRT_NR_EPJ_X2, src/petar.hpp:1-15)
 #   libref_simd64.so   AVX-512 PhantomGrapeQuad64Bit  (P3T_64BIT: CALC_EP_64bit,
 #                      CALC_SP_64bit, RSQRT_NR_EPJ_X4, RSQRT_NR_SPJ_X4)
+#   libref_changeover.so  changeover W functions      (src/changeover.hpp; SDAR's
+#                      Common/Float.h replaced by oracle/ref/shim/Common/Float.h)
 # The SIMD kernels are x86 only; on other hosts only the NoSimd library is
 # built.  The NoSimd build uses -ffp-contract=off so its FP64 results are
 # defined by source order alone.
@@ -31,5 +33,7 @@ if [ "$(uname -m)" = "x86_64" ]; then
     "$CXX" "${SIMD[@]}" "${COMMON[@]}" -DREF_SIMD -DCALC_EP_64bit -DCALC_SP_64bit \
         -DRSQRT_NR_EPJ_X4 -DRSQRT_NR_SPJ_X4 "$HERE/ref_driver.cpp" -o "$OUT/libref_simd64.so" &
 fi
+"$CXX" -O2 -ffp-contract=off -std=c++17 -fPIC -shared -I"$HERE/shim" -I"$SRC" \
+    "$HERE/ref_changeover.cpp" -o "$OUT/libref_changeover.so" &
 wait
 ls "$OUT"

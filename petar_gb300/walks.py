@@ -189,3 +189,56 @@ def concat_batches(batches: list[WalkBatch]) -> WalkBatch:
         epi_index=np.concatenate([(b.epi_index if b.epi_index is not None else np.arange(b.epi_rs.size)) + o
                                   for b, o in zip(batches, i_off[:-1])]),
         meta={"n_cluster": len(batches)})
+
+
+@dataclass
+class ChangeoverSet:
+    """Per-particle changeover data for the fused changeover mode.
+
+    PeTar's changeover radii scale with mass as r * max((m / m_avg)^(1/3), 1)
+    (ChangeOver::setR, src/changeover.hpp:43-60); the artificial-particle
+    information is the (mass_backup, status) pair of
+    src/artificial_particles.hpp:15-90 (single: both 0; member: status < 0,
+    potential mass in mass_backup, soft mass 0; anything else: its potential
+    is removed from neighbours').  self_mass is the mass whose self-potential
+    G m / r_out the correction removes (src/hard.hpp:1663-1674), 0 for none."""
+    epi_id: np.ndarray
+    epi_r_in: np.ndarray
+    epi_r_out: np.ndarray
+    epi_self_mass: np.ndarray
+    epj_id: np.ndarray
+    epj_r_in: np.ndarray
+    epj_r_out: np.ndarray
+    epj_mass_backup: np.ndarray
+    epj_status: np.ndarray
+
+
+def make_changeover(batch: WalkBatch, r_in: float, r_out: float, member_fraction: float = 0.1,
+                    artificial_fraction: float = 0.05, seed: int = 0) -> tuple[WalkBatch, ChangeoverSet]:
+    """Changeover data for a single-cluster batch (EPI and EPJ rows are the
+    same particles, ``batch.epi_index``): mass-scaled radii, and a random share
+    of members (soft mass 0, mass in mass_backup) and artificial particles.
+    Returns the batch with the members' EPJ masses set to 0, and the set."""
+    assert batch.epi_index is not None and batch.epi_rs.size == batch.epj_mass.size
+    rng = np.random.default_rng(seed)
+    n = batch.epj_mass.size
+    ids = batch.epi_index.astype(np.int64)
+    m = batch.epj_mass.astype(np.float64)
+    m_fac = m / m.mean()
+    scale = np.maximum(np.power(m_fac, 1.0 / 3.0), 1.0)  # std::pow(m_fac, 1.0/3.0) as setR
+    u = rng.random(n)
+    member = u < member_fraction
+    artificial = (u >= member_fraction) & (u < member_fraction + artificial_fraction)
+    status = np.zeros(n)
+    status[member] = -1.0
+    status[artificial] = 1.0
+    mbk = np.zeros(n)
+    mbk[member] = m[member]
+    soft_m = np.where(member, 0.0, m)
+    self_mass = np.where(member | artificial, 0.0, m)
+    co = ChangeoverSet(epi_id=ids, epi_r_in=r_in * scale, epi_r_out=r_out * scale, epi_self_mass=self_mass,
+                       epj_id=ids.copy(), epj_r_in=r_in * scale, epj_r_out=r_out * scale,
+                       epj_mass_backup=mbk, epj_status=status)
+    out = WalkBatch(**{k: getattr(batch, k) for k in batch.__dataclass_fields__})
+    out.epj_mass = soft_m
+    return out, co

@@ -26,7 +26,14 @@ Outputs per case and reference variant (``nosimd``: FP64 NoSimd functors;
 ``simd32``: AVX-512 PhantomGrapeQuad; ``simd64``: AVX-512 PhantomGrapeQuad64Bit):
 EP-EP acc/pot/n_ngb and EP-SP acc/pot, G-scaled as the functors write them.
 
-Usage: python tests/golden/make_golden.py
+``changeover_w.npz``
+    The reference's changeover functions (src/changeover.hpp, compiled into
+    ``libref_changeover.so``): W_acc and W_pot of single changeovers and of
+    pairs (the larger r_out wins), and the mass-scaled radii of setR(m_fac,
+    r_in, r_out), on random radii with separations below r_in, inside the
+    changeover, beyond r_out and on both boundaries.
+
+Usage: python tests/golden/make_golden.py [fixture names]   (default: all)
 """
 from __future__ import annotations
 
@@ -126,10 +133,50 @@ def walks_of(case: dict) -> list[dict]:
     return out
 
 
+def changeover_case(seed: int) -> dict:
+    """Inputs and reference outputs of the changeover W functions."""
+    lib = ctypes.CDLL(str(REF_LIBS / "libref_changeover.so"))
+    vp, ci = ctypes.c_void_p, ctypes.c_int
+    lib.ref_co_w.argtypes = [ci] + [vp] * 5
+    lib.ref_co_w_two.argtypes = [ci] + [vp] * 7
+    lib.ref_co_setr_mfac.argtypes = [ci] + [vp] * 5
+    rng = np.random.default_rng(seed)
+    n = 6000
+    r_out = 10 ** rng.uniform(-4, -1, n)
+    r_in = r_out * rng.uniform(0.05, 0.5, n)
+    u = rng.uniform(-0.3, 1.3, n)
+    dr = r_in + u * (r_out - r_in)
+    dr[:200] = r_in[:200]
+    dr[200:400] = r_out[200:400]
+    dr[400:600] = rng.uniform(0, 1, 200) * r_in[400:600]
+    dr = np.abs(dr)
+    acc0w = np.zeros(n)
+    potw = np.zeros(n)
+    lib.ref_co_w(n, _p(r_in), _p(r_out), _p(dr), _p(acc0w), _p(potw))
+    r_out2 = r_out * rng.uniform(0.5, 2.0, n)
+    r_out2[:300] = r_out[:300]  # ties: the second changeover wins
+    r_in2 = r_out2 * rng.uniform(0.05, 0.5, n)
+    acc0w2 = np.zeros(n)
+    potw2 = np.zeros(n)
+    lib.ref_co_w_two(n, _p(r_in), _p(r_out), _p(r_in2), _p(r_out2), _p(dr), _p(acc0w2), _p(potw2))
+    m_fac = 10 ** rng.uniform(-2, 2.5, n)
+    rin_m = np.zeros(n)
+    rout_m = np.zeros(n)
+    lib.ref_co_setr_mfac(n, _p(m_fac), _p(r_in), _p(r_out), _p(rin_m), _p(rout_m))
+    return dict(r_in=r_in, r_out=r_out, dr=dr, acc0w=acc0w, potw=potw, r_in2=r_in2, r_out2=r_out2,
+                acc0w_two=acc0w2, potw_two=potw2, m_fac=m_fac, r_in_mfac=rin_m, r_out_mfac=rout_m)
+
+
 def main() -> None:
-    if not (REF_LIBS / "libref_nosimd.so").exists():
+    if not (REF_LIBS / "libref_nosimd.so").exists() or not (REF_LIBS / "libref_changeover.so").exists():
         subprocess.run([str(ROOT / "oracle" / "ref" / "build_ref.sh")], check=True)
     sys.path.insert(0, str(ROOT))
+    only = set(sys.argv[1:])
+    if not only or "changeover_w" in only:
+        np.savez_compressed(HERE / "changeover_w.npz", **changeover_case(77))
+        print("changeover_w")
+    if only and not only - {"changeover_w"}:
+        return
     cases = {
         "kernel_test": kernel_test_case(20240, rs_var=False),
         "kernel_test_rsvar": kernel_test_case(20241, rs_var=True),
@@ -137,6 +184,8 @@ def main() -> None:
     }
     libs = {v: _load(v) for v in VARIANTS if (REF_LIBS / f"libref_{v}.so").exists()}
     for name, case in cases.items():
+        if only and name not in only:
+            continue
         ws = walks_of(case)
         payload = dict(case)
         for v, lib in libs.items():

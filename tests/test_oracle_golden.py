@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import load_golden, rel_err, rel_err_vec
+from helpers import GOLDEN, load_golden, rel_err, rel_err_vec
 
 CASES = ["kernel_test", "kernel_test_rsvar", "plummer2048_walks"]
 
@@ -79,3 +79,66 @@ def test_oracle_total_is_sum_of_parts():
     o = oracle.force(wb, parts=True)
     np.testing.assert_array_equal(o["acc"], (0.0 + o["acc_ep"]) + o["acc_sp"])
     np.testing.assert_array_equal(o["pot"], (0.0 + o["pot_ep"]) + o["pot_sp"])
+
+
+def test_changeover_w_matches_reference():
+    """The oracle's changeover W functions against the reference's ChangeOver
+    (src/changeover.hpp) compiled from its source: bit-exact, single and pair
+    forms, including the tie rule of the pair form."""
+    d = dict(np.load(GOLDEN / "changeover_w.npz"))
+    a, p = oracle.co_w(d["r_in"], d["r_out"], d["dr"])
+    np.testing.assert_array_equal(a, d["acc0w"])
+    np.testing.assert_array_equal(p, d["potw"])
+    a2, p2 = oracle.co_w_two(d["r_in"], d["r_out"], d["r_in2"], d["r_out2"], d["dr"])
+    np.testing.assert_array_equal(a2, d["acc0w_two"])
+    np.testing.assert_array_equal(p2, d["potw_two"])
+
+
+def test_changeover_mass_scaling_matches_reference():
+    """make_changeover's radii follow ChangeOver::setR(m_fac, r_in, r_out)."""
+    d = dict(np.load(GOLDEN / "changeover_w.npz"))
+    scale = np.maximum(np.power(d["m_fac"], 1.0 / 3.0), 1.0)
+    np.testing.assert_allclose(d["r_in"] * scale, d["r_in_mfac"], rtol=4e-16, atol=0)
+    np.testing.assert_allclose(d["r_out"] * scale, d["r_out_mfac"], rtol=4e-16, atol=0)
+
+
+def test_changeover_oracle_composition():
+    """The oracle's correction sequence (linear-cutoff kernel, then the
+    reference's per-neighbour correction) against the composite it must equal,
+    evaluated directly: changeover force and potentials for neighbours,
+    linear cutoff for everything else, self-potential removed."""
+    from petar_gb300 import ics, walks
+    cl = ics.make_plummer_cluster(9, 1500, 0.03, binary_fraction=0.3)
+    wb, co = walks.make_changeover(walks.build_walks(cl), cl.r_in, cl.r_out, seed=3)
+    o = oracle.force_changeover(wb, co)
+    base = oracle.force(wb, parts=True)
+    G, r_out2 = wb.G, wb.rcut2
+    r_out = np.sqrt(r_out2)
+    for w in range(wb.n_walk):
+        for i in range(wb.epi_disp[w], wb.epi_disp[w + 1]):
+            js = wb.id_epj[wb.epj_disp[w]:wb.epj_disp[w + 1]]
+            dx = wb.epj_pos[js] - wb.epi_pos[i]
+            r2 = (dx * dx).sum(1) + wb.eps2
+            nb = (r2 < np.maximum(wb.epi_rs[i], wb.epj_rs[js]) ** 2) & (co.epj_id[js] != co.epi_id[i])
+            m = wb.epj_mass[js]
+            rmax = np.sqrt(np.maximum(r2, r_out2))
+            r = np.sqrt(r2)
+            pick_i = co.epi_r_out[i] > co.epj_r_out[js]
+            rin = np.where(pick_i, co.epi_r_in[i], co.epj_r_in[js])
+            rou = np.where(pick_i, co.epi_r_out[i], co.epj_r_out[js])
+            wa, wp = oracle.co_w(rin, rou, np.where(nb, r, 1.0))
+            single = (co.epj_status[js] == 0) & (co.epj_mass_backup[js] == 0)
+            member = co.epj_status[js] < 0
+            meff = np.where(single, m, np.where(member, co.epj_mass_backup[js], 0.0))
+            rr = np.where(nb, r, 1.0)
+            acc = np.where(nb[:, None], (m * (1 - wa) / rr ** 3)[:, None] * dx, (m / rmax ** 3)[:, None] * dx)
+            pt = np.where(nb, -meff / rr, -m / rmax)
+            ps = np.where(nb, -meff * (1 - wp) / rr, -m / rmax)
+            self_pot = co.epi_self_mass[i] / r_out
+            want_acc = G * acc.sum(0) + base["acc_sp"][i]
+            want_pt = G * (pt.sum() + self_pot) + base["pot_sp"][i]
+            want_ps = G * (ps.sum() + self_pot) + base["pot_sp"][i]
+            scale = np.abs(G * acc).sum(0).max() + abs(base["acc_sp"][i]).max()
+            assert np.abs(o["acc"][i] - want_acc).max() <= 1e-11 * scale
+            assert abs(o["pot"][i] - want_pt) <= 1e-11 * (G * np.abs(pt).sum() + abs(base["pot_sp"][i]) + G * self_pot)
+            assert abs(o["pot_soft"][i] - want_ps) <= 1e-11 * (G * np.abs(ps).sum() + abs(base["pot_sp"][i]) + G * self_pot)
