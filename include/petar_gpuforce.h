@@ -55,10 +55,44 @@ enum {
 /* What an index dispatch computes (pgf_set_mode). */
 enum {
     PGF_MODE_FORCE = 0,           /* soft force: acc, pot and n_ngb (default) */
-    PGF_MODE_NEIGHBOR_SEARCH = 1  /* n_ngb only, as SearchNeighborEpEpNoSimd
+    PGF_MODE_NEIGHBOR_SEARCH = 1, /* n_ngb only, as SearchNeighborEpEpNoSimd
                                      (src/soft_force.hpp:11-34): r^2 < max(rs_i, rs_j)^2
                                      without softening; SPJ lists are ignored */
+    PGF_MODE_FORCE_CHANGEOVER = 2 /* soft force with the changeover correction of
+                                     neighbours fused in (see pgf_set_changeover_layout) */
 };
+
+/* Fused changeover mode.  PeTar corrects the soft force on the CPU after the
+ * kernel: for every tree neighbour j of i, calcAccPotShortWithLinearCutoff
+ * (src/hard.hpp:1404-1480) replaces the linear-cutoff pair term by the
+ * changeover force G m_j (1 - W_acc(r)) / r^3 (W of the pair's larger
+ * r_out, src/changeover.hpp:294-334, 364-375) and splits the potential into
+ * pot_tot and pot_soft by j's artificial-particle status; the particle's own
+ * G m / r_out self-term is removed (src/hard.hpp:1663-1674).  In this mode
+ * the kernel evaluates the corrected result directly.  Neighbours are the
+ * pairs the neighbour count counts (|dx|^2 + eps^2 < max(rs_i, rs_j)^2, the
+ * tree search's test when eps = 0), the particle itself (same id) excluded.
+ * The caller's records carry the extra fields at these byte offsets: ids are
+ * 8-byte integers, everything else F64.  Set the layout before the send
+ * (send_flag) so that the EPJ changeover data is packed with the EPJ array;
+ * retrieve writes the total potential to pot and the soft one to pot_soft. */
+typedef struct pgf_changeover_layout {
+    size_t epi_off_id;          /* EPI: particle id */
+    size_t epi_off_r_in;        /* EPI: changeover r_in */
+    size_t epi_off_r_out;       /* EPI: changeover r_out */
+    size_t epi_off_self_mass;   /* EPI: mass of the self-potential term to remove (0: none) */
+    size_t epj_off_id;          /* EPJ: particle id */
+    size_t epj_off_r_in;        /* EPJ: changeover r_in (EPJSoft::r_in) */
+    size_t epj_off_r_out;       /* EPJ: changeover r_out (EPJSoft::r_out) */
+    size_t epj_off_mass_backup; /* EPJ: group_data.artificial mass_backup */
+    size_t epj_off_status;      /* EPJ: group_data.artificial status */
+    size_t force_off_pot_soft;  /* Force: F64 soft potential (written) */
+} pgf_changeover_layout;
+
+/* Sets (or with NULL clears) the changeover layout used by the send and by
+ * dispatches in PGF_MODE_FORCE_CHANGEOVER.  No counterpart in the reference,
+ * whose correction runs on the CPU. */
+int pgf_set_changeover_layout(const pgf_changeover_layout *layout);
 
 /* Record layouts (sizes and byte offsets). */
 typedef struct pgf_epi_layout {

@@ -173,3 +173,73 @@ inline PS::S32 RetrieveForceCUDA(const PS::S32 tag, const PS::S32 n_walk, const 
     check(pgf_retrieve(tag, n_walk, ni, reinterpret_cast<void* const*>(force), &fl), "pgf_retrieve");
     return 0;
 }
+
+// ---- Fused changeover mode (no counterpart in the reference, whose
+// correction runs on the CPU after the kernel, src/hard.hpp:1656-1693) ----
+//
+// Tepi is PeTar's EPISoft extended with the particle's changeover radii and
+// the mass of its self-potential term (members: fields id, pos, r_search,
+// r_in, r_out, self_mass); Tforce is ForceSoft extended with pot_soft.  The
+// EPJ side uses EPJSoft's own id, r_in, r_out and group_data, whose
+// artificial-particle information starts with (mass_backup, status)
+// (src/artificial_particles.hpp:20-23).  After retrieve, pot holds pot_tot
+// and pot_soft the soft potential; FPSoft takes them instead of copying pot
+// into both (src/soft_ptcl.hpp:84-95), and the CPU correction pass is skipped.
+namespace petar_gpuforce {
+template <class Tepi, class Tepj, class Tforce>
+inline pgf_changeover_layout changeover_layout() {
+    pgf_changeover_layout l;
+    l.epi_off_id = offsetof(Tepi, id);
+    l.epi_off_r_in = offsetof(Tepi, r_in);
+    l.epi_off_r_out = offsetof(Tepi, r_out);
+    l.epi_off_self_mass = offsetof(Tepi, self_mass);
+    l.epj_off_id = offsetof(Tepj, id);
+    l.epj_off_r_in = offsetof(Tepj, r_in);
+    l.epj_off_r_out = offsetof(Tepj, r_out);
+    l.epj_off_mass_backup = offsetof(Tepj, group_data);
+    l.epj_off_status = offsetof(Tepj, group_data) + sizeof(double);
+    l.force_off_pot_soft = offsetof(Tforce, pot_soft);
+    return l;
+}
+}  // namespace petar_gpuforce
+
+template <class Tepi, class Tforce>
+struct CalcForceWithLinearCutoffChangeoverCUDAMultiWalk {
+    PS::S32 my_rank;
+    PS::F64 eps2;
+    PS::F64 rcut2;
+    PS::F64 G;
+
+    CalcForceWithLinearCutoffChangeoverCUDAMultiWalk() {}
+    CalcForceWithLinearCutoffChangeoverCUDAMultiWalk(PS::S32 _rank, PS::F64 _eps2, PS::F64 _rcut2, PS::F64 _G)
+        : my_rank(_rank), eps2(_eps2), rcut2(_rcut2), G(_G) {}
+
+    PS::S32 operator()(const PS::S32 tag, const PS::S32 n_walk, const Tepi** epi, const PS::S32* n_epi,
+                       const PS::S32** id_epj, const PS::S32* n_epj, const PS::S32** id_spj, const PS::S32* n_spj,
+                       const EPJSoft* epj, const PS::S32 n_epj_tot, const SPJSoft* spj, const PS::S32 n_spj_tot,
+                       const bool send_flag) {
+        using namespace petar_gpuforce;
+        check(pgf_initialize(my_rank, eps2, rcut2, G), "pgf_initialize");
+        const pgf_changeover_layout col = changeover_layout<Tepi, EPJSoft, Tforce>();
+        check(pgf_set_changeover_layout(&col), "pgf_set_changeover_layout");
+        check(pgf_set_mode(PGF_MODE_FORCE_CHANGEOVER), "pgf_set_mode");
+        const pgf_epi_layout il = epi_layout<Tepi>();
+        const pgf_epj_layout jl = epj_layout<EPJSoft>();
+        const pgf_spj_layout sl = spj_layout<SPJSoft>();
+        check(pgf_dispatch_index(tag, n_walk, reinterpret_cast<const void* const*>(epi), n_epi, &il,
+                                 reinterpret_cast<const int* const*>(id_epj), n_epj,
+                                 reinterpret_cast<const int* const*>(id_spj), n_spj, epj, n_epj_tot, &jl, spj,
+                                 n_spj_tot, &sl, send_flag ? 1 : 0),
+              "pgf_dispatch_index");
+        return 0;
+    }
+};
+
+template <class Tforce>
+inline PS::S32 RetrieveForceChangeoverCUDA(const PS::S32 tag, const PS::S32 n_walk, const PS::S32* ni,
+                                           Tforce** force) {
+    using namespace petar_gpuforce;
+    const pgf_force_layout fl = force_layout<Tforce>();
+    check(pgf_retrieve(tag, n_walk, ni, reinterpret_cast<void* const*>(force), &fl), "pgf_retrieve");
+    return 0;
+}

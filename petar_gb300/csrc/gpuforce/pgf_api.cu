@@ -119,6 +119,10 @@ struct TagState {
     HostBuf<Accp> h_accp;
     HostBuf<int32_t> h_nnb;
     HostBuf<int32_t> h_flags;  // queue head, n_retest, err, re-tested records
+    DevBuf<CoRec> epi_co;      // fused changeover mode
+    HostBuf<CoRec> h_epi_co;
+    DevBuf<double> pot_soft;
+    HostBuf<double> h_pot_soft;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     // Pipelined dispatch, per stage: copy start/end, main kernel start/end,
     // stage done (after the re-test kernel).
@@ -149,6 +153,11 @@ struct State {
     DevBuf<SpjQ64> spj_q64;
     DevBuf<EpjF32> epj32;  // (hi, lo) FP32 copies built on the device
     DevBuf<SpjF32> spj32;
+    bool co_set = false;   // changeover layout given (pgf_set_changeover_layout)
+    pgf_changeover_layout co{};
+    bool j_co_sent = false;  // the last send packed the EPJ changeover records
+    DevBuf<CoRec> epj_co;
+    HostBuf<CoRec> h_epj_co;
     HostBuf<EpjMix> h_epj;
     HostBuf<double> h_epj_m64, h_epj_rs64;
     HostBuf<SpjMix> h_spj;
@@ -220,6 +229,28 @@ inline const double* dptr(const void* base, size_t off) {
     return reinterpret_cast<const double*>(reinterpret_cast<const char*>(base) + off);
 }
 
+inline int64_t i64at(const char* r, size_t off) {
+    int64_t v;
+    std::memcpy(&v, r + off, sizeof(v));
+    return v;
+}
+
+// Changeover record of one particle: the derived ChangeOver members of
+// src/changeover.hpp:64-75 in FP64, rounded to FP32.
+inline CoRec make_co(double r_in, double r_out, double mass, int64_t id) {
+    CoRec c;
+    const double norm = 1.0 / (r_out - r_in);
+    const double coff = (r_out - r_in) / (r_out + r_in);
+    c.r_in = (float)r_in;
+    c.r_out = (float)r_out;
+    c.norm = (float)norm;
+    c.coff = (float)coff;
+    c.pot_off = (float)((1.0 + coff) / r_out);
+    c.mass = (float)mass;
+    c.id = id;
+    return c;
+}
+
 // Adds the time of the last j send to the profile once its copies are done.
 void harvest_send(bool wait = false) {
     if (!g.send_pending) return;
@@ -256,6 +287,21 @@ int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, co
     PGF_CUDA(g.spj_q64.ensure(n_spj));
     PGF_CUDA(g.epj32.ensure(n_epj));
     PGF_CUDA(g.spj32.ensure(n_spj));
+    g.j_co_sent = false;
+    if (g.co_set && n_epj > 0) {
+        PGF_CUDA(g.h_epj_co.ensure(n_epj));
+        PGF_CUDA(g.epj_co.ensure(n_epj));
+        const pgf_changeover_layout& L = g.co;
+#pragma omp parallel for schedule(static)
+        for (int64_t j = 0; j < n_epj; ++j) {
+            const char* r = reinterpret_cast<const char*>(epj) + j * el->size;
+            const double status = *dptr(r, L.epj_off_status), mbk = *dptr(r, L.epj_off_mass_backup);
+            // Mass of the pair potential of a neighbour (src/hard.hpp:1458-1476):
+            // singles their mass, members their backup mass, others none.
+            const double m_pot = (status == 0.0 && mbk == 0.0) ? *dptr(r, el->off_mass) : (status < 0.0 ? mbk : 0.0);
+            g.h_epj_co.h[j] = make_co(*dptr(r, L.epj_off_r_in), *dptr(r, L.epj_off_r_out), m_pot, i64at(r, L.epj_off_id));
+        }
+    }
 #pragma omp parallel for schedule(static)
     for (int64_t j = 0; j < n_epj; ++j) {
         const char* r = reinterpret_cast<const char*>(epj) + j * el->size;
@@ -313,6 +359,10 @@ int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, co
         PGF_CUDA(cudaMemcpyAsync(g.spj_q64.d, g.h_spj_q64.h, n_spj * sizeof(SpjQ64), cudaMemcpyHostToDevice,
                                  g.stream));
     }
+    if (g.co_set && n_epj > 0) {
+        PGF_CUDA(cudaMemcpyAsync(g.epj_co.d, g.h_epj_co.h, n_epj * sizeof(CoRec), cudaMemcpyHostToDevice, g.stream));
+        g.j_co_sent = true;
+    }
     {
         const cudaError_t e = launch_split_j(g.epj.d, n_epj, g.epj32.d, g.spj.d, n_spj, g.spj32.d, g.stream);
         if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "j split kernel failed: %s", cudaGetErrorString(e));
@@ -352,7 +402,11 @@ void bind_scratch(Params& p, int stage = -1, int n_stages = 1) {
 int launch_kernels(const TagState& t, const Params& p, cudaStream_t s, cudaEvent_t ev_start, cudaEvent_t ev_end) {
     PGF_CUDA(cudaEventRecord(ev_start, s));
     cudaError_t e;
-    if (t.mode == PGF_MODE_NEIGHBOR_SEARCH) {
+    if (t.mode == PGF_MODE_FORCE_CHANGEOVER) {
+        e = launch_ws_changeover(p, s, g.num_sms);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_end, s);
+        if (e == cudaSuccess && p.n_walk > 0) e = launch_retest(p, s, g.num_sms);
+    } else if (t.mode == PGF_MODE_NEIGHBOR_SEARCH) {
         e = launch_ws_search(p, s, g.num_sms);
         if (e == cudaSuccess) e = cudaEventRecord(ev_end, s);
         if (e == cudaSuccess && p.n_walk > 0) e = launch_retest(p, s, g.num_sms);
@@ -428,6 +482,11 @@ bool pack_walk(TagState& t, int k, int w, const Slot3& o, const void* const* epi
         const double* p = dptr(r, il->off_pos);
         EpiDev e{p[0], p[1], p[2], *dptr(r, il->off_r_search)};
         t.h_epi.h[o.i + i] = e;
+        if (t.mode == PGF_MODE_FORCE_CHANGEOVER) {
+            const pgf_changeover_layout& L = g.co;
+            t.h_epi_co.h[o.i + i] = make_co(*dptr(r, L.epi_off_r_in), *dptr(r, L.epi_off_r_out),
+                                            *dptr(r, L.epi_off_self_mass), i64at(r, L.epi_off_id));
+        }
         rs_max = std::max(rs_max, e.rs);
         for (int d = 0; d < 3; ++d) {
             lo[d] = std::min(lo[d], p[d]);
@@ -524,6 +583,16 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     const int64_t ni = off[n_walk].i, ne = off[n_walk].e, ns = off[n_walk].s;
     if (ni > kMaxRows) return fail(PGF_ERR_CAPACITY, "%lld i-particles exceed 2^31-1", (long long)ni);
     if (ne > 0 && !g.j_sent) return fail(PGF_ERR_STATE, "EPJ ids given before the EPJ array was sent");
+    const bool co_mode = g.mode == PGF_MODE_FORCE_CHANGEOVER;
+    if (co_mode && !g.co_set) return fail(PGF_ERR_STATE, "changeover mode without pgf_set_changeover_layout");
+    if (co_mode && ne > 0 && !g.j_co_sent)
+        return fail(PGF_ERR_STATE, "changeover mode: the EPJ array was sent before the changeover layout was set");
+    t.mode = g.mode;
+    if (co_mode) {
+        PGF_CUDA(t.h_epi_co.ensure(ni));
+        PGF_CUDA(t.epi_co.ensure(ni));
+        PGF_CUDA(t.pot_soft.ensure(ni));
+    }
     PGF_CUDA(t.h_epi.ensure(ni));
     PGF_CUDA(t.h_id_epj.ensure(ne));
     PGF_CUDA(t.h_id_spj.ensure(ns));
@@ -554,7 +623,6 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     t.n_epi.assign(n_epi, n_epi + n_walk);
     t.precision = g.precision;
     t.variant = g.variant;
-    t.mode = g.mode;
     Params& p = t.params;
     p = Params{};
     p.epi = t.epi.d;
@@ -565,6 +633,11 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     p.spj_q64 = g.spj_q64.d;
     p.epj32 = g.epj32.d;
     p.spj32 = g.spj32.d;
+    if (co_mode) {
+        p.epj_co = g.epj_co.d;
+        p.epi_co = t.epi_co.d;
+        p.out_pot_soft = t.pot_soft.d;
+    }
     p.id_epj = t.id_epj.d;
     p.id_spj = t.id_spj.d;
     p.walks = t.walks.d;
@@ -596,6 +669,9 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
         const Slot3 a = off[k0], b = off[k1];
         if (b.i > a.i)
             PGF_CUDA(cudaMemcpyAsync(t.epi.d + a.i, t.h_epi.h + a.i, (b.i - a.i) * sizeof(EpiDev),
+                                     cudaMemcpyHostToDevice, s));
+        if (b.i > a.i && co_mode)
+            PGF_CUDA(cudaMemcpyAsync(t.epi_co.d + a.i, t.h_epi_co.h + a.i, (b.i - a.i) * sizeof(CoRec),
                                      cudaMemcpyHostToDevice, s));
         if (b.e > a.e)
             PGF_CUDA(cudaMemcpyAsync(t.id_epj.d + a.e, t.h_id_epj.h + a.e, (b.e - a.e) * sizeof(int32_t),
@@ -806,8 +882,19 @@ int pgf_set_kernel_variant(int variant) {
 }
 
 int pgf_set_mode(int mode) {
-    if (mode != PGF_MODE_FORCE && mode != PGF_MODE_NEIGHBOR_SEARCH) return fail(PGF_ERR_ARG, "unknown mode %d", mode);
+    if (mode != PGF_MODE_FORCE && mode != PGF_MODE_NEIGHBOR_SEARCH && mode != PGF_MODE_FORCE_CHANGEOVER)
+        return fail(PGF_ERR_ARG, "unknown mode %d", mode);
     g.mode = mode;
+    return PGF_OK;
+}
+
+int pgf_set_changeover_layout(const pgf_changeover_layout* layout) {
+    if (!layout) {
+        g.co_set = false;
+        return PGF_OK;
+    }
+    g.co = *layout;
+    g.co_set = true;
     return PGF_OK;
 }
 
@@ -881,6 +968,10 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
     if (n) {
         PGF_CUDA(cudaMemcpyAsync(t.h_accp.h, t.accp.d, n * sizeof(Accp), cudaMemcpyDeviceToHost, s));
         PGF_CUDA(cudaMemcpyAsync(t.h_nnb.h, t.nnb.d, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        if (t.mode == PGF_MODE_FORCE_CHANGEOVER) {
+            PGF_CUDA(t.h_pot_soft.ensure(n));
+            PGF_CUDA(cudaMemcpyAsync(t.h_pot_soft.h, t.pot_soft.d, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
     }
     PGF_CUDA(cudaMemcpyAsync(t.h_flags.h, g.scratch.d, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     PGF_CUDA(cudaMemsetAsync(g.scratch.d + 2, 0, 2 * sizeof(int32_t), s));
@@ -901,13 +992,15 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
         const int64_t o = t.epi_disp[w];
         for (int i = 0; i < ni[w]; ++i) {
             char* r = base + (size_t)i * fl->size;
-            if (t.mode == PGF_MODE_FORCE) {
+            if (t.mode != PGF_MODE_NEIGHBOR_SEARCH) {
                 const Accp a = t.h_accp.h[o + i];
                 double* acc = reinterpret_cast<double*>(r + fl->off_acc);
                 acc[0] = a.x;
                 acc[1] = a.y;
                 acc[2] = a.z;
                 *reinterpret_cast<double*>(r + fl->off_pot) = a.w;
+                if (t.mode == PGF_MODE_FORCE_CHANGEOVER)
+                    *reinterpret_cast<double*>(r + g.co.force_off_pot_soft) = t.h_pot_soft.h[o + i];
             }
             if (fl->n_ngb_bytes == 8)
                 *reinterpret_cast<int64_t*>(r + fl->off_n_ngb) = t.h_nnb.h[o + i];
@@ -968,6 +1061,10 @@ int pgf_finalize(void) {
         t.h_accp.release();
         t.h_nnb.release();
         t.h_flags.release();
+        t.epi_co.release();
+        t.h_epi_co.release();
+        t.pot_soft.release();
+        t.h_pot_soft.release();
         for (auto& ev : t.ev) {
             if (ev) cudaEventDestroy(ev);
             ev = nullptr;
@@ -987,6 +1084,9 @@ int pgf_finalize(void) {
     g.spj_q64.release();
     g.epj32.release();
     g.spj32.release();
+    g.epj_co.release();
+    g.h_epj_co.release();
+    g.j_co_sent = false;
     g.h_epj.release();
     g.h_epj_m64.release();
     g.h_epj_rs64.release();

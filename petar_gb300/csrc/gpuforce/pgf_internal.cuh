@@ -62,6 +62,19 @@ struct __align__(32) SpjF32 {
 };
 static_assert(sizeof(SpjF32) == 64, "SpjF32 layout");
 
+// Changeover data of one particle for the fused changeover mode: the
+// ChangeOver members of src/changeover.hpp:8-14 (r_in, r_out, norm =
+// 1/(r_out - r_in), coff = (r_out - r_in)/(r_out + r_in), pot_off =
+// (1 + coff)/r_out), computed in FP64 and rounded; the particle id; and a mass:
+// for EPJ the mass its neighbours' potentials use (m for singles, mass_backup
+// for members, 0 otherwise), for EPI the mass of its self-potential term.
+struct __align__(32) CoRec {
+    float r_in, r_out, norm, coff;
+    float pot_off, mass;
+    int64_t id;
+};
+static_assert(sizeof(CoRec) == 32, "CoRec layout");
+
 struct __align__(16) SpjQ64 {
     double m;
     double q[6];  // raw second moment: xx, yy, zz, xy, xz, yz (zero for monopoles)
@@ -101,6 +114,8 @@ struct Retest {
     int64_t j_begin;  // offset in id_epj
     int32_t i;        // EPI row
     int32_t n;        // number of list entries
+    int32_t walk;     // walk (descriptor index) of the i-particle
+    int32_t pad;
 };
 
 struct Params {
@@ -112,6 +127,9 @@ struct Params {
     const SpjQ64* spj_q64;
     const EpjF32* epj32;
     const SpjF32* spj32;
+    const CoRec* epj_co;   // fused changeover mode only (else null)
+    const CoRec* epi_co;
+    double* out_pot_soft;  // fused changeover mode: soft potential (G applied)
     const int32_t* id_epj;
     const int32_t* id_spj;
     const WalkDesc* walks;
@@ -145,6 +163,37 @@ __device__ __forceinline__ int exact_neighbour(double xi, double yi, double zi, 
     return __dadd_rn(r2, eps2) < __dmul_rn(rs, rs) ? 1 : 0;
 }
 
+// FP64 difference between the changeover pair terms and the linear-cutoff
+// pair terms of one neighbour pair (the fused mode's correction for pairs
+// whose neighbour status only the FP64 re-test decides): acceleration x, y,
+// z, pot_tot and pot_soft, without G.  Same formulas as the FP32 pair path.
+__device__ __forceinline__ void co_pair_diff(const EpiDev& ei, const CoRec& ci, const EpjMix& ej, float mj, const CoRec& cj,
+                                    double eps2, double rcut2, double out[5]) {
+    const double dx = ej.x - ei.x, dy = ej.y - ei.y, dz = ej.z - ei.z;
+    const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+    const double r = sqrt(r2), ri = 1.0 / r;
+    const double rimax = 1.0 / sqrt(r2 > rcut2 ? r2 : rcut2);
+    const CoRec& c = ci.r_out > cj.r_out ? ci : cj;
+    const double x = (r - (double)c.r_in) * (double)c.norm;
+    const double xa = x < 0.0 ? 0.0 : (x > 1.0 ? 1.0 : x);
+    const double x_1 = xa - 1.0, x_2 = x_1 * x_1, xa2 = xa * xa;
+    const double wacc = (x_2 * x_2) * (1.0 + 4.0 * xa + 10.0 * xa2 + 20.0 * xa2 * xa + 35.0 * (double)c.coff * xa2 * xa2);
+    double wpot = 1.0;
+    if (x >= 1.0) {
+        wpot = (double)c.pot_off * r;
+    } else if (x > 0.0) {
+        const double x2 = x * x, x3 = x2 * x;
+        wpot = 1.0 - (double)c.coff * (x2 * x3) * (5.0 * x3 - 20.0 * x2 + 28.0 * x - 14.0);
+    }
+    const double f = (double)mj * ((1.0 - wacc) * ri * ri * ri - rimax * rimax * rimax);
+    out[0] = f * dx;
+    out[1] = f * dy;
+    out[2] = f * dz;
+    const double meff = (double)cj.mass;
+    out[3] = -meff * ri + (double)mj * rimax;
+    out[4] = -meff * (1.0 - wpot) * ri + (double)mj * rimax;
+}
+
 // Launchers (stream-ordered, asynchronous).
 cudaError_t launch_fp64(const Params& p, cudaStream_t s, int num_sms);
 cudaError_t launch_mixed(const Params& p, cudaStream_t s, int num_sms);
@@ -157,5 +206,7 @@ constexpr int kNumWsVariants = 8;
 cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant);
 // Neighbour search (counts only, SPJ lists ignored) with the warp-specialised kernel.
 cudaError_t launch_ws_search(const Params& p, cudaStream_t s, int num_sms);
+// Soft force with the changeover correction of neighbours fused in.
+cudaError_t launch_ws_changeover(const Params& p, cudaStream_t s, int num_sms);
 
 }  // namespace pgf

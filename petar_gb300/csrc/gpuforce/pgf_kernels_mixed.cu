@@ -182,7 +182,8 @@ __global__ __launch_bounds__(kThreads, PGF_MINB) void mixed_kernel(Params p) {
         __syncthreads();
         const int wq = s.w;
         if (wq >= p.n_walk) break;
-        const WalkDesc wd = p.walks[p.order[wq]];
+        const int widx = p.order[wq];
+        const WalkDesc wd = p.walks[widx];
         const double cx = wd.cx, cy = wd.cy, cz = wd.cz;
         const float rcut2 = (float)wd.rcut2;
         const float rsmax2 = wd.rs_max * wd.rs_max;
@@ -468,6 +469,8 @@ __global__ __launch_bounds__(kThreads, PGF_MINB) void mixed_kernel(Params p) {
                                 rr.j_begin = rt.base;
                                 rr.i = gi[k];
                                 rr.n = rt.nt;
+                                rr.walk = widx;
+                                rr.pad = 0;
                                 p.retest[slot_r] = rr;
                             } else {
                                 cnt[k] += exact_count(p, gi[k], rt.base, rt.nt);
@@ -529,7 +532,22 @@ __global__ __launch_bounds__(256) void retest_kernel(Params p) {
         for (int k = lane; k < rec.n; k += 32) {
             const int id = p.id_epj[rec.j_begin + k];
             const EpjMix e = p.epj[id];
-            c += exact_neighbour(ei.x, ei.y, ei.z, ei.rs, e.x, e.y, e.z, p.epj_rs64[id], p.eps2);
+            const int nb = exact_neighbour(ei.x, ei.y, ei.z, ei.rs, e.x, e.y, e.z, p.epj_rs64[id], p.eps2);
+            c += nb;
+            if (p.epi_co && nb) {
+                // Fused changeover mode: the interaction kernel used the linear
+                // cutoff for this pair; replace it by the changeover terms.
+                const CoRec ci = p.epi_co[rec.i], cj = p.epj_co[id];
+                if (ci.id != cj.id) {
+                    double d[5];
+                    co_pair_diff(ei, ci, e, e.m, cj, p.eps2, p.walks[rec.walk].rcut2, d);
+                    atomicAdd(&p.out_accp[rec.i].x, p.G * d[0]);
+                    atomicAdd(&p.out_accp[rec.i].y, p.G * d[1]);
+                    atomicAdd(&p.out_accp[rec.i].z, p.G * d[2]);
+                    atomicAdd(&p.out_accp[rec.i].w, p.G * d[3]);
+                    atomicAdd(&p.out_pot_soft[rec.i], p.G * d[4]);
+                }
+            }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);

@@ -172,6 +172,39 @@ union Slot<true, TE> {
     SlotEPx2<TE> ep;
     SlotSPx2<TE> sp;
 };
+// Changeover mode: the EP slot also carries each near entry's changeover record.
+template <int TE>
+struct SlotEPco {
+    float4 nh[TE];
+    float4 nl[TE];
+    float4 fr[TE];
+    int nidx[TE];
+    CoRec nco[TE];
+};
+template <int TE>
+union SlotCo {
+    SlotEPco<TE> ep;
+    SlotSP<TE> sp;
+};
+// What a kernel computes: soft force, neighbour search, or soft force with the
+// changeover correction of neighbours fused in (scalar arithmetic only).
+enum : int { kModeForce = 0, kModeSearch = 1, kModeChangeover = 2 };
+template <bool PK, int TE, int MD>
+struct SlotSel {
+    using type = Slot<PK, TE>;
+};
+template <int TE>
+struct SlotSel<false, TE, kModeChangeover> {
+    using type = SlotCo<TE>;
+};
+template <int KI, int CT, bool CO>
+struct CoExtra {};
+template <int KI, int CT>
+struct CoExtra<KI, CT, true> {
+    float2 dtot[KI][CT];   // (hi, lo) flushed neighbour-pair partials of pot_tot
+    float2 dsoft[KI][CT];  // the same for pot_soft
+    CoRec coi[KI][CT];     // changeover record of each i
+};
 constexpr float kDummyPos = 1e15f;
 struct Hdr {
     int kind;
@@ -183,9 +216,9 @@ struct Hdr {
     int64_t base;  // first list entry of the tile
 };
 
-template <int CW, int KI, bool PK, int TE, int NS>
+template <int CW, int KI, bool PK, int TE, int NS, int MD>
 struct Smem {
-    Slot<PK, TE> slot[NS];
+    typename SlotSel<PK, TE, MD>::type slot[NS];
     Hdr hdr[NS];
     uint64_t full[NS];
     uint64_t empty[NS];
@@ -193,14 +226,44 @@ struct Smem {
     int cnt[KI][CW * 32];        // neighbour counts
     float4 nlo[KI][CW * 32];     // near-pair data of each i: lo x, y, z and r_search^2
     int nkb[KI][CW * 32];        // guard band of each i (ulps)
+    CoExtra<KI, CW * 32, MD == kModeChangeover> co;
 };
+
+// k_acc = 1 - W_acc and k_pot = 1 - W_pot of the changeover functions
+// (src/changeover.hpp:294-334) in FP32.  W_acc is within an ulp of 1 for x
+// near 0 (r near r_in), so 1 - W_acc is not formed by subtraction: with
+// y = 1 - x, the identity (1-x)^4 (1 + 4x + 10x^2 + 20x^3)
+// = 1 - x^4 (1 + 4y + 10y^2 + 20y^3) gives
+// 1 - W_acc = x^4 (1 + 4y + 10y^2 + 20y^3 - 35 coff y^4), accurate to a few
+// ulps of itself.  1 - W_pot is coff x^5 (5x^3 - 20x^2 + 28x - 14) inside the
+// changeover, 0 below r_in and 1 - pot_off r beyond r_out.
+__device__ __forceinline__ void co_k_f32(float r, float r_in, float norm, float coff, float pot_off, float& kacc,
+                                         float& kpot) {
+    const float x = (r - r_in) * norm;
+    const float xa = fminf(fmaxf(x, 0.f), 1.f);
+    const float y = 1.f - xa;
+    const float xa2 = xa * xa;
+    const float y2 = y * y;
+    kacc = (xa2 * xa2) * (1.f + 4.f * y + 10.f * y2 + 20.f * (y2 * y) - 35.f * coff * (y2 * y2));
+    if (x >= 1.f) {
+        kpot = 1.f - pot_off * r;
+    } else if (x > 0.f) {
+        const float x2 = x * x;
+        const float x3 = x2 * x;
+        kpot = coff * (x2 * x3) * (5.f * x3 - 20.f * x2 + 28.f * x - 14.f);
+    } else {
+        kpot = 0.f;
+    }
+}
 
 // ---------------------------------------------------------------- producer
 
 // SR (neighbour search): EPJ tiles only, near entries only; far entries can
 // hold no neighbour and SPJ lists are skipped.
-template <int CW, int KI, bool PK, bool SR, int TE, int NS>
-__device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int lane) {
+template <int CW, int KI, bool PK, int MD, int TE, int NS>
+__device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int lane) {
+    constexpr bool SR = MD == kModeSearch, CO = MD == kModeChangeover;
+    static_assert(!(CO && PK), "the changeover mode runs scalar tiles");
     constexpr int kMaxPass = CW * 32 * KI;
     constexpr int kTileEP = TE, kTileSP = TE / 2, kSlots = NS;
     constexpr int QE = TE / 32, QS = TE / 64;  // EPJ and SPJ entries per lane and tile
@@ -316,6 +379,7 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int lane)
                         S.nh[pos] = make_float4(hx, hy, hz, m);
                         S.nl[pos] = make_float4(lx, ly, lz, rs2);
                         S.nidx[pos] = e;
+                        if constexpr (CO) S.nco[pos] = p.epj_co[id[q]];
                     } else if (valid && !SR) {
                         const int pos = nf + __popc(bf & lt);
                         if constexpr (PK) {
@@ -442,8 +506,9 @@ __device__ __forceinline__ float pass_cost(int nip, int ku, int ct_threads) {
 // coordinates and the pair accumulators.  The near-only data of each i (lo
 // coordinates, r_search^2, guard band) and the neighbour counts live in
 // shared memory and are read once per tile that has near entries.
-template <int CW, int KI, bool PK, bool SR, int TE, int NS>
-__device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int ct) {
+template <int CW, int KI, bool PK, int MD, int TE, int NS>
+__device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int ct) {
+    constexpr bool SR = MD == kModeSearch, CO = MD == kModeChangeover;
     constexpr int kSlots = NS;
     constexpr int CT = CW * 32;
     constexpr int kMaxPass = CT * KI;
@@ -464,7 +529,14 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int ct) {
     float a[PK ? 1 : KI][4];
     float2 nx2[PK ? KI : 1], ny2[PK ? KI : 1], nz2[PK ? KI : 1];
     float2 b[PK ? KI : 1][4];
+    // Changeover: pot_tot and pot_soft partials of neighbour pairs (all other
+    // pairs add the same term to both, in a[k][3]).
+    float dt[CO ? KI : 1], ds[CO ? KI : 1];
+    double r_out_walk = 0.0, rcut2d = 0.0;
+    int walk_cur = 0;
     int since = 0;
+#pragma unroll
+    for (int k = 0; k < (CO ? KI : 1); ++k) dt[k] = ds[k] = 0.f;
 #pragma unroll
     for (int k = 0; k < (PK ? 1 : KI); ++k) {
         xih[k] = yih[k] = zih[k] = 0.f;
@@ -508,6 +580,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int ct) {
 #pragma unroll
                 for (int q = 0; q < 4; ++q) a[k][q] = 0.f;
             }
+            if constexpr (CO) dt[k] = ds[k] = 0.f;
         }
     };
 
@@ -530,6 +603,17 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int ct) {
                 v.y += e;
                 s.acc[k][q][ct] = v;
             }
+            if constexpr (CO) {
+                float2 v = s.co.dtot[k][ct];
+                float e;
+                two_sum(v.x, dt[k], v.x, e);
+                v.y += e;
+                s.co.dtot[k][ct] = v;
+                v = s.co.dsoft[k][ct];
+                two_sum(v.x, ds[k], v.x, e);
+                v.y += e;
+                s.co.dsoft[k][ct] = v;
+            }
         }
         clear_acc();
         since = 0;
@@ -542,13 +626,31 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int ct) {
             rr.j_begin = jidx;
             rr.i = gi;
             rr.n = 1;
+            rr.walk = CO ? walk_cur : 0;  // only the changeover re-test reads it
+            rr.pad = 0;
             p.retest[r] = rr;
             return 0;
         }
         const EpiDev ei = p.epi[gi];
         const int id = p.id_epj[jidx];
         const EpjMix e = p.epj[id];
-        return exact_neighbour(ei.x, ei.y, ei.z, ei.rs, e.x, e.y, e.z, p.epj_rs64[id], p.eps2);
+        const int nb = exact_neighbour(ei.x, ei.y, ei.z, ei.rs, e.x, e.y, e.z, p.epj_rs64[id], p.eps2);
+        if constexpr (CO) {
+            // Capacity overflow: apply the changeover difference here.
+            const CoRec ci = p.epi_co[gi], cj = p.epj_co[id];
+            if (nb && ci.id != cj.id) {
+                double d[5];
+                co_pair_diff(ei, ci, e, e.m, cj, p.eps2, rcut2d, d);
+                if constexpr (!PK) {
+                    a[k][0] += (float)d[0];
+                    a[k][1] += (float)d[1];
+                    a[k][2] += (float)d[2];
+                }
+                dt[k] += (float)d[3];
+                ds[k] += (float)d[4];
+            }
+        }
+        return nb;
     };
 
     // One EPJ tile with KU i-particles per thread.
@@ -562,13 +664,16 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int ct) {
             float4 lo[KU];
             int kb[KU], c[KU];
             bool vk[KU];
+            CoRec ci[CO ? KU : 1];
 #pragma unroll
             for (int k = 0; k < KU; ++k) {
                 lo[k] = s.nlo[k][ct];
                 kb[k] = s.nkb[k][ct];
                 c[k] = 0;
                 vk[k] = slot + k * S < nip;
+                if constexpr (CO) ci[k] = s.co.coi[k][ct];
             }
+            (void)ci;
 #pragma unroll 1
             for (int j = j0; j < j1; ++j) {
                 const float4 hh = T.nh[j];
@@ -585,7 +690,30 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int ct) {
                     const int e = __float_as_int(r2) - __float_as_int(rs2) + kb[k];
                     c[k] += (int)((unsigned)e >> 31);
                     if ((unsigned)e < (unsigned)(2 * kb[k]) && vk[k]) c[k] += push_retest(k, h.base + T.nidx[j]);
-                    if constexpr (!SR) {
+                    if constexpr (CO) {
+                        const CoRec& cj = T.nco[j];
+                        if ((e < 0) && cj.id != ci[k].id) {
+                            // neighbour: changeover force and potentials (src/hard.hpp:1404-1480
+                            // composed with the linear-cutoff kernel term it replaces)
+                            const float ri = rsqrt_approx(r2);
+                            const float r = r2 * ri;
+                            const bool use_i = ci[k].r_out > cj.r_out;
+                            float kacc, kpot;
+                            co_k_f32(r, use_i ? ci[k].r_in : cj.r_in, use_i ? ci[k].norm : cj.norm,
+                                     use_i ? ci[k].coff : cj.coff, use_i ? ci[k].pot_off : cj.pot_off, kacc, kpot);
+                            const float f = hh.w * kacc * (ri * ri * ri);
+                            a[k][0] = fmaf(f, dx, a[k][0]);
+                            a[k][1] = fmaf(f, dy, a[k][1]);
+                            a[k][2] = fmaf(f, dz, a[k][2]);
+                            const float meri = cj.mass * ri;
+                            dt[k] -= meri;
+                            ds[k] = fmaf(-meri, kpot, ds[k]);
+                        } else {
+                            const float ri = rsqrt_approx(fmaxf(r2, rcut2));
+                            const float mri = hh.w * ri;
+                            acc4(k, mri * (ri * ri), dx, dy, dz, mri);
+                        }
+                    } else if constexpr (!SR) {
                         const float ri = rsqrt_approx(fmaxf(r2, rcut2));
                         const float mri = hh.w * ri;
                         acc4(k, mri * (ri * ri), dx, dy, dz, mri);
@@ -764,6 +892,11 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int ct) {
             slot = ct - js * S;
             active = js < n_js;
             gbase = wd.i_begin + h.ipass + slot;
+            if constexpr (CO) {
+                r_out_walk = sqrt(wd.rcut2);
+                rcut2d = wd.rcut2;
+                walk_cur = h.walk;
+            }
 #pragma unroll
             for (int k = 0; k < KI; ++k) {
                 const bool valid = active && k < ku && slot + k * S < nip;
@@ -791,6 +924,14 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int ct) {
                 }
                 s.nlo[k][ct] = lo;
                 s.nkb[k][ct] = kb;
+                if constexpr (CO) {
+                    CoRec cr{};
+                    cr.id = -1;
+                    if (valid) cr = p.epi_co[gbase + k * S];
+                    s.co.coi[k][ct] = cr;
+                    s.co.dtot[k][ct] = make_float2(0.f, 0.f);
+                    s.co.dsoft[k][ct] = make_float2(0.f, 0.f);
+                }
                 s.cnt[k][ct] = 0;
 #pragma unroll
                 for (int q = 0; q < 4; ++q) s.acc[k][q][ct] = make_float2(0.f, 0.f);
@@ -821,7 +962,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int ct) {
 #pragma unroll
                 for (int k = 0; k < KI; ++k) {
                     if (!(k < ku && slot + k * S < nip)) continue;
-                    double r[4] = {0.0, 0.0, 0.0, 0.0};
+                    double r[4] = {0.0, 0.0, 0.0, 0.0}, rt = 0.0, rs = 0.0;
                     int n = 0;
                     for (int q = 0; q < n_js; ++q) {
                         const int src = q * S + slot;
@@ -830,10 +971,22 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int ct) {
                             const float2 v = s.acc[k][c][src];
                             r[c] += (double)v.x + (double)v.y;
                         }
+                        if constexpr (CO) {
+                            const float2 v = s.co.dtot[k][src], w = s.co.dsoft[k][src];
+                            rt += (double)v.x + (double)v.y;
+                            rs += (double)w.x + (double)w.y;
+                        }
                         n += s.cnt[k][src];
                     }
                     const int gi = gbase + k * S;
-                    if constexpr (!SR) p.out_accp[gi] = Accp{G * r[0], G * r[1], G * r[2], G * r[3]};
+                    if constexpr (CO) {
+                        // self-potential G m / r_out removed (src/hard.hpp:1663-1674)
+                        const double self = (double)s.co.coi[k][slot].mass / r_out_walk;
+                        p.out_accp[gi] = Accp{G * r[0], G * r[1], G * r[2], G * ((r[3] + rt) + self)};
+                        p.out_pot_soft[gi] = G * ((r[3] + rs) + self);
+                    } else if constexpr (!SR) {
+                        p.out_accp[gi] = Accp{G * r[0], G * r[1], G * r[2], G * r[3]};
+                    }
                     p.out_nnb[gi] = n;
                 }
             }
@@ -844,10 +997,10 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS>& s, int ct) {
     }
 }
 
-template <int CW, int KI, int MINB, bool PK, bool SR, int TE, int NS>
+template <int CW, int KI, int MINB, bool PK, int MD, int TE, int NS>
 __global__ __launch_bounds__((CW + 1) * 32, MINB) void ws_kernel(Params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    Smem<CW, KI, PK, TE, NS>& s = *reinterpret_cast<Smem<CW, KI, PK, TE, NS>*>(smem_raw);
+    Smem<CW, KI, PK, TE, NS, MD>& s = *reinterpret_cast<Smem<CW, KI, PK, TE, NS, MD>*>(smem_raw);
     const int tid = threadIdx.x;
     if (tid == 0) {
         for (int i = 0; i < NS; ++i) {
@@ -857,30 +1010,30 @@ __global__ __launch_bounds__((CW + 1) * 32, MINB) void ws_kernel(Params p) {
     }
     __syncthreads();
     if (tid >= CW * 32)
-        producer<CW, KI, PK, SR, TE, NS>(p, s, tid - CW * 32);
+        producer<CW, KI, PK, MD, TE, NS>(p, s, tid - CW * 32);
     else
-        consumer<CW, KI, PK, SR, TE, NS>(p, s, tid);
+        consumer<CW, KI, PK, MD, TE, NS>(p, s, tid);
 }
 
-template <int CW, int KI, int MINB, bool PK, bool SR = false, int TE = 128, int NS = 4>
+template <int CW, int KI, int MINB, bool PK, int MD = kModeForce, int TE = 128, int NS = 4>
 cudaError_t launch_ws_t(const Params& p, cudaStream_t st, int num_sms) {
     cudaError_t e = cudaMemsetAsync(p.queue_head, 0, sizeof(int32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), st);
     if (e != cudaSuccess) return e;
     if (p.n_walk <= 0) return cudaSuccess;
     static int per_sm = 0;
-    const size_t smem = sizeof(Smem<CW, KI, PK, TE, NS>);
+    const size_t smem = sizeof(Smem<CW, KI, PK, TE, NS, MD>);
     if (per_sm == 0) {
-        e = cudaFuncSetAttribute(ws_kernel<CW, KI, MINB, PK, SR, TE, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(ws_kernel<CW, KI, MINB, PK, MD, TE, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ws_kernel<CW, KI, MINB, PK, SR, TE, NS>, (CW + 1) * 32, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ws_kernel<CW, KI, MINB, PK, MD, TE, NS>, (CW + 1) * 32, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
     int grid = num_sms * per_sm;
     if (grid > p.n_walk) grid = p.n_walk;
-    ws_kernel<CW, KI, MINB, PK, SR, TE, NS><<<grid, (CW + 1) * 32, smem, st>>>(p);
+    ws_kernel<CW, KI, MINB, PK, MD, TE, NS><<<grid, (CW + 1) * 32, smem, st>>>(p);
     return cudaGetLastError();
 }
 
@@ -937,19 +1090,23 @@ cudaError_t launch_split_j(const EpjMix* epj, int64_t n_epj, EpjF32* epj32, cons
 cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant) {
     switch (variant) {
         case 0: return launch_ws_t<4, 3, 4, false>(p, s, num_sms);
-        case 1: return launch_ws_t<4, 3, 4, false, false, 64, 8>(p, s, num_sms);
-        case 2: return launch_ws_t<4, 3, 4, true, false, 64, 8>(p, s, num_sms);
-        case 3: return launch_ws_t<4, 2, 4, true, false, 64, 8>(p, s, num_sms);
+        case 1: return launch_ws_t<4, 3, 4, false, kModeForce, 64, 8>(p, s, num_sms);
+        case 2: return launch_ws_t<4, 3, 4, true, kModeForce, 64, 8>(p, s, num_sms);
+        case 3: return launch_ws_t<4, 2, 4, true, kModeForce, 64, 8>(p, s, num_sms);
         case 4: return launch_ws_t<4, 2, 4, true>(p, s, num_sms);
         case 5: return launch_ws_t<4, 3, 4, true>(p, s, num_sms);
-        case 6: return launch_ws_t<4, 4, 4, false, false, 64, 8>(p, s, num_sms);
-        case 7: return launch_ws_t<4, 3, 3, true, false, 128, 6>(p, s, num_sms);
+        case 6: return launch_ws_t<4, 4, 4, false, kModeForce, 64, 8>(p, s, num_sms);
+        case 7: return launch_ws_t<4, 3, 3, true, kModeForce, 128, 6>(p, s, num_sms);
         default: return cudaErrorInvalidValue;
     }
 }
 
 cudaError_t launch_ws_search(const Params& p, cudaStream_t s, int num_sms) {
-    return launch_ws_t<4, 3, 4, false, true>(p, s, num_sms);
+    return launch_ws_t<4, 3, 4, false, kModeSearch>(p, s, num_sms);
+}
+
+cudaError_t launch_ws_changeover(const Params& p, cudaStream_t s, int num_sms) {
+    return launch_ws_t<4, 3, 3, false, kModeChangeover, 64, 4>(p, s, num_sms);
 }
 
 }  // namespace pgf

@@ -29,6 +29,7 @@ PGF_PRECISION_FP64 = 1
 NUM_KERNEL_VARIANTS = 9  # PGF_NUM_KERNEL_VARIANTS
 PGF_MODE_FORCE = 0
 PGF_MODE_NEIGHBOR_SEARCH = 1
+PGF_MODE_FORCE_CHANGEOVER = 2
 
 # PeTar's EPISoft (src/soft_ptcl.hpp:271-308): id, pos, r_search, rank_org, type.
 EPI_DTYPE = np.dtype([("id", "<i8"), ("pos", "<f8", 3), ("r_search", "<f8"), ("rank_org", "<i4"),
@@ -41,6 +42,13 @@ EPJ_DTYPE = np.dtype([("id", "<i8"), ("mass", "<f8"), ("pos", "<f8", 3), ("vel",
 SPJ_DTYPE = np.dtype([("mass", "<f8"), ("pos", "<f8", 3), ("quad", "<f8", 6)], align=True)
 # PeTar's ForceSoft (src/soft_ptcl.hpp:4-24): acc, pot, n_ngb.
 FORCE_DTYPE = np.dtype([("acc", "<f8", 3), ("pot", "<f8"), ("n_ngb", "<i8")], align=True)
+# For the fused changeover mode: EPISoft extended with the particle's changeover
+# radii and self-potential mass, ForceSoft with the soft potential.  EPJSoft
+# already carries id, r_in, r_out and group_data = (mass_backup, status).
+EPI_CO_DTYPE = np.dtype([("id", "<i8"), ("pos", "<f8", 3), ("r_search", "<f8"), ("rank_org", "<i4"),
+                         ("type", "<i4"), ("r_in", "<f8"), ("r_out", "<f8"), ("self_mass", "<f8")], align=True)
+FORCE_CO_DTYPE = np.dtype([("acc", "<f8", 3), ("pot", "<f8"), ("n_ngb", "<i8"), ("pot_soft", "<f8")],
+                          align=True)
 
 
 class GpuForceError(RuntimeError):
@@ -61,6 +69,12 @@ class _EpjLayout(ctypes.Structure):
 class _SpjLayout(ctypes.Structure):
     _fields_ = [("size", ctypes.c_size_t), ("off_mass", ctypes.c_size_t), ("off_pos", ctypes.c_size_t),
                 ("off_quad", ctypes.c_size_t), ("has_quad", ctypes.c_int)]
+
+
+class _ChangeoverLayout(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_size_t) for k in (
+        "epi_off_id", "epi_off_r_in", "epi_off_r_out", "epi_off_self_mass", "epj_off_id", "epj_off_r_in",
+        "epj_off_r_out", "epj_off_mass_backup", "epj_off_status", "force_off_pot_soft")]
 
 
 class _ForceLayout(ctypes.Structure):
@@ -126,6 +140,7 @@ def load(build: bool = True) -> ctypes.CDLL:
         "pgf_set_kernel_variant": [ci],
         "pgf_set_dispatch_stages": [ci],
         "pgf_set_mode": [ci],
+        "pgf_set_changeover_layout": [vp],
         "pgf_get_kernel_variant": [vp],
         "pgf_autotune": [ci, ci, vp, vp],
         "pgf_wait": [ci],
@@ -245,12 +260,16 @@ class CalcForceWithLinearCutoffCUDAMultiWalk:
         _check(load().pgf_initialize(rank, eps2, rcut2, G))
 
     def __call__(self, tag, n_walk, epi, n_epi, id_epj, n_epj, id_spj, n_spj, epj, n_epj_tot, spj,
-                 n_spj_tot, send_flag):
+                 n_spj_tot, send_flag, epi_dtype=None):
+        """epi_dtype: the EPI record type when ``epi`` is a table of raw
+        addresses (default EPI_DTYPE, or the dtype of the arrays passed)."""
         lib = load()
         # Re-assert this functor's constants: like the reference, the device
         # state is process-wide and the last initialize() wins.
         _check(lib.pgf_initialize(self.my_rank, self.eps2, self.rcut2, self.G))
-        el, jl, sl, _ = _layouts(EPI_DTYPE, epj.dtype if epj is not None else EPJ_DTYPE,
+        if epi_dtype is None:
+            epi_dtype = epi[0].dtype if isinstance(epi, (list, tuple)) and len(epi) else EPI_DTYPE
+        el, jl, sl, _ = _layouts(epi_dtype, epj.dtype if epj is not None else EPJ_DTYPE,
                                  spj.dtype if spj is not None else SPJ_DTYPE)
         if send_flag:
             _check(lib.pgf_dispatch_index(tag, 0, None, None, None, None, None, None, None,
@@ -279,7 +298,9 @@ class CalcForceWithLinearCutoffCUDA:
     def __call__(self, tag, n_walk, epi, n_epi, epj, n_epj, spj, n_spj):
         lib = load()
         _check(lib.pgf_initialize(self.my_rank, self.eps2, self.rcut2, self.G))
-        el, jl, sl, _ = _layouts()
+        def dt(a, default):
+            return a[0].dtype if isinstance(a, (list, tuple)) and len(a) else default
+        el, jl, sl, _ = _layouts(dt(epi, EPI_DTYPE), dt(epj, EPJ_DTYPE), dt(spj, SPJ_DTYPE))
         n_epi = np.ascontiguousarray(n_epi, dtype=np.int32)
         n_epj = np.ascontiguousarray(n_epj, dtype=np.int32)
         n_spj = np.ascontiguousarray(n_spj, dtype=np.int32)
@@ -290,10 +311,13 @@ class CalcForceWithLinearCutoffCUDA:
         return 0
 
 
-def RetrieveForceCUDA(tag, n_walk, ni, force) -> int:
-    """src/force_gpu_cuda.hpp:165-168: overwrites acc, pot, n_ngb of force[w]."""
+def RetrieveForceCUDA(tag, n_walk, ni, force, force_dtype=None) -> int:
+    """src/force_gpu_cuda.hpp:165-168: overwrites acc, pot, n_ngb of force[w].
+    force_dtype: the record type when ``force`` is a table of raw addresses."""
     lib = load()
-    fdt = force[0].dtype if isinstance(force, (list, tuple)) and len(force) else FORCE_DTYPE
+    fdt = force_dtype
+    if fdt is None:
+        fdt = force[0].dtype if isinstance(force, (list, tuple)) and len(force) else FORCE_DTYPE
     _, _, _, fl = _layouts(force_dt=fdt)
     ni = np.ascontiguousarray(ni, dtype=np.int32)
     pf = _ptr_table(force)
@@ -309,9 +333,11 @@ class Records:
     """A WalkBatch converted to PeTar-layout record arrays plus the per-walk
     pointer tables the functors take."""
 
-    def __init__(self, batch):
+    def __init__(self, batch, co=None):
+        """co: a walks.ChangeoverSet for the fused changeover mode (extended
+        EPI and Force records; EPJ ids, radii and group_data filled in)."""
         ni = batch.epi_rs.size
-        self.epi = np.zeros(ni, EPI_DTYPE)
+        self.epi = np.zeros(ni, EPI_CO_DTYPE if co is not None else EPI_DTYPE)
         self.epi["pos"] = batch.epi_pos
         self.epi["r_search"] = batch.epi_rs
         self.epi["type"] = 1
@@ -321,18 +347,31 @@ class Records:
         self.epj["pos"] = batch.epj_pos
         self.epj["r_search"] = batch.epj_rs
         self.epj["id"] = np.arange(batch.epj_mass.size)
+        self.co = co
+        if co is not None:
+            self.epi["id"] = co.epi_id
+            self.epi["r_in"] = co.epi_r_in
+            self.epi["r_out"] = co.epi_r_out
+            self.epi["self_mass"] = co.epi_self_mass
+            self.epj["id"] = co.epj_id
+            self.epj["r_in"] = co.epj_r_in
+            self.epj["r_out"] = co.epj_r_out
+            gd = self.epj["group_data"].view(np.float64).reshape(-1, 2)
+            gd[:, 0] = co.epj_mass_backup
+            gd[:, 1] = co.epj_status
+            self.epj["group_data"] = gd.view(np.int64).reshape(-1, 2)
         self.spj = np.zeros(batch.spj_mass.size, SPJ_DTYPE)
         self.spj["mass"] = batch.spj_mass
         self.spj["pos"] = batch.spj_pos
         self.spj["quad"] = batch.spj_quad
-        self.force = np.zeros(ni, FORCE_DTYPE)
+        self.force = np.zeros(ni, FORCE_CO_DTYPE if co is not None else FORCE_DTYPE)
         self.id_epj = np.ascontiguousarray(batch.id_epj, dtype=np.int32)
         self.id_spj = np.ascontiguousarray(batch.id_spj, dtype=np.int32)
         self.n_walk = batch.n_walk
         self.n_epi = np.diff(batch.epi_disp).astype(np.int32)
         self.n_epj = np.diff(batch.epj_disp).astype(np.int32)
         self.n_spj = np.diff(batch.spj_disp).astype(np.int32)
-        isz, fsz = EPI_DTYPE.itemsize, FORCE_DTYPE.itemsize
+        isz, fsz = self.epi.dtype.itemsize, self.force.dtype.itemsize
         d = np.asarray(batch.epi_disp[:-1], dtype=np.uint64)
         self.p_epi = (np.uint64(self.epi.ctypes.data) + d * np.uint64(isz)).astype(np.uint64)
         self.p_force = (np.uint64(self.force.ctypes.data) + d * np.uint64(fsz)).astype(np.uint64)
@@ -357,13 +396,13 @@ def dispatch(rec: Records, tag: int = 0, send: bool = True) -> None:
     set_walk_rcut2(rec.walk_rcut2)
     try:
         f(tag, rec.n_walk, rec.p_epi, rec.n_epi, rec.p_id_epj, rec.n_epj, rec.p_id_spj, rec.n_spj,
-          None, 0, None, 0, False)
+          None, 0, None, 0, False, epi_dtype=rec.epi.dtype)
     finally:
         set_walk_rcut2(None)
 
 
 def retrieve(rec: Records, tag: int = 0) -> np.ndarray:
-    RetrieveForceCUDA(tag, rec.n_walk, rec.n_epi, rec.p_force)
+    RetrieveForceCUDA(tag, rec.n_walk, rec.n_epi, rec.p_force, force_dtype=rec.force.dtype)
     return rec.force
 
 
@@ -388,3 +427,36 @@ def search_neighbors(batch, rec: Records | None = None) -> np.ndarray:
     finally:
         set_mode(PGF_MODE_FORCE)
     return f["n_ngb"].copy()
+
+
+def changeover_layout(rec: Records) -> _ChangeoverLayout:
+    """The pgf_changeover_layout of a Records built with a ChangeoverSet."""
+    fi, fj, ff = rec.epi.dtype.fields, rec.epj.dtype.fields, rec.force.dtype.fields
+    gd = fj["group_data"][1]
+    return _ChangeoverLayout(fi["id"][1], fi["r_in"][1], fi["r_out"][1], fi["self_mass"][1], fj["id"][1],
+                             fj["r_in"][1], fj["r_out"][1], gd, gd + 8, ff["pot_soft"][1])
+
+
+def set_changeover_layout(rec: Records | None) -> None:
+    """Sets (rec with a ChangeoverSet) or clears (None) the changeover layout."""
+    if rec is None:
+        _check(load().pgf_set_changeover_layout(None))
+    else:
+        lay = changeover_layout(rec)
+        _check(load().pgf_set_changeover_layout(ctypes.byref(lay)))
+
+
+def compute_changeover(batch, co, rec: Records | None = None) -> dict:
+    """acc, pot (total), pot_soft and nnb of every EPI row in the fused
+    changeover mode, through the C ABI (send and dispatch as FDPS does)."""
+    rec = rec if rec is not None else Records(batch, co)
+    set_precision(PGF_PRECISION_MIXED)
+    set_changeover_layout(rec)
+    set_mode(PGF_MODE_FORCE_CHANGEOVER)
+    try:
+        dispatch(rec)
+        f = retrieve(rec)
+    finally:
+        set_mode(PGF_MODE_FORCE)
+        set_changeover_layout(None)
+    return dict(acc=f["acc"].copy(), pot=f["pot"].copy(), pot_soft=f["pot_soft"].copy(), nnb=f["n_ngb"].copy())

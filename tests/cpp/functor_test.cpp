@@ -61,6 +61,25 @@ struct ForceSoft {
 
 #include "petar_gpuforce.hpp"
 
+// Records of the fused changeover mode: EPISoft and ForceSoft extended.
+struct EPISoftCO {
+    PS::S64 id;
+    PS::F64vec pos;
+    PS::F64 r_search;
+    PS::S32 rank_org;
+    PS::S32 type;
+    PS::F64 r_in, r_out, self_mass;
+};
+struct ForceSoftCO {
+    PS::F64vec acc;
+    PS::F64 pot;
+    PS::S64 n_ngb;
+    PS::F64 pot_soft;
+};
+// The changeover functor and retrieve instantiate with them (compile check).
+template struct CalcForceWithLinearCutoffChangeoverCUDAMultiWalk<EPISoftCO, ForceSoftCO>;
+template PS::S32 RetrieveForceChangeoverCUDA<ForceSoftCO>(const PS::S32, const PS::S32, const PS::S32*, ForceSoftCO**);
+
 template <class T>
 static void rd(FILE* f, T* p, size_t n) {
     if (n && fread(p, sizeof(T), n, f) != n) {

@@ -336,3 +336,94 @@ def test_neighbor_search_binaries_leaves_acc_and_pot():
     assert (rec.force["acc"] == 7.0).all() and (rec.force["pot"] == -3.0).all()
     res = gpuforce.compute(wb, PGF_PRECISION_MIXED)
     check(wb, res, PGF_PRECISION_MIXED, o=o_force, label="force after search")
+
+
+def check_changeover(batch, co, res, label=""):
+    """Fused changeover mode against the oracle's kernel + correction
+    composition: counts exact, acc and both potentials at the mixed-precision
+    tolerances."""
+    o = oracle.force_changeover(batch, co)
+    np.testing.assert_array_equal(res["nnb"], o["nnb"], err_msg=f"{label} neighbour counts")
+    for key, e in (("acc", rel_err_vec(res["acc"], o["acc"])), ("pot", rel_err(res["pot"], o["pot"])),
+                   ("pot_soft", rel_err(res["pot_soft"], o["pot_soft"]))):
+        st = stats(e)
+        assert st["median"] <= MIXED_MEDIAN and st["p999"] <= MIXED_P999 and st["max"] <= MIXED_MAX, (label, key, st)
+    return o
+
+
+@pytest.mark.parametrize("seed,bf", [(31, 0.0), (32, 0.5)])
+def test_changeover_mode_matches_oracle(seed, bf):
+    """Soft force with the neighbour changeover correction fused into the
+    kernel, against the reference's CPU composition: linear-cutoff kernel,
+    then calcAccPotShortWithLinearCutoff for every neighbour, with singles,
+    members and artificial particles among the j and mass-scaled radii."""
+    cl = ics.make_plummer_cluster(seed, 20000, 0.004, binary_fraction=bf)
+    wb, co = walks.make_changeover(walks.build_walks(cl), cl.r_in, cl.r_out, seed=seed)
+    res = gpuforce.compute_changeover(wb, co)
+    o = check_changeover(wb, co, res, label=f"changeover seed {seed}")
+    plain = oracle.force(wb)
+    assert np.abs(o["acc"] - plain["acc"]).max() > 0  # the correction matters here
+    # the force mode is back afterwards
+    check(wb, gpuforce.compute(wb, PGF_PRECISION_MIXED), PGF_PRECISION_MIXED, o=plain, label="force after")
+
+
+def test_changeover_mode_boundary_pairs_retested():
+    """Pairs at r_search to within FP64 ulps: the FP32 test cannot decide them,
+    and the FP64 re-test must both count them and replace their linear-cutoff
+    potentials by the changeover ones (pot_soft gains G m pot_off per
+    neighbour beyond r_out)."""
+    rng = np.random.default_rng(6)
+    n = 3000
+    rs = 0.01
+    xi = rng.normal(size=(1, 3)) * 0.02
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    r = rs * (1.0 + rng.integers(-8, 9, n) * 2.0 ** -52)
+    xj = xi + u * r[:, None]
+    mass = np.full(n, 1.0 / n)
+    status = rng.choice([0.0, -1.0, 1.0], size=n, p=[0.7, 0.2, 0.1])
+    mbk = np.where(status < 0, mass, 0.0)
+    mass = np.where(status < 0, 0.0, mass)
+    wb = walks.WalkBatch(
+        epi_pos=xi, epi_rs=np.array([rs]), epi_disp=np.array([0, 1], np.int64),
+        epj_pos=xj, epj_mass=mass, epj_rs=np.full(n, rs), spj_pos=np.zeros((0, 3)),
+        spj_mass=np.zeros(0), spj_quad=np.zeros((0, 6)), epj_disp=np.array([0, n], np.int64),
+        id_epj=np.arange(n, dtype=np.int32), spj_disp=np.array([0, 0], np.int64),
+        id_spj=np.zeros(0, np.int32), eps2=0.0, rcut2=(0.3 * rs) ** 2, G=1.0)
+    co = walks.ChangeoverSet(
+        epi_id=np.array([-7], np.int64), epi_r_in=np.array([0.03 * rs]), epi_r_out=np.array([0.3 * rs]),
+        epi_self_mass=np.array([0.0]), epj_id=np.arange(n, dtype=np.int64),
+        epj_r_in=np.full(n, 0.05 * rs), epj_r_out=np.full(n, 0.5 * rs), epj_mass_backup=mbk, epj_status=status)
+    o = oracle.force_changeover(wb, co)
+    assert 0 < o["nnb"][0] < n
+    before = gpuforce.get_profile()["n_retest"]
+    res = gpuforce.compute_changeover(wb, co)
+    assert gpuforce.get_profile()["n_retest"] > before
+    np.testing.assert_array_equal(res["nnb"], o["nnb"])
+    for key in ("pot", "pot_soft"):
+        assert abs(res[key][0] - o[key][0]) <= 1e-5 * abs(o[key][0]), (key, res[key][0], o[key][0])
+    np.testing.assert_allclose(res["acc"], o["acc"], rtol=1e-5, atol=1e-5 * np.abs(o["acc"]).max())
+
+
+def test_changeover_mode_pipelined_and_without_layout():
+    """Pipeline stages give bit-identical changeover results; the mode refuses
+    to run without its layout."""
+    cl = ics.make_plummer_cluster(33, 20000, 0.004, binary_fraction=0.5)
+    wb, co = walks.make_changeover(walks.build_walks(cl), cl.r_in, cl.r_out, seed=4)
+    out = {}
+    try:
+        for stages in (1, 4):
+            gpuforce.set_dispatch_stages(stages)
+            out[stages] = gpuforce.compute_changeover(wb, co)
+    finally:
+        gpuforce.set_dispatch_stages(0)
+    for k in ("acc", "pot", "pot_soft", "nnb"):
+        np.testing.assert_array_equal(out[1][k], out[4][k])
+    rec = gpuforce.Records(wb, co)
+    gpuforce.set_mode(gpuforce.PGF_MODE_FORCE_CHANGEOVER)
+    try:
+        with pytest.raises(gpuforce.GpuForceError) as e:
+            gpuforce.dispatch(rec)
+        assert e.value.code == 4
+    finally:
+        gpuforce.set_mode(gpuforce.PGF_MODE_FORCE)
