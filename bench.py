@@ -338,7 +338,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", init_method="env://")
     torch.cuda.set_device(local)
-    from petar_gb300 import gpuforce
+    from petar_gb300 import gpuforce, walks
     from petar_gb300.gpuforce import PGF_PRECISION_FP64, PGF_PRECISION_MIXED
 
     def barrier():
@@ -439,8 +439,11 @@ def run_ours(args):
 
     # ---- end to end through the C ABI with host records ----
     ni, ne, ns = wb.epi_rs.size, wb.id_epj.size, wb.id_spj.size
-    h2d = (wb.epj_mass.size * (32 + 8 + 4) + wb.spj_mass.size * 80 + ni * 32 + (ne + ns) * 4 + wb.n_walk * (64 + 4))
-    d2h = ni * (32 + 4) + 12
+    # EPJ: EpjMix 32 B + FP64 mass and r_search 16 B; SPJ: SpjMix 64 B + SpjQ64 64 B;
+    # EPI 32 B; ids 4 B; walk descriptor 96 B + queue entry 4 B.  Back: Accp
+    # 32 B + count 4 B per i, and the 16-byte status words.
+    h2d = (wb.epj_mass.size * 48 + wb.spj_mass.size * 128 + ni * 32 + (ne + ns) * 4 + wb.n_walk * 100)
+    d2h = ni * (32 + 4) + 16
     e2e_t = []
     for k in range(args.warmup + args.steps):
         barrier()
@@ -457,6 +460,49 @@ def run_ours(args):
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
            "ms_per_step": 1e3 * e2e_total / args.steps,
            "breakdown_ms_per_step": {k: 1e3 * bd[k] / args.steps for k in ("copy", "send", "calc", "recv")}}
+
+    # ---- the other modes on the same lists ----
+    modes = None
+    if not args.no_modes:
+        def time_recompute(tag: int, n: int = 3) -> float:
+            ts = []
+            for _ in range(n + 1):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                gpuforce.recompute(tag)
+                e1.record(stream)
+                gpuforce.wait(tag)
+                ts.append(e0.elapsed_time(e1))
+            return statistics.mean(ts[1:])
+        modes = {}
+        # neighbour search (SearchNeighborEpEp): EP-EP lists only
+        gpuforce.set_mode(gpuforce.PGF_MODE_NEIGHBOR_SEARCH)
+        try:
+            gpuforce.dispatch(rec, tag=1, send=False)
+            gpuforce.retrieve(rec, tag=1)
+            t = time_recompute(1)
+        finally:
+            gpuforce.set_mode(gpuforce.PGF_MODE_FORCE)
+        modes["neighbor_search"] = {"ms_per_step": t, "value": n_epep / t / 1e6, "unit": "Gpairs/s",
+                                    "pairs": n_epep}
+        # soft force with the changeover correction of neighbours fused in
+        wb_co, co = walks.make_changeover(wb, cl.r_in, cl.r_out, seed=1)
+        rec_co = gpuforce.Records(wb_co, co)
+        gpuforce.set_changeover_layout(rec_co)
+        gpuforce.set_mode(gpuforce.PGF_MODE_FORCE_CHANGEOVER)
+        try:
+            gpuforce.dispatch(rec_co, tag=2)
+            gpuforce.retrieve(rec_co, tag=2)
+            t = time_recompute(2)
+        finally:
+            gpuforce.set_mode(gpuforce.PGF_MODE_FORCE)
+            gpuforce.set_changeover_layout(None)
+        co_entry = {"ms_per_step": t, "value": n_int / t / 1e6, "unit": "Ginteractions/s",
+                    "overhead_vs_force_mode": t / statistics.mean(step_ms),
+                    "members_fraction": 0.1, "artificial_fraction": 0.05,
+                    "parity": "tests/test_gpu_parity.py::test_changeover_mode_*"}
+        modes["force_changeover"] = co_entry
 
     if rank != 0:
         torch.distributed.barrier()
@@ -496,7 +542,7 @@ def run_ours(args):
         "gpu_launches": 2 * args.steps,
         "kernel_variant": best_variant, "variant_main_ms": variant_ms,
         "fp64_plain": fp64, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-        "retest_records_per_step": n_retest, "wall_s_timed_region": wall,
+        "retest_records_per_step": n_retest, "wall_s_timed_region": wall, "modes": modes,
     }
     print(json.dumps(out), flush=True)
     if world > 1:
@@ -513,6 +559,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-modes", action="store_true", help="skip the search and changeover mode timings")
     ap.add_argument("--variant", type=int, default=-1,
                     help="use this kernel variant instead of the autotuner's choice")
     args = ap.parse_args()

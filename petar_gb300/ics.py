@@ -189,12 +189,17 @@ def king(rng: np.random.Generator, mass: np.ndarray, W0: float = 7.0) -> tuple[n
     vmax = np.sqrt(2.0 * w)
     vv = np.zeros(n)
     todo = np.arange(n)
+    # Envelope: the maximum of p over v on a grid of w values (p's maximum
+    # grows with w), interpolated per particle with a 10% margin.
     xs = np.linspace(0.0, 1.0, 257)[1:]
+    wgrid = np.linspace(0.0, float(w.max()) if n else 0.0, 2049)
+    vgrid = np.sqrt(2.0 * wgrid)[:, None] * xs[None, :]
+    pgrid = (vgrid ** 2 * (np.exp(wgrid[:, None] - 0.5 * vgrid ** 2) - 1.0)).max(axis=1)
+    pmax_all = np.interp(w, wgrid, pgrid) * 1.10 + 1e-300
     while todo.size:
         vm = vmax[todo]
         ww = w[todo]
-        grid = vm[:, None] * xs[None, :]
-        pmax = (grid ** 2 * (np.exp(ww[:, None] - 0.5 * grid ** 2) - 1.0)).max(axis=1) * 1.05 + 1e-300
+        pmax = pmax_all[todo]
         v_try = vm * rng.random(todo.size)
         p = v_try ** 2 * (np.exp(ww - 0.5 * v_try ** 2) - 1.0)
         ok = rng.random(todo.size) * pmax < p

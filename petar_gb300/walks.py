@@ -242,3 +242,14 @@ def make_changeover(batch: WalkBatch, r_in: float, r_out: float, member_fraction
     out = WalkBatch(**{k: getattr(batch, k) for k in batch.__dataclass_fields__})
     out.epj_mass = soft_m
     return out, co
+
+
+def subset_changeover(batch: WalkBatch, co: ChangeoverSet, walks: np.ndarray) -> ChangeoverSet:
+    """The changeover set of ``batch.subset(walks)``: EPI arrays restricted to
+    the rows of those walks, EPJ arrays shared."""
+    walks = np.asarray(walks, dtype=np.int64)
+    rows = np.concatenate([np.arange(batch.epi_disp[w], batch.epi_disp[w + 1]) for w in walks]) \
+        if walks.size else np.zeros(0, np.int64)
+    return ChangeoverSet(epi_id=co.epi_id[rows], epi_r_in=co.epi_r_in[rows], epi_r_out=co.epi_r_out[rows],
+                         epi_self_mass=co.epi_self_mass[rows], epj_id=co.epj_id, epj_r_in=co.epj_r_in,
+                         epj_r_out=co.epj_r_out, epj_mass_backup=co.epj_mass_backup, epj_status=co.epj_status)
