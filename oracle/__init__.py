@@ -48,6 +48,8 @@ def _lib():
         lib.oracle_co_w.argtypes = [ctypes.c_int64] + [vp] * 5
         lib.oracle_co_w_two.restype = None
         lib.oracle_co_w_two.argtypes = [ctypes.c_int64] + [vp] * 7
+        lib.oracle_gradient.restype = None
+        lib.oracle_gradient.argtypes = [ctypes.c_int64] + [vp] * 13 + [ctypes.c_double] * 3 + [vp] * 4
         lib.oracle_force_changeover.restype = None
         lib.oracle_force_changeover.argtypes = ([ctypes.c_int64] + [vp] * 13 + [ctypes.c_double] * 3 + [vp]
                                                 + [vp] * 9 + [vp] * 4)
@@ -129,6 +131,23 @@ def force_changeover(batch, co) -> dict:
     lib.oracle_force_changeover(batch.n_walk, *[_p(a) for a in arrs], float(batch.eps2), float(batch.rcut2),
                                 float(batch.G), _p(wr), *[_p(a) for a in coa], _p(out["acc"]), _p(out["pot"]),
                                 _p(out["pot_soft"]), _p(out["nnb"]))
+    return out
+
+
+def gradient(batch, epi_acc, epj_acc) -> dict:
+    """KDKDK_4TH gradient-correction pass of every EPI row (oracle_gradient):
+    acorr, acc and pot as the reference's functors write them."""
+    lib = _lib()
+    ni = batch.epi_rs.size
+    arrs = [_c(batch.epi_disp, np.int64), _c(batch.epi_pos, np.float64), _c(epi_acc, np.float64),
+            _c(batch.epj_pos, np.float64), _c(batch.epj_mass, np.float64), _c(epj_acc, np.float64),
+            _c(batch.spj_pos, np.float64), _c(batch.spj_mass, np.float64), _c(batch.spj_quad, np.float64),
+            _c(batch.epj_disp, np.int64), _c(batch.id_epj, np.int32), _c(batch.spj_disp, np.int64),
+            _c(batch.id_spj, np.int32)]
+    wr = None if batch.walk_rcut2 is None else _c(batch.walk_rcut2, np.float64)
+    out = dict(acorr=np.zeros((ni, 3)), acc=np.zeros((ni, 3)), pot=np.zeros(ni))
+    lib.oracle_gradient(batch.n_walk, *[_p(a) for a in arrs], float(batch.eps2), float(batch.rcut2),
+                        float(batch.G), _p(wr), _p(out["acorr"]), _p(out["acc"]), _p(out["pot"]))
     return out
 
 

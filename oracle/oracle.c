@@ -345,3 +345,54 @@ void oracle_force_changeover(int64_t n_walk, const int64_t *epi_disp, const doub
         }
     }
 }
+
+/* KDKDK_4TH gradient-correction pass (src/petar.hpp:1123-1140): per walk,
+ * CalcCorrectEpEpWithLinearCutoffNoSimd (src/soft_force.hpp:89-122) over the
+ * EPJ list, then the quadrupole EP-SP force functor (src/soft_force.hpp:
+ * 160-200), accumulated into one cleared ForceSoft as FDPS does:
+ *   acorr = 2 sum_j -m_j/r^3 (da - 3 (dr.da)/r^2 dr)   (no G; r = max(r, r_out))
+ *   acc   = acc_i + G acc_sp,   pot = G pot_sp. */
+void oracle_gradient(int64_t n_walk, const int64_t *epi_disp, const double *epi_pos, const double *epi_acc,
+                     const double *epj_pos, const double *epj_mass, const double *epj_acc,
+                     const double *spj_pos, const double *spj_mass, const double *spj_quad,
+                     const int64_t *epj_disp, const int32_t *id_epj, const int64_t *spj_disp,
+                     const int32_t *id_spj, double eps2, double rcut2, double G, const double *walk_rcut2,
+                     double *acorr, double *acc, double *pot) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t w = 0; w < n_walk; ++w) {
+        const double r_out2 = walk_rcut2 ? walk_rcut2[w] : rcut2;
+        for (int64_t i = epi_disp[w]; i < epi_disp[w + 1]; ++i) {
+            const double *xi = epi_pos + 3 * i;
+            const double *ai = epi_acc + 3 * i;
+            double cx = 0.0, cy = 0.0, cz = 0.0;
+            for (int64_t k = epj_disp[w]; k < epj_disp[w + 1]; ++k) {
+                const int64_t j = id_epj[k];
+                const double drx = xi[0] - epj_pos[3 * j + 0];
+                const double dry = xi[1] - epj_pos[3 * j + 1];
+                const double drz = xi[2] - epj_pos[3 * j + 2];
+                const double dax = ai[0] - epj_acc[3 * j + 0];
+                const double day = ai[1] - epj_acc[3 * j + 1];
+                const double daz = ai[2] - epj_acc[3 * j + 2];
+                const double r2 = drx * drx + dry * dry + drz * drz + eps2;
+                const double drda = drx * dax + dry * day + drz * daz;
+                const double r2_tmp = (r2 > r_out2) ? r2 : r_out2;
+                const double r_inv = 1.0 / sqrt(r2_tmp);
+                const double r2_inv = r_inv * r_inv;
+                const double m_r = epj_mass[j] * r_inv;
+                const double m_r3 = m_r * r2_inv;
+                const double alpha = 3.0 * drda * r2_inv;
+                cx -= m_r3 * (dax - alpha * drx);
+                cy -= m_r3 * (day - alpha * dry);
+                cz -= m_r3 * (daz - alpha * drz);
+            }
+            acorr[3 * i + 0] = 0.0 + 2.0 * cx;
+            acorr[3 * i + 1] = 0.0 + 2.0 * cy;
+            acorr[3 * i + 2] = 0.0 + 2.0 * cz;
+            double as[3], ps;
+            epsp_one(xi, spj_pos, spj_mass, spj_quad, id_spj + spj_disp[w], spj_disp[w + 1] - spj_disp[w], eps2,
+                     as, &ps);
+            for (int d = 0; d < 3; ++d) acc[3 * i + d] = ai[d] + G * as[d];
+            pot[i] = 0.0 + G * ps;
+        }
+    }
+}

@@ -9,6 +9,8 @@
 #                      CALC_SP_64bit, RSQRT_NR_EPJ_X4, RSQRT_NR_SPJ_X4)
 #   libref_changeover.so  changeover W functions      (src/changeover.hpp; SDAR's
 #                      Common/Float.h replaced by oracle/ref/shim/Common/Float.h)
+#   libref_kdkdk.so    NoSimd functors built with KDKDK_4TH, for the gradient
+#                      correction CalcCorrectEpEpWithLinearCutoffNoSimd
 # The SIMD kernels are x86 only; on other hosts only the NoSimd library is
 # built.  The NoSimd build uses -ffp-contract=off so its FP64 results are
 # defined by source order alone.
@@ -33,6 +35,8 @@ if [ "$(uname -m)" = "x86_64" ]; then
     "$CXX" "${SIMD[@]}" "${COMMON[@]}" -DREF_SIMD -DCALC_EP_64bit -DCALC_SP_64bit \
         -DRSQRT_NR_EPJ_X4 -DRSQRT_NR_SPJ_X4 "$HERE/ref_driver.cpp" -o "$OUT/libref_simd64.so" &
 fi
+"$CXX" -O2 -ffp-contract=off "${COMMON[@]}" -DREF_NOSIMD -DKDKDK_4TH "$HERE/ref_driver.cpp" \
+    -o "$OUT/libref_kdkdk.so" &
 "$CXX" -O2 -ffp-contract=off -std=c++17 -fPIC -shared -I"$HERE/shim" -I"$SRC" \
     "$HERE/ref_changeover.cpp" -o "$OUT/libref_changeover.so" &
 wait

@@ -124,4 +124,44 @@ void ref_nb(int ni, const double* xi, const double* rsi, int nj, const double* x
     delete[] f;
 }
 
+#if defined(KDKDK_4TH) && defined(REF_NOSIMD)
+// KDKDK_4TH gradient correction, EP-EP part (CalcCorrectEpEpWithLinearCutoffNoSimd,
+// src/soft_force.hpp:89-122): acorr (no G) and the acc the functor writes
+// (the i-particle's own acc), for ni i-particles against nj j-particles.
+void ref_correct(int ni, const double* xi, const double* ai, int nj, const double* xj, const double* mj,
+                 const double* aj, double* acorr, double* acc) {
+    EPISoft* epi = new EPISoft[ni > 0 ? ni : 1];
+    EPJSoft* epj = new EPJSoft[nj > 0 ? nj : 1];
+    ForceSoft* f = new ForceSoft[ni > 0 ? ni : 1];
+    for (int i = 0; i < ni; ++i) {
+        epi[i].id = i;
+        epi[i].pos = PS::F64vec(xi[3 * i], xi[3 * i + 1], xi[3 * i + 2]);
+        epi[i].acc = PS::F64vec(ai[3 * i], ai[3 * i + 1], ai[3 * i + 2]);
+        epi[i].r_search = 0.0;
+        epi[i].rank_org = 0;
+        epi[i].type = 1;
+    }
+    for (int j = 0; j < nj; ++j) {
+        epj[j].id = j;
+        epj[j].mass = mj[j];
+        epj[j].pos = PS::F64vec(xj[3 * j], xj[3 * j + 1], xj[3 * j + 2]);
+        epj[j].acc = PS::F64vec(aj[3 * j], aj[3 * j + 1], aj[3 * j + 2]);
+        epj[j].r_search = 0.0;
+    }
+    for (int i = 0; i < ni; ++i) f[i].clear();
+    CalcCorrectEpEpWithLinearCutoffNoSimd()(epi, ni, epj, nj, f);
+    for (int i = 0; i < ni; ++i) {
+        acorr[3 * i] = f[i].acorr.x;
+        acorr[3 * i + 1] = f[i].acorr.y;
+        acorr[3 * i + 2] = f[i].acorr.z;
+        acc[3 * i] = f[i].acc.x;
+        acc[3 * i + 1] = f[i].acc.y;
+        acc[3 * i + 2] = f[i].acc.z;
+    }
+    delete[] epi;
+    delete[] epj;
+    delete[] f;
+}
+#endif
+
 }  // extern "C"

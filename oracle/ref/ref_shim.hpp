@@ -44,9 +44,16 @@ class ForceSoft {
 public:
     PS::F64vec acc;
     PS::F64 pot;
+#ifdef KDKDK_4TH
+    PS::F64vec acorr;
+#endif
     PS::S64 n_ngb;
     static PS::F64 grav_const;
+#ifdef KDKDK_4TH
+    void clear() { acc = 0.0; pot = 0.0; acorr = 0.0; n_ngb = 0; }
+#else
     void clear() { acc = 0.0; pot = 0.0; n_ngb = 0; }
+#endif
 };
 
 class EPISoft {
@@ -56,6 +63,9 @@ public:
     PS::F64 r_search;
     PS::S32 rank_org;
     PS::S32 type;
+#ifdef KDKDK_4TH
+    PS::F64vec acc;
+#endif
     static PS::F64 eps;
     static PS::F64 r_out;
     PS::F64vec getPos() const { return pos; }
@@ -66,6 +76,9 @@ public:
     PS::S64 id;
     PS::F64 mass;
     PS::F64vec pos;
+#ifdef KDKDK_4TH
+    PS::F64vec acc;
+#endif
     PS::F64 r_search;
     PS::F64vec getPos() const { return pos; }
     PS::F64 getCharge() const { return mass; }

@@ -186,6 +186,19 @@ union SlotCo {
     SlotEPco<TE> ep;
     SlotSP<TE> sp;
 };
+template <int TE>
+struct SlotEPx2co {
+    float4 nh[TE];
+    float4 nl[TE];
+    float4 fp[TE / 2][2];
+    int nidx[TE];
+    CoRec nco[TE];
+};
+template <int TE>
+union SlotCox2 {
+    SlotEPx2co<TE> ep;
+    SlotSPx2<TE> sp;
+};
 // What a kernel computes: soft force, neighbour search, or soft force with the
 // changeover correction of neighbours fused in (scalar arithmetic only).
 enum : int { kModeForce = 0, kModeSearch = 1, kModeChangeover = 2 };
@@ -196,6 +209,10 @@ struct SlotSel {
 template <int TE>
 struct SlotSel<false, TE, kModeChangeover> {
     using type = SlotCo<TE>;
+};
+template <int TE>
+struct SlotSel<true, TE, kModeChangeover> {
+    using type = SlotCox2<TE>;
 };
 template <int KI, int CT, bool CO>
 struct CoExtra {};
@@ -263,7 +280,6 @@ __device__ __forceinline__ void co_k_f32(float r, float r_in, float norm, float 
 template <int CW, int KI, bool PK, int MD, int TE, int NS>
 __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int lane) {
     constexpr bool SR = MD == kModeSearch, CO = MD == kModeChangeover;
-    static_assert(!(CO && PK), "the changeover mode runs scalar tiles");
     constexpr int kMaxPass = CW * 32 * KI;
     constexpr int kTileEP = TE, kTileSP = TE / 2, kSlots = NS;
     constexpr int QE = TE / 32, QS = TE / 64;  // EPJ and SPJ entries per lane and tile
@@ -570,6 +586,18 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int c
             a[k][3] -= mri;
         }
     };
+    // Acceleration-only accumulation (changeover neighbour pairs).
+    auto acc3 = [&](int k, float f, float dx, float dy, float dz) {
+        if constexpr (PK) {
+            b[k][0].x = fmaf(f, dx, b[k][0].x);
+            b[k][1].x = fmaf(f, dy, b[k][1].x);
+            b[k][2].x = fmaf(f, dz, b[k][2].x);
+        } else {
+            a[k][0] = fmaf(f, dx, a[k][0]);
+            a[k][1] = fmaf(f, dy, a[k][1]);
+            a[k][2] = fmaf(f, dz, a[k][2]);
+        }
+    };
     auto clear_acc = [&]() {
 #pragma unroll
         for (int k = 0; k < KI; ++k) {
@@ -641,11 +669,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int c
             if (nb && ci.id != cj.id) {
                 double d[5];
                 co_pair_diff(ei, ci, e, e.m, cj, p.eps2, rcut2d, d);
-                if constexpr (!PK) {
-                    a[k][0] += (float)d[0];
-                    a[k][1] += (float)d[1];
-                    a[k][2] += (float)d[2];
-                }
+                acc3(k, 1.f, (float)d[0], (float)d[1], (float)d[2]);
                 dt[k] += (float)d[3];
                 ds[k] += (float)d[4];
             }
@@ -702,9 +726,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int c
                             co_k_f32(r, use_i ? ci[k].r_in : cj.r_in, use_i ? ci[k].norm : cj.norm,
                                      use_i ? ci[k].coff : cj.coff, use_i ? ci[k].pot_off : cj.pot_off, kacc, kpot);
                             const float f = hh.w * kacc * (ri * ri * ri);
-                            a[k][0] = fmaf(f, dx, a[k][0]);
-                            a[k][1] = fmaf(f, dy, a[k][1]);
-                            a[k][2] = fmaf(f, dz, a[k][2]);
+                            acc3(k, f, dx, dy, dz);
                             const float meri = cj.mass * ri;
                             dt[k] -= meri;
                             ds[k] = fmaf(-meri, kpot, ds[k]);
@@ -1105,8 +1127,11 @@ cudaError_t launch_ws_search(const Params& p, cudaStream_t s, int num_sms) {
     return launch_ws_t<4, 3, 4, false, kModeSearch>(p, s, num_sms);
 }
 
+// Packed far and SP tiles, 128-entry EP tiles, 2 CTAs per SM: the fastest of
+// the changeover configurations timed on the 1M binary workload (26.7 ms,
+// against 30.3 ms for scalar 64-entry tiles at 3 CTAs per SM).
 cudaError_t launch_ws_changeover(const Params& p, cudaStream_t s, int num_sms) {
-    return launch_ws_t<4, 3, 3, false, kModeChangeover, 64, 4>(p, s, num_sms);
+    return launch_ws_t<4, 3, 2, true, kModeChangeover, 128, 4>(p, s, num_sms);
 }
 
 }  // namespace pgf

@@ -33,6 +33,15 @@ EP-EP acc/pot/n_ngb and EP-SP acc/pot, G-scaled as the functors write them.
     r_in, r_out), on random radii with separations below r_in, inside the
     changeover, beyond r_out and on both boundaries.
 
+``gradient_walks.npz``
+    The KDKDK_4TH gradient-correction pass (src/petar.hpp:1123-1140): the
+    reference's CalcCorrectEpEpWithLinearCutoffNoSimd (built with KDKDK_4TH into
+    ``libref_kdkdk.so``) and its quadrupole EP-SP functor, per walk, on a
+    4096-centre Plummer cluster with 30% binaries, eps = 1e-4, G = 0.9, and
+    accelerations from the Plummer potential's smooth field.  Outputs: acorr
+    (2 x the EP-EP sum, no G), acc (the i's own acc plus G x the SP
+    acceleration) and pot (G x the SP potential), as one FDPS walk writes them.
+
 Usage: python tests/golden/make_golden.py [fixture names]   (default: all)
 """
 from __future__ import annotations
@@ -167,6 +176,45 @@ def changeover_case(seed: int) -> dict:
                 acc0w_two=acc0w2, potw_two=potw2, m_fac=m_fac, r_in_mfac=rin_m, r_out_mfac=rout_m)
 
 
+def gradient_case(seed: int) -> dict:
+    """Walks and accelerations for the gradient-correction fixture."""
+    from petar_gb300 import ics, walks
+    cl = ics.make_plummer_cluster(seed, 4096, 0.015, binary_fraction=0.3, theta=0.3)
+    wb = walks.build_walks(cl)
+    b2 = (3.0 * np.pi / 16.0) ** 2  # Plummer scale length squared in Henon units
+    acc = -wb.epj_pos / ((wb.epj_pos ** 2).sum(1) + b2)[:, None] ** 1.5
+    return dict(epi_pos=wb.epi_pos, epi_rs=wb.epi_rs, epj_pos=wb.epj_pos, epj_mass=wb.epj_mass,
+                epj_rs=wb.epj_rs, spj_pos=wb.spj_pos, spj_mass=wb.spj_mass, spj_quad=wb.spj_quad,
+                epi_disp=wb.epi_disp, epj_disp=wb.epj_disp, id_epj=wb.id_epj, spj_disp=wb.spj_disp,
+                id_spj=wb.id_spj, eps=np.float64(1e-4), r_out=np.float64(cl.r_out), G=np.float64(0.9),
+                epi_acc=acc.copy(), epj_acc=acc.copy())
+
+
+def run_ref_gradient(case: dict) -> dict:
+    lib = _load("kdkdk")
+    vp, ci = ctypes.c_void_p, ctypes.c_int
+    lib.ref_correct.argtypes = [ci, vp, vp, ci, vp, vp, vp, vp, vp]
+    lib.ref_set_params(float(case["eps"]), float(case["r_out"]), float(case["G"]))
+    c = np.ascontiguousarray
+    out = {k: [] for k in ("acorr", "acc", "pot")}
+    for w in range(case["epi_disp"].size - 1):
+        i0, i1 = case["epi_disp"][w], case["epi_disp"][w + 1]
+        je = case["id_epj"][case["epj_disp"][w]:case["epj_disp"][w + 1]]
+        js = case["id_spj"][case["spj_disp"][w]:case["spj_disp"][w + 1]]
+        xi, ai = c(case["epi_pos"][i0:i1]), c(case["epi_acc"][i0:i1])
+        xj, mj, aj = c(case["epj_pos"][je]), c(case["epj_mass"][je]), c(case["epj_acc"][je])
+        ni = i1 - i0
+        acorr = np.zeros((ni, 3)); acc_i = np.zeros((ni, 3))
+        lib.ref_correct(ni, _p(xi), _p(ai), je.size, _p(xj), _p(mj), _p(aj), _p(acorr), _p(acc_i))
+        a_sp = np.zeros((ni, 3)); p_sp = np.zeros(ni)
+        if js.size:
+            # keep the gathered arrays referenced while the C call reads them
+            xs, ms, qs = c(case["spj_pos"][js]), c(case["spj_mass"][js]), c(case["spj_quad"][js])
+            lib.ref_epsp(ni, _p(xi), js.size, _p(xs), _p(ms), _p(qs), _p(a_sp), _p(p_sp))
+        out["acorr"].append(acorr); out["acc"].append(acc_i + a_sp); out["pot"].append(p_sp)
+    return {k: np.concatenate(v) for k, v in out.items()}
+
+
 def main() -> None:
     if not (REF_LIBS / "libref_nosimd.so").exists() or not (REF_LIBS / "libref_changeover.so").exists():
         subprocess.run([str(ROOT / "oracle" / "ref" / "build_ref.sh")], check=True)
@@ -175,7 +223,13 @@ def main() -> None:
     if not only or "changeover_w" in only:
         np.savez_compressed(HERE / "changeover_w.npz", **changeover_case(77))
         print("changeover_w")
-    if only and not only - {"changeover_w"}:
+    if not only or "gradient_walks" in only:
+        case = gradient_case(12)
+        payload = dict(case)
+        payload.update({f"ref__{k}": v for k, v in run_ref_gradient(case).items()})
+        np.savez_compressed(HERE / "gradient_walks.npz", **payload)
+        print("gradient_walks")
+    if only and not only - {"changeover_w", "gradient_walks"}:
         return
     cases = {
         "kernel_test": kernel_test_case(20240, rs_var=False),

@@ -48,9 +48,11 @@ def test_plummer65k_against_oracle_and_direct_sum():
     acc_d, pot_d = oracle.direct(cl.pos, cl.mass, wb.epi_index[rows], wb.eps2, wb.rcut2)
     e_gpu = rel_err_vec(res["acc"][rows], acc_d)
     e_tree = rel_err_vec(o["acc"][rows], acc_d)
+    # The kernel's own error (about 1e-7 against the oracle) shifts these
+    # statistics by no more than the mixed-precision tolerances.
     assert np.median(e_tree) < 2e-3
-    assert abs(np.median(e_gpu) - np.median(e_tree)) <= 1e-3 * np.median(e_tree)
-    assert abs(np.quantile(e_gpu, 0.999) - np.quantile(e_tree, 0.999)) <= 1e-2 * np.quantile(e_tree, 0.999)
+    assert abs(np.median(e_gpu) - np.median(e_tree)) <= MIXED_MEDIAN
+    assert abs(np.quantile(e_gpu, 0.999) - np.quantile(e_tree, 0.999)) <= MIXED_P999
 
 
 def test_king4m_sampled_walks():

@@ -142,3 +142,22 @@ def test_changeover_oracle_composition():
             assert np.abs(o["acc"][i] - want_acc).max() <= 1e-11 * scale
             assert abs(o["pot"][i] - want_pt) <= 1e-11 * (G * np.abs(pt).sum() + abs(base["pot_sp"][i]) + G * self_pot)
             assert abs(o["pot_soft"][i] - want_ps) <= 1e-11 * (G * np.abs(ps).sum() + abs(base["pot_sp"][i]) + G * self_pot)
+
+
+def _gradient_batch(d):
+    from petar_gb300.walks import WalkBatch
+    return WalkBatch(epi_pos=d["epi_pos"], epi_rs=d["epi_rs"], epi_disp=d["epi_disp"], epj_pos=d["epj_pos"],
+                     epj_mass=d["epj_mass"], epj_rs=d["epj_rs"], spj_pos=d["spj_pos"], spj_mass=d["spj_mass"],
+                     spj_quad=d["spj_quad"], epj_disp=d["epj_disp"], id_epj=d["id_epj"], spj_disp=d["spj_disp"],
+                     id_spj=d["id_spj"], eps2=float(d["eps"]) ** 2, rcut2=float(d["r_out"]) ** 2, G=float(d["G"]))
+
+
+def test_gradient_correction_matches_reference():
+    """The oracle's KDKDK_4TH gradient-correction pass against the reference's
+    CalcCorrectEpEpWithLinearCutoffNoSimd and quadrupole EP-SP functors
+    (compiled from source with KDKDK_4TH): bit-exact acorr, acc and pot."""
+    d = dict(np.load(GOLDEN / "gradient_walks.npz"))
+    o = oracle.gradient(_gradient_batch(d), d["epi_acc"], d["epj_acc"])
+    np.testing.assert_array_equal(o["acorr"], d["ref__acorr"])
+    np.testing.assert_array_equal(o["acc"], d["ref__acc"])
+    np.testing.assert_array_equal(o["pot"], d["ref__pot"])
