@@ -503,6 +503,20 @@ def run_ours(args):
                     "members_fraction": 0.1, "artificial_fraction": 0.05,
                     "parity": "tests/test_gpu_parity.py::test_changeover_mode_*"}
         modes["force_changeover"] = co_entry
+        # KDKDK_4TH gradient-correction pass, with the force pass's accelerations
+        acc = f_mixed["acc"]
+        rec_gr = gpuforce.Records(wb, acc=(acc, acc))
+        gpuforce.set_gradient_layout(rec_gr)
+        gpuforce.set_mode(gpuforce.PGF_MODE_GRADIENT)
+        try:
+            gpuforce.dispatch(rec_gr, tag=3)
+            gpuforce.retrieve(rec_gr, tag=3)
+            t = time_recompute(3)
+        finally:
+            gpuforce.set_mode(gpuforce.PGF_MODE_FORCE)
+            gpuforce.set_gradient_layout(None)
+        modes["gradient_kdkdk"] = {"ms_per_step": t, "value": n_int / t / 1e6, "unit": "Ginteractions/s",
+                                   "parity": "tests/test_gpu_parity.py::test_gradient_mode_*"}
 
     if rank != 0:
         torch.distributed.barrier()

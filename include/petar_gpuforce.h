@@ -58,9 +58,31 @@ enum {
     PGF_MODE_NEIGHBOR_SEARCH = 1, /* n_ngb only, as SearchNeighborEpEpNoSimd
                                      (src/soft_force.hpp:11-34): r^2 < max(rs_i, rs_j)^2
                                      without softening; SPJ lists are ignored */
-    PGF_MODE_FORCE_CHANGEOVER = 2 /* soft force with the changeover correction of
+    PGF_MODE_FORCE_CHANGEOVER = 2, /* soft force with the changeover correction of
                                      neighbours fused in (see pgf_set_changeover_layout) */
+    PGF_MODE_GRADIENT = 3         /* KDKDK_4TH gradient-correction pass (see
+                                     pgf_set_gradient_layout) */
 };
+
+/* KDKDK_4TH gradient-correction pass (src/petar.hpp:1123-1140), run on the CPU
+ * by the reference: per i, CalcCorrectEpEpWithLinearCutoffNoSimd
+ * (src/soft_force.hpp:89-122) over the EPJ list and the quadrupole force over
+ * the SPJ list, into one cleared ForceSoft:
+ *   acorr = 2 sum_j -m_j / r^3 (da - 3 (dr.da) / r^2 dr)  (no G; dr = x_i - x_j,
+ *           da = a_i - a_j, r^2 = max(|dr|^2 + eps^2, r_out^2)),
+ *   acc = a_i + G acc_sp, pot = G pot_sp, n_ngb = 0.
+ * The EPI and EPJ records carry the particle's acceleration (EPISoft::acc,
+ * EPJSoft::acc under KDKDK_4TH) and the Force record acorr, at these byte
+ * offsets (three F64 each).  Set the layout before the send. */
+typedef struct pgf_gradient_layout {
+    size_t epi_off_acc;
+    size_t epj_off_acc;
+    size_t force_off_acorr;
+} pgf_gradient_layout;
+
+/* Sets (or with NULL clears) the layout of the gradient mode.  No
+ * counterpart in the reference, whose pass runs on the CPU. */
+int pgf_set_gradient_layout(const pgf_gradient_layout *layout);
 
 /* Fused changeover mode.  PeTar corrects the soft force on the CPU after the
  * kernel: for every tree neighbour j of i, calcAccPotShortWithLinearCutoff

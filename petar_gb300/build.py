@@ -59,6 +59,7 @@ GPU_SOURCES = [
     "gpuforce/pgf_kernels_mixed.cu",
     "gpuforce/pgf_kernels_ws.cu",
     "gpuforce/pgf_noalloc.cu",
+    "gpuforce/pgf_kernels_gradient.cu",
 ]
 GPU_HEADERS = [
     "gpuforce/pgf_internal.cuh",

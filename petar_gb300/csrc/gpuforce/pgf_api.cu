@@ -123,6 +123,10 @@ struct TagState {
     HostBuf<CoRec> h_epi_co;
     DevBuf<double> pot_soft;
     HostBuf<double> h_pot_soft;
+    DevBuf<Accp> epi_acc;  // gradient mode: EPI accelerations in, acorr out
+    HostBuf<Accp> h_epi_acc;
+    DevBuf<Accp> acorr;
+    HostBuf<Accp> h_acorr;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     // Pipelined dispatch, per stage: copy start/end, main kernel start/end,
     // stage done (after the re-test kernel).
@@ -158,6 +162,11 @@ struct State {
     bool j_co_sent = false;  // the last send packed the EPJ changeover records
     DevBuf<CoRec> epj_co;
     HostBuf<CoRec> h_epj_co;
+    bool gr_set = false;  // gradient layout given (pgf_set_gradient_layout)
+    pgf_gradient_layout gr{};
+    bool j_gr_sent = false;
+    DevBuf<AccF32> epj_acc32;
+    HostBuf<AccF32> h_epj_acc32;
     HostBuf<EpjMix> h_epj;
     HostBuf<double> h_epj_m64, h_epj_rs64;
     HostBuf<SpjMix> h_spj;
@@ -288,6 +297,25 @@ int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, co
     PGF_CUDA(g.epj32.ensure(n_epj));
     PGF_CUDA(g.spj32.ensure(n_spj));
     g.j_co_sent = false;
+    g.j_gr_sent = false;
+    if (g.gr_set && n_epj > 0) {
+        PGF_CUDA(g.h_epj_acc32.ensure(n_epj));
+        PGF_CUDA(g.epj_acc32.ensure(n_epj));
+#pragma omp parallel for schedule(static)
+        for (int64_t j = 0; j < n_epj; ++j) {
+            const char* r = reinterpret_cast<const char*>(epj) + j * el->size;
+            const double* a = dptr(r, g.gr.epj_off_acc);
+            AccF32 o;
+            o.xh = (float)a[0];
+            o.yh = (float)a[1];
+            o.zh = (float)a[2];
+            o.xl = (float)(a[0] - (double)o.xh);
+            o.yl = (float)(a[1] - (double)o.yh);
+            o.zl = (float)(a[2] - (double)o.zh);
+            o.pad0 = o.pad1 = 0.f;
+            g.h_epj_acc32.h[j] = o;
+        }
+    }
     if (g.co_set && n_epj > 0) {
         PGF_CUDA(g.h_epj_co.ensure(n_epj));
         PGF_CUDA(g.epj_co.ensure(n_epj));
@@ -363,6 +391,11 @@ int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, co
         PGF_CUDA(cudaMemcpyAsync(g.epj_co.d, g.h_epj_co.h, n_epj * sizeof(CoRec), cudaMemcpyHostToDevice, g.stream));
         g.j_co_sent = true;
     }
+    if (g.gr_set && n_epj > 0) {
+        PGF_CUDA(cudaMemcpyAsync(g.epj_acc32.d, g.h_epj_acc32.h, n_epj * sizeof(AccF32), cudaMemcpyHostToDevice,
+                                 g.stream));
+        g.j_gr_sent = true;
+    }
     {
         const cudaError_t e = launch_split_j(g.epj.d, n_epj, g.epj32.d, g.spj.d, n_spj, g.spj32.d, g.stream);
         if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "j split kernel failed: %s", cudaGetErrorString(e));
@@ -402,7 +435,10 @@ void bind_scratch(Params& p, int stage = -1, int n_stages = 1) {
 int launch_kernels(const TagState& t, const Params& p, cudaStream_t s, cudaEvent_t ev_start, cudaEvent_t ev_end) {
     PGF_CUDA(cudaEventRecord(ev_start, s));
     cudaError_t e;
-    if (t.mode == PGF_MODE_FORCE_CHANGEOVER) {
+    if (t.mode == PGF_MODE_GRADIENT) {
+        e = launch_gradient(p, s, g.num_sms);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_end, s);
+    } else if (t.mode == PGF_MODE_FORCE_CHANGEOVER) {
         e = launch_ws_changeover(p, s, g.num_sms);
         if (e == cudaSuccess) e = cudaEventRecord(ev_end, s);
         if (e == cudaSuccess && p.n_walk > 0) e = launch_retest(p, s, g.num_sms);
@@ -482,6 +518,10 @@ bool pack_walk(TagState& t, int k, int w, const Slot3& o, const void* const* epi
         const double* p = dptr(r, il->off_pos);
         EpiDev e{p[0], p[1], p[2], *dptr(r, il->off_r_search)};
         t.h_epi.h[o.i + i] = e;
+        if (t.mode == PGF_MODE_GRADIENT) {
+            const double* a = dptr(r, g.gr.epi_off_acc);
+            t.h_epi_acc.h[o.i + i] = Accp{a[0], a[1], a[2], 0.0};
+        }
         if (t.mode == PGF_MODE_FORCE_CHANGEOVER) {
             const pgf_changeover_layout& L = g.co;
             t.h_epi_co.h[o.i + i] = make_co(*dptr(r, L.epi_off_r_in), *dptr(r, L.epi_off_r_out),
@@ -587,7 +627,16 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     if (co_mode && !g.co_set) return fail(PGF_ERR_STATE, "changeover mode without pgf_set_changeover_layout");
     if (co_mode && ne > 0 && !g.j_co_sent)
         return fail(PGF_ERR_STATE, "changeover mode: the EPJ array was sent before the changeover layout was set");
+    const bool gr_mode = g.mode == PGF_MODE_GRADIENT;
+    if (gr_mode && !g.gr_set) return fail(PGF_ERR_STATE, "gradient mode without pgf_set_gradient_layout");
+    if (gr_mode && ne > 0 && !g.j_gr_sent)
+        return fail(PGF_ERR_STATE, "gradient mode: the EPJ array was sent before the gradient layout was set");
     t.mode = g.mode;
+    if (gr_mode) {
+        PGF_CUDA(t.h_epi_acc.ensure(ni));
+        PGF_CUDA(t.epi_acc.ensure(ni));
+        PGF_CUDA(t.acorr.ensure(ni));
+    }
     if (co_mode) {
         PGF_CUDA(t.h_epi_co.ensure(ni));
         PGF_CUDA(t.epi_co.ensure(ni));
@@ -633,6 +682,11 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     p.spj_q64 = g.spj_q64.d;
     p.epj32 = g.epj32.d;
     p.spj32 = g.spj32.d;
+    if (gr_mode) {
+        p.epj_acc32 = g.epj_acc32.d;
+        p.epi_acc64 = t.epi_acc.d;
+        p.out_acorr = t.acorr.d;
+    }
     if (co_mode) {
         p.epj_co = g.epj_co.d;
         p.epi_co = t.epi_co.d;
@@ -669,6 +723,9 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
         const Slot3 a = off[k0], b = off[k1];
         if (b.i > a.i)
             PGF_CUDA(cudaMemcpyAsync(t.epi.d + a.i, t.h_epi.h + a.i, (b.i - a.i) * sizeof(EpiDev),
+                                     cudaMemcpyHostToDevice, s));
+        if (b.i > a.i && gr_mode)
+            PGF_CUDA(cudaMemcpyAsync(t.epi_acc.d + a.i, t.h_epi_acc.h + a.i, (b.i - a.i) * sizeof(Accp),
                                      cudaMemcpyHostToDevice, s));
         if (b.i > a.i && co_mode)
             PGF_CUDA(cudaMemcpyAsync(t.epi_co.d + a.i, t.h_epi_co.h + a.i, (b.i - a.i) * sizeof(CoRec),
@@ -882,9 +939,20 @@ int pgf_set_kernel_variant(int variant) {
 }
 
 int pgf_set_mode(int mode) {
-    if (mode != PGF_MODE_FORCE && mode != PGF_MODE_NEIGHBOR_SEARCH && mode != PGF_MODE_FORCE_CHANGEOVER)
+    if (mode != PGF_MODE_FORCE && mode != PGF_MODE_NEIGHBOR_SEARCH && mode != PGF_MODE_FORCE_CHANGEOVER &&
+        mode != PGF_MODE_GRADIENT)
         return fail(PGF_ERR_ARG, "unknown mode %d", mode);
     g.mode = mode;
+    return PGF_OK;
+}
+
+int pgf_set_gradient_layout(const pgf_gradient_layout* layout) {
+    if (!layout) {
+        g.gr_set = false;
+        return PGF_OK;
+    }
+    g.gr = *layout;
+    g.gr_set = true;
     return PGF_OK;
 }
 
@@ -968,6 +1036,10 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
     if (n) {
         PGF_CUDA(cudaMemcpyAsync(t.h_accp.h, t.accp.d, n * sizeof(Accp), cudaMemcpyDeviceToHost, s));
         PGF_CUDA(cudaMemcpyAsync(t.h_nnb.h, t.nnb.d, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        if (t.mode == PGF_MODE_GRADIENT) {
+            PGF_CUDA(t.h_acorr.ensure(n));
+            PGF_CUDA(cudaMemcpyAsync(t.h_acorr.h, t.acorr.d, n * sizeof(Accp), cudaMemcpyDeviceToHost, s));
+        }
         if (t.mode == PGF_MODE_FORCE_CHANGEOVER) {
             PGF_CUDA(t.h_pot_soft.ensure(n));
             PGF_CUDA(cudaMemcpyAsync(t.h_pot_soft.h, t.pot_soft.d, n * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1001,6 +1073,13 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
                 *reinterpret_cast<double*>(r + fl->off_pot) = a.w;
                 if (t.mode == PGF_MODE_FORCE_CHANGEOVER)
                     *reinterpret_cast<double*>(r + g.co.force_off_pot_soft) = t.h_pot_soft.h[o + i];
+                if (t.mode == PGF_MODE_GRADIENT) {
+                    double* ac = reinterpret_cast<double*>(r + g.gr.force_off_acorr);
+                    const Accp c = t.h_acorr.h[o + i];
+                    ac[0] = c.x;
+                    ac[1] = c.y;
+                    ac[2] = c.z;
+                }
             }
             if (fl->n_ngb_bytes == 8)
                 *reinterpret_cast<int64_t*>(r + fl->off_n_ngb) = t.h_nnb.h[o + i];
@@ -1065,6 +1144,10 @@ int pgf_finalize(void) {
         t.h_epi_co.release();
         t.pot_soft.release();
         t.h_pot_soft.release();
+        t.epi_acc.release();
+        t.h_epi_acc.release();
+        t.acorr.release();
+        t.h_acorr.release();
         for (auto& ev : t.ev) {
             if (ev) cudaEventDestroy(ev);
             ev = nullptr;
@@ -1087,6 +1170,9 @@ int pgf_finalize(void) {
     g.epj_co.release();
     g.h_epj_co.release();
     g.j_co_sent = false;
+    g.epj_acc32.release();
+    g.h_epj_acc32.release();
+    g.j_gr_sent = false;
     g.h_epj.release();
     g.h_epj_m64.release();
     g.h_epj_rs64.release();

@@ -62,6 +62,15 @@ struct __align__(32) SpjF32 {
 };
 static_assert(sizeof(SpjF32) == 64, "SpjF32 layout");
 
+// Acceleration of one EPJ as an FP32 (hi, lo) pair (KDKDK_4TH gradient mode):
+// differences a_j - a_i are formed from both halves, accurate to an ulp of
+// the difference itself.
+struct __align__(32) AccF32 {
+    float xh, yh, zh, pad0;
+    float xl, yl, zl, pad1;
+};
+static_assert(sizeof(AccF32) == 32, "AccF32 layout");
+
 // Changeover data of one particle for the fused changeover mode: the
 // ChangeOver members of src/changeover.hpp:8-14 (r_in, r_out, norm =
 // 1/(r_out - r_in), coff = (r_out - r_in)/(r_out + r_in), pot_off =
@@ -130,6 +139,9 @@ struct Params {
     const CoRec* epj_co;   // fused changeover mode only (else null)
     const CoRec* epi_co;
     double* out_pot_soft;  // fused changeover mode: soft potential (G applied)
+    const AccF32* epj_acc32;  // gradient mode: EPJ accelerations (hi, lo)
+    const Accp* epi_acc64;    // gradient mode: EPI accelerations (x, y, z; w unused)
+    Accp* out_acorr;          // gradient mode: acorr (no G; w unused)
     const int32_t* id_epj;
     const int32_t* id_spj;
     const WalkDesc* walks;
@@ -208,5 +220,7 @@ cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant)
 cudaError_t launch_ws_search(const Params& p, cudaStream_t s, int num_sms);
 // Soft force with the changeover correction of neighbours fused in.
 cudaError_t launch_ws_changeover(const Params& p, cudaStream_t s, int num_sms);
+// KDKDK_4TH gradient-correction pass (pgf_kernels_gradient.cu).
+cudaError_t launch_gradient(const Params& p, cudaStream_t s, int num_sms);
 
 }  // namespace pgf

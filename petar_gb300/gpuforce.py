@@ -30,6 +30,7 @@ NUM_KERNEL_VARIANTS = 9  # PGF_NUM_KERNEL_VARIANTS
 PGF_MODE_FORCE = 0
 PGF_MODE_NEIGHBOR_SEARCH = 1
 PGF_MODE_FORCE_CHANGEOVER = 2
+PGF_MODE_GRADIENT = 3
 
 # PeTar's EPISoft (src/soft_ptcl.hpp:271-308): id, pos, r_search, rank_org, type.
 EPI_DTYPE = np.dtype([("id", "<i8"), ("pos", "<f8", 3), ("r_search", "<f8"), ("rank_org", "<i4"),
@@ -48,6 +49,16 @@ FORCE_DTYPE = np.dtype([("acc", "<f8", 3), ("pot", "<f8"), ("n_ngb", "<i8")], al
 EPI_CO_DTYPE = np.dtype([("id", "<i8"), ("pos", "<f8", 3), ("r_search", "<f8"), ("rank_org", "<i4"),
                          ("type", "<i4"), ("r_in", "<f8"), ("r_out", "<f8"), ("self_mass", "<f8")], align=True)
 FORCE_CO_DTYPE = np.dtype([("acc", "<f8", 3), ("pot", "<f8"), ("n_ngb", "<i8"), ("pot_soft", "<f8")],
+                          align=True)
+# KDKDK_4TH builds of PeTar: EPISoft and EPJSoft carry acc, ForceSoft acorr
+# (src/soft_ptcl.hpp:4-30, 271-345).
+EPI_GR_DTYPE = np.dtype([("id", "<i8"), ("pos", "<f8", 3), ("r_search", "<f8"), ("rank_org", "<i4"),
+                         ("type", "<i4"), ("acc", "<f8", 3)], align=True)
+EPJ_GR_DTYPE = np.dtype([("id", "<i8"), ("mass", "<f8"), ("pos", "<f8", 3), ("vel", "<f8", 3),
+                         ("acc", "<f8", 3), ("r_in", "<f8"), ("r_out", "<f8"), ("r_search", "<f8"),
+                         ("r_scale_next", "<f8"), ("group_data", "<i8", 2), ("rank_org", "<i4"),
+                         ("adr_org", "<i4")], align=True)
+FORCE_GR_DTYPE = np.dtype([("acc", "<f8", 3), ("pot", "<f8"), ("acorr", "<f8", 3), ("n_ngb", "<i8")],
                           align=True)
 
 
@@ -75,6 +86,11 @@ class _ChangeoverLayout(ctypes.Structure):
     _fields_ = [(k, ctypes.c_size_t) for k in (
         "epi_off_id", "epi_off_r_in", "epi_off_r_out", "epi_off_self_mass", "epj_off_id", "epj_off_r_in",
         "epj_off_r_out", "epj_off_mass_backup", "epj_off_status", "force_off_pot_soft")]
+
+
+class _GradientLayout(ctypes.Structure):
+    _fields_ = [("epi_off_acc", ctypes.c_size_t), ("epj_off_acc", ctypes.c_size_t),
+                ("force_off_acorr", ctypes.c_size_t)]
 
 
 class _ForceLayout(ctypes.Structure):
@@ -141,6 +157,7 @@ def load(build: bool = True) -> ctypes.CDLL:
         "pgf_set_dispatch_stages": [ci],
         "pgf_set_mode": [ci],
         "pgf_set_changeover_layout": [vp],
+        "pgf_set_gradient_layout": [vp],
         "pgf_get_kernel_variant": [vp],
         "pgf_autotune": [ci, ci, vp, vp],
         "pgf_wait": [ci],
@@ -333,21 +350,27 @@ class Records:
     """A WalkBatch converted to PeTar-layout record arrays plus the per-walk
     pointer tables the functors take."""
 
-    def __init__(self, batch, co=None):
+    def __init__(self, batch, co=None, acc=None):
         """co: a walks.ChangeoverSet for the fused changeover mode (extended
-        EPI and Force records; EPJ ids, radii and group_data filled in)."""
+        EPI and Force records; EPJ ids, radii and group_data filled in).
+        acc: (epi_acc, epj_acc) for the KDKDK_4TH gradient mode (records of a
+        KDKDK_4TH build)."""
         ni = batch.epi_rs.size
-        self.epi = np.zeros(ni, EPI_CO_DTYPE if co is not None else EPI_DTYPE)
+        gr = acc is not None
+        self.epi = np.zeros(ni, EPI_CO_DTYPE if co is not None else (EPI_GR_DTYPE if gr else EPI_DTYPE))
         self.epi["pos"] = batch.epi_pos
         self.epi["r_search"] = batch.epi_rs
         self.epi["type"] = 1
         self.epi["id"] = np.arange(ni)
-        self.epj = np.zeros(batch.epj_mass.size, EPJ_DTYPE)
+        self.epj = np.zeros(batch.epj_mass.size, EPJ_GR_DTYPE if gr else EPJ_DTYPE)
         self.epj["mass"] = batch.epj_mass
         self.epj["pos"] = batch.epj_pos
         self.epj["r_search"] = batch.epj_rs
         self.epj["id"] = np.arange(batch.epj_mass.size)
         self.co = co
+        if gr:
+            self.epi["acc"] = acc[0]
+            self.epj["acc"] = acc[1]
         if co is not None:
             self.epi["id"] = co.epi_id
             self.epi["r_in"] = co.epi_r_in
@@ -364,7 +387,7 @@ class Records:
         self.spj["mass"] = batch.spj_mass
         self.spj["pos"] = batch.spj_pos
         self.spj["quad"] = batch.spj_quad
-        self.force = np.zeros(ni, FORCE_CO_DTYPE if co is not None else FORCE_DTYPE)
+        self.force = np.zeros(ni, FORCE_CO_DTYPE if co is not None else (FORCE_GR_DTYPE if gr else FORCE_DTYPE))
         self.id_epj = np.ascontiguousarray(batch.id_epj, dtype=np.int32)
         self.id_spj = np.ascontiguousarray(batch.id_spj, dtype=np.int32)
         self.n_walk = batch.n_walk
@@ -460,3 +483,28 @@ def compute_changeover(batch, co, rec: Records | None = None) -> dict:
         set_mode(PGF_MODE_FORCE)
         set_changeover_layout(None)
     return dict(acc=f["acc"].copy(), pot=f["pot"].copy(), pot_soft=f["pot_soft"].copy(), nnb=f["n_ngb"].copy())
+
+
+def set_gradient_layout(rec: Records | None) -> None:
+    """Sets (rec built with accelerations) or clears (None) the gradient layout."""
+    if rec is None:
+        _check(load().pgf_set_gradient_layout(None))
+        return
+    lay = _GradientLayout(rec.epi.dtype.fields["acc"][1], rec.epj.dtype.fields["acc"][1],
+                          rec.force.dtype.fields["acorr"][1])
+    _check(load().pgf_set_gradient_layout(ctypes.byref(lay)))
+
+
+def compute_gradient(batch, epi_acc, epj_acc, rec: Records | None = None) -> dict:
+    """acorr, acc and pot of every EPI row from the KDKDK_4TH gradient pass
+    through the C ABI."""
+    rec = rec if rec is not None else Records(batch, acc=(epi_acc, epj_acc))
+    set_gradient_layout(rec)
+    set_mode(PGF_MODE_GRADIENT)
+    try:
+        dispatch(rec)
+        f = retrieve(rec)
+    finally:
+        set_mode(PGF_MODE_FORCE)
+        set_gradient_layout(None)
+    return dict(acorr=f["acorr"].copy(), acc=f["acc"].copy(), pot=f["pot"].copy(), nnb=f["n_ngb"].copy())

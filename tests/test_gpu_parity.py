@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import load_golden, rel_err, rel_err_vec, stats
+from helpers import GOLDEN, load_golden, rel_err, rel_err_vec, stats
 from petar_gb300 import gpuforce, ics, walks
 from petar_gb300.gpuforce import PGF_PRECISION_FP64, PGF_PRECISION_MIXED
 
@@ -427,3 +427,34 @@ def test_changeover_mode_pipelined_and_without_layout():
         assert e.value.code == 4
     finally:
         gpuforce.set_mode(gpuforce.PGF_MODE_FORCE)
+
+
+def _gradient_check(res, o, label):
+    for key, e in (("acorr", rel_err_vec(res["acorr"], o["acorr"])), ("acc", rel_err_vec(res["acc"], o["acc"])),
+                   ("pot", rel_err(res["pot"], o["pot"]))):
+        st = stats(e)
+        assert st["median"] <= MIXED_MEDIAN and st["p999"] <= MIXED_P999 and st["max"] <= MIXED_MAX, (label, key, st)
+    assert (res["nnb"] == 0).all()
+
+
+def test_gradient_mode_golden():
+    """KDKDK_4TH gradient pass on the fixture whose outputs the reference's
+    own functors (built with KDKDK_4TH) produced."""
+    d = dict(np.load(GOLDEN / "gradient_walks.npz"))
+    wb = walks.WalkBatch(epi_pos=d["epi_pos"], epi_rs=d["epi_rs"], epi_disp=d["epi_disp"], epj_pos=d["epj_pos"],
+                         epj_mass=d["epj_mass"], epj_rs=d["epj_rs"], spj_pos=d["spj_pos"], spj_mass=d["spj_mass"],
+                         spj_quad=d["spj_quad"], epj_disp=d["epj_disp"], id_epj=d["id_epj"],
+                         spj_disp=d["spj_disp"], id_spj=d["id_spj"], eps2=float(d["eps"]) ** 2,
+                         rcut2=float(d["r_out"]) ** 2, G=float(d["G"]))
+    res = gpuforce.compute_gradient(wb, d["epi_acc"], d["epj_acc"])
+    _gradient_check(res, dict(acorr=d["ref__acorr"], acc=d["ref__acc"], pot=d["ref__pot"]), "golden")
+
+
+def test_gradient_mode_binaries_with_true_accelerations():
+    """Binary-rich cluster with each particle's own soft acceleration as a_i
+    (binary companions pull hard, so a_i - a_j spans many orders)."""
+    cl = ics.make_plummer_cluster(34, 20000, 0.004, binary_fraction=0.5)
+    wb = walks.build_walks(cl)
+    acc = oracle.force(wb)["acc"]
+    res = gpuforce.compute_gradient(wb, acc, acc)
+    _gradient_check(res, oracle.gradient(wb, acc, acc), "binaries")
