@@ -129,9 +129,12 @@ struct TagState {
     HostBuf<Accp> h_acorr;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     // Pipelined dispatch, per stage: copy start/end, main kernel start/end,
-    // stage done (after the re-test kernel).
-    cudaEvent_t evc[kMaxChunks][5] = {};
+    // stage done (after the re-test kernel), results copied back.
+    cudaEvent_t evc[kMaxChunks][6] = {};
     int n_chunks = 0;  // stages of the last dispatch (0: a single launch)
+    std::vector<int32_t> ord;  // layout position -> walk
+    std::vector<int> stage_k;  // stage boundaries in layout positions
+    std::vector<int64_t> stage_i;  // and in EPI rows
     bool times_pending = false;  // kernel events recorded, not yet added to the profile
     Params params{};
 };
@@ -144,6 +147,7 @@ struct State {
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // host-to-device copies of pipelined dispatches
     cudaStream_t stage_stream[kMaxChunks] = {};  // kernels of pipeline stages
+    cudaStream_t d2h_stream = nullptr;             // results of pipeline stages back
     bool user_stream = false;
     double eps2 = 0, rcut2 = 0, G = 1;
     int precision = PGF_PRECISION_MIXED;
@@ -211,6 +215,7 @@ int setup_device(int rank) {
     PGF_CUDA(cudaStreamCreateWithFlags(&g.own_stream, cudaStreamNonBlocking));
     PGF_CUDA(cudaStreamCreateWithFlags(&g.copy_stream, cudaStreamNonBlocking));
     for (auto& st : g.stage_stream) PGF_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    PGF_CUDA(cudaStreamCreateWithFlags(&g.d2h_stream, cudaStreamNonBlocking));
     if (!g.user_stream) g.stream = g.own_stream;
     PGF_CUDA(cudaEventCreate(&g.ev_send0));
     PGF_CUDA(cudaEventCreate(&g.ev_send1));
@@ -655,14 +660,15 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     PGF_CUDA(t.accp.ensure(ni));
     PGF_CUDA(t.nnb.ensure(ni));
 
-    // Stages: contiguous ranges of the sorted layout with about equal numbers
-    // of list entries.
+    // Stages: contiguous ranges of the sorted layout.  The first has half the
+    // list entries of the others, so the GPU starts sooner; the rest share
+    // the remainder equally.
     int n_chunks = g.stages > 0 ? g.stages : (int)std::min<int64_t>(kMaxChunks, (ne + ns) / kChunkIdEntries + 1);
     if (n_walk < 8 * n_chunks) n_chunks = 1;
     std::vector<int> cb(n_chunks + 1, n_walk);
     cb[0] = 0;
     for (int c = 1, k = 0; c < n_chunks; ++c) {
-        const int64_t target = (ne + ns) * c / n_chunks;
+        const int64_t target = (ne + ns) * (2 * c - 1) / (2 * n_chunks - 1);
         while (k < n_walk && off[k].e + off[k].s < target) ++k;
         cb[c] = k;
     }
@@ -799,6 +805,10 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     }
     PGF_CUDA(cudaEventRecord(t.ev[3], g.stream));
     g.prof.copy += pack_s;
+    t.ord = ord;
+    t.stage_k = cb;
+    t.stage_i.resize(n_chunks + 1);
+    for (int c = 0; c <= n_chunks; ++c) t.stage_i[c] = off[cb[c]].i;
     t.n_chunks = n_chunks;
     t.dispatched = true;
     t.has_data = true;
@@ -1014,6 +1024,50 @@ int pgf_autotune(int tag, int repeats, int* best_variant, double* best_ms) {
     return PGF_OK;
 }
 
+// Writes the results of walk w into the caller's records.
+void unpack_walk(const TagState& t, int w, const int* ni, void* const* force, const pgf_force_layout* fl) {
+    char* base = reinterpret_cast<char*>(force[w]);
+    const int64_t o = t.epi_disp[w];
+    for (int i = 0; i < ni[w]; ++i) {
+        char* r = base + (size_t)i * fl->size;
+        if (t.mode != PGF_MODE_NEIGHBOR_SEARCH) {
+            const Accp a = t.h_accp.h[o + i];
+            double* acc = reinterpret_cast<double*>(r + fl->off_acc);
+            acc[0] = a.x;
+            acc[1] = a.y;
+            acc[2] = a.z;
+            *reinterpret_cast<double*>(r + fl->off_pot) = a.w;
+            if (t.mode == PGF_MODE_FORCE_CHANGEOVER)
+                *reinterpret_cast<double*>(r + g.co.force_off_pot_soft) = t.h_pot_soft.h[o + i];
+            if (t.mode == PGF_MODE_GRADIENT) {
+                double* ac = reinterpret_cast<double*>(r + g.gr.force_off_acorr);
+                const Accp c = t.h_acorr.h[o + i];
+                ac[0] = c.x;
+                ac[1] = c.y;
+                ac[2] = c.z;
+            }
+        }
+        if (fl->n_ngb_bytes == 8)
+            *reinterpret_cast<int64_t*>(r + fl->off_n_ngb) = t.h_nnb.h[o + i];
+        else
+            *reinterpret_cast<int32_t*>(r + fl->off_n_ngb) = t.h_nnb.h[o + i];
+    }
+}
+
+// D2H copies of the result rows [r0, r1) on stream s.
+int copy_back(TagState& t, int64_t r0, int64_t r1, cudaStream_t s) {
+    if (r1 <= r0) return PGF_OK;
+    const int64_t n = r1 - r0;
+    PGF_CUDA(cudaMemcpyAsync(t.h_accp.h + r0, t.accp.d + r0, n * sizeof(Accp), cudaMemcpyDeviceToHost, s));
+    PGF_CUDA(cudaMemcpyAsync(t.h_nnb.h + r0, t.nnb.d + r0, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    if (t.mode == PGF_MODE_GRADIENT)
+        PGF_CUDA(cudaMemcpyAsync(t.h_acorr.h + r0, t.acorr.d + r0, n * sizeof(Accp), cudaMemcpyDeviceToHost, s));
+    if (t.mode == PGF_MODE_FORCE_CHANGEOVER)
+        PGF_CUDA(cudaMemcpyAsync(t.h_pot_soft.h + r0, t.pot_soft.d + r0, n * sizeof(double), cudaMemcpyDeviceToHost,
+                                 s));
+    return PGF_OK;
+}
+
 int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const pgf_force_layout* fl) {
     if (int r = ensure_init()) return r;
     if (!valid_tag(tag)) return fail(PGF_ERR_ARG, "tag %d outside [0, %d)", tag, kMaxTags);
@@ -1031,20 +1085,48 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
     PGF_CUDA(t.h_accp.ensure(n));
     PGF_CUDA(t.h_nnb.ensure(n));
     PGF_CUDA(t.h_flags.ensure(4));
+    if (t.mode == PGF_MODE_GRADIENT) PGF_CUDA(t.h_acorr.ensure(n));
+    if (t.mode == PGF_MODE_FORCE_CHANGEOVER) PGF_CUDA(t.h_pot_soft.ensure(n));
+    if (t.n_chunks > 0) {
+        // Pipelined dispatch: copy back and unpack each stage as soon as its
+        // kernels are done, while later stages still run.
+        cudaStream_t ds = g.d2h_stream;
+        for (int c = 0; c < t.n_chunks; ++c) {
+            PGF_CUDA(cudaStreamWaitEvent(ds, t.evc[c][4], 0));
+            if (c == 0) PGF_CUDA(cudaEventRecord(t.ev[4], ds));
+            if (int r = copy_back(t, t.stage_i[c], t.stage_i[c + 1], ds)) return r;
+            PGF_CUDA(cudaEventRecord(t.evc[c][5], ds));
+        }
+        // g.stream already waits for every stage; the flags follow them.
+        PGF_CUDA(cudaStreamWaitEvent(ds, t.ev[3], 0));
+        PGF_CUDA(cudaMemcpyAsync(t.h_flags.h, g.scratch.d, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, ds));
+        PGF_CUDA(cudaMemsetAsync(g.scratch.d + 2, 0, 2 * sizeof(int32_t), ds));
+        PGF_CUDA(cudaEventRecord(t.ev[5], ds));
+        PGF_CUDA(cudaStreamWaitEvent(g.stream, t.ev[5], 0));  // later work follows the memset
+        double unpack_s = 0.0;
+        for (int c = 0; c < t.n_chunks; ++c) {
+            PGF_CUDA(cudaEventSynchronize(t.evc[c][5]));
+            const double t0 = now_s();
+            const int k0 = t.stage_k[c], k1 = t.stage_k[c + 1];
+#pragma omp parallel for schedule(dynamic, 8)
+            for (int k = k0; k < k1; ++k) unpack_walk(t, t.ord[k], ni, force, fl);
+            unpack_s += now_s() - t0;
+        }
+        PGF_CUDA(cudaEventSynchronize(t.ev[5]));
+        t.dispatched = false;
+        harvest_times(t);
+        harvest_send();
+        float ms_recv = 0;
+        cudaEventElapsedTime(&ms_recv, t.ev[4], t.ev[5]);
+        g.prof.recv += 1e-3 * ms_recv;
+        g.prof.n_retest += t.h_flags.h[3];
+        g.prof.copy += unpack_s;
+        if (t.h_flags.h[2] != 0) return fail(PGF_ERR_DEVICE, "device error word %d", t.h_flags.h[2]);
+        return PGF_OK;
+    }
     cudaStream_t s = g.stream;
     PGF_CUDA(cudaEventRecord(t.ev[4], s));
-    if (n) {
-        PGF_CUDA(cudaMemcpyAsync(t.h_accp.h, t.accp.d, n * sizeof(Accp), cudaMemcpyDeviceToHost, s));
-        PGF_CUDA(cudaMemcpyAsync(t.h_nnb.h, t.nnb.d, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-        if (t.mode == PGF_MODE_GRADIENT) {
-            PGF_CUDA(t.h_acorr.ensure(n));
-            PGF_CUDA(cudaMemcpyAsync(t.h_acorr.h, t.acorr.d, n * sizeof(Accp), cudaMemcpyDeviceToHost, s));
-        }
-        if (t.mode == PGF_MODE_FORCE_CHANGEOVER) {
-            PGF_CUDA(t.h_pot_soft.ensure(n));
-            PGF_CUDA(cudaMemcpyAsync(t.h_pot_soft.h, t.pot_soft.d, n * sizeof(double), cudaMemcpyDeviceToHost, s));
-        }
-    }
+    if (int r = copy_back(t, 0, n, s)) return r;
     PGF_CUDA(cudaMemcpyAsync(t.h_flags.h, g.scratch.d, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     PGF_CUDA(cudaMemsetAsync(g.scratch.d + 2, 0, 2 * sizeof(int32_t), s));
     PGF_CUDA(cudaEventRecord(t.ev[5], s));
@@ -1059,34 +1141,7 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
     if (t.h_flags.h[2] != 0) return fail(PGF_ERR_DEVICE, "device error word %d", t.h_flags.h[2]);
     const double t0 = now_s();
 #pragma omp parallel for schedule(dynamic, 8)
-    for (int w = 0; w < n_walk; ++w) {
-        char* base = reinterpret_cast<char*>(force[w]);
-        const int64_t o = t.epi_disp[w];
-        for (int i = 0; i < ni[w]; ++i) {
-            char* r = base + (size_t)i * fl->size;
-            if (t.mode != PGF_MODE_NEIGHBOR_SEARCH) {
-                const Accp a = t.h_accp.h[o + i];
-                double* acc = reinterpret_cast<double*>(r + fl->off_acc);
-                acc[0] = a.x;
-                acc[1] = a.y;
-                acc[2] = a.z;
-                *reinterpret_cast<double*>(r + fl->off_pot) = a.w;
-                if (t.mode == PGF_MODE_FORCE_CHANGEOVER)
-                    *reinterpret_cast<double*>(r + g.co.force_off_pot_soft) = t.h_pot_soft.h[o + i];
-                if (t.mode == PGF_MODE_GRADIENT) {
-                    double* ac = reinterpret_cast<double*>(r + g.gr.force_off_acorr);
-                    const Accp c = t.h_acorr.h[o + i];
-                    ac[0] = c.x;
-                    ac[1] = c.y;
-                    ac[2] = c.z;
-                }
-            }
-            if (fl->n_ngb_bytes == 8)
-                *reinterpret_cast<int64_t*>(r + fl->off_n_ngb) = t.h_nnb.h[o + i];
-            else
-                *reinterpret_cast<int32_t*>(r + fl->off_n_ngb) = t.h_nnb.h[o + i];
-        }
-    }
+    for (int w = 0; w < n_walk; ++w) unpack_walk(t, w, ni, force, fl);
     g.prof.copy += now_s() - t0;
     return PGF_OK;
 }
@@ -1124,6 +1179,7 @@ int pgf_finalize(void) {
     if (g.copy_stream) cudaStreamSynchronize(g.copy_stream);
     for (auto& st : g.stage_stream)
         if (st) cudaStreamSynchronize(st);
+    if (g.d2h_stream) cudaStreamSynchronize(g.d2h_stream);
     for (auto& t : g.tags) {
         t.epi.release();
         t.id_epj.release();
@@ -1191,6 +1247,8 @@ int pgf_finalize(void) {
         if (st) cudaStreamDestroy(st);
         st = nullptr;
     }
+    if (g.d2h_stream) cudaStreamDestroy(g.d2h_stream);
+    g.d2h_stream = nullptr;
     if (!g.user_stream) g.stream = nullptr;
     g.j_sent = false;
     g.init = false;
