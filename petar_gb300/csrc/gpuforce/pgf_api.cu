@@ -14,6 +14,8 @@
 #include "petar_gpuforce.h"
 #include "pgf_internal.cuh"
 
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -161,6 +163,7 @@ struct State {
     DevBuf<SpjQ64> spj_q64;
     DevBuf<EpjF32> epj32;  // (hi, lo) FP32 copies built on the device
     DevBuf<SpjF32> spj32;
+    TensorMaps tmaps;      // TMA descriptors of epj32 / spj32
     bool co_set = false;   // changeover layout given (pgf_set_changeover_layout)
     pgf_changeover_layout co{};
     bool j_co_sent = false;  // the last send packed the EPJ changeover records
@@ -263,6 +266,44 @@ inline CoRec make_co(double r_in, double r_out, double mass, int64_t id) {
     c.mass = (float)mass;
     c.id = id;
     return c;
+}
+
+// 2-D tensor map over n rows of `row_floats` floats, boxes one row high (the
+// form TMA gather4 loads take).
+int encode_rows(CUtensorMap* map, void* base, int64_t n, int row_floats) {
+    const cuuint64_t dims[2] = {(cuuint64_t)row_floats, (cuuint64_t)n};
+    const cuuint64_t strides[1] = {(cuuint64_t)row_floats * sizeof(float)};
+    const cuuint32_t box[2] = {(cuuint32_t)row_floats, 1};
+    const cuuint32_t estr[2] = {1, 1};
+    // The driver entry point is looked up through the runtime, so the library
+    // does not link libcuda and loads on hosts without a driver.
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q{};
+        void* fn = nullptr;
+        const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+            return fail(PGF_ERR_CUDA, "cuTensorMapEncodeTiled not available from the driver");
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(PGF_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return PGF_OK;
+}
+
+// Rebuilds the TMA descriptors of the (hi, lo) j arrays after a send.
+int encode_tensor_maps(int64_t n_epj, int64_t n_spj) {
+    g.tmaps.valid = false;
+    std::memset(&g.tmaps.epj, 0, sizeof(CUtensorMap));
+    std::memset(&g.tmaps.spj, 0, sizeof(CUtensorMap));
+    if (n_epj > 0)
+        if (int r = encode_rows(&g.tmaps.epj, g.epj32.d, n_epj, (int)(sizeof(EpjF32) / sizeof(float)))) return r;
+    if (n_spj > 0)
+        if (int r = encode_rows(&g.tmaps.spj, g.spj32.d, n_spj, (int)(sizeof(SpjF32) / sizeof(float)))) return r;
+    g.tmaps.valid = true;
+    return PGF_OK;
 }
 
 // Adds the time of the last j send to the profile once its copies are done.
@@ -405,6 +446,7 @@ int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, co
         const cudaError_t e = launch_split_j(g.epj.d, n_epj, g.epj32.d, g.spj.d, n_spj, g.spj32.d, g.stream);
         if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "j split kernel failed: %s", cudaGetErrorString(e));
     }
+    if (int r = encode_tensor_maps(n_epj, n_spj)) return r;
     // The copies run behind the caller's next steps (walk packing); the
     // staging is not written again before the next send, which waits first.
     PGF_CUDA(cudaEventRecord(g.ev_send1, g.stream));
@@ -456,7 +498,7 @@ int launch_kernels(const TagState& t, const Params& p, cudaStream_t s, cudaEvent
         if (e == cudaSuccess) e = cudaEventRecord(ev_end, s);
         if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), s);
     } else {
-        e = t.variant == 0 ? launch_mixed(p, s, g.num_sms) : launch_ws(p, s, g.num_sms, t.variant - 1);
+        e = t.variant == 0 ? launch_mixed(p, s, g.num_sms) : launch_ws(p, s, g.num_sms, t.variant - 1, &g.tmaps);
         if (e == cudaSuccess) e = cudaEventRecord(ev_end, s);
         if (e == cudaSuccess && p.n_walk > 0) e = launch_retest(p, s, g.num_sms);
     }

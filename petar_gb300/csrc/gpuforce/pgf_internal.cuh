@@ -23,6 +23,7 @@
 // HBM once per force evaluation.
 #pragma once
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace pgf {
@@ -215,7 +216,14 @@ cudaError_t launch_split_j(const EpjMix* epj, int64_t n_epj, EpjF32* epj32, cons
                            SpjF32* spj32, cudaStream_t s);
 // Warp-specialised kernel, variants 0..kNumWsVariants-1 (see pgf_kernels_ws.cu).
 constexpr int kNumWsVariants = 8;
-cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant);
+// TMA descriptors of the (hi, lo) EPJ and SPJ arrays (rows of 32 and 64
+// bytes, boxes one row high), rebuilt at every send.
+struct TensorMaps {
+    CUtensorMap epj;
+    CUtensorMap spj;
+    bool valid = false;
+};
+cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant, const TensorMaps* tm);
 // Neighbour search (counts only, SPJ lists ignored) with the warp-specialised kernel.
 cudaError_t launch_ws_search(const Params& p, cudaStream_t s, int num_sms);
 // Soft force with the changeover correction of neighbours fused in.

@@ -32,6 +32,8 @@
 //   sets the device error word and returns.  The host reports PGF_ERR_DEVICE.
 #include "pgf_internal.cuh"
 
+#include <cuda.h>
+
 namespace pgf {
 namespace {
 
@@ -131,6 +133,27 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int32_
     }
 }
 
+// mbarrier arrival that also expects `bytes` of asynchronous (TMA) writes.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile(
+        "{\n\t.reg .b64 st;\n\t"
+        "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_addr(bar)),
+        "r"(bytes)
+        : "memory");
+}
+
+// TMA gather of four rows (r0..r3) of a 2-D tensor map whose box is one row
+// high, into consecutive rows at smem_dst; completion is signalled on bar.
+// The rows must lie inside the tensor; the column coordinate is 0.
+__device__ __forceinline__ void tma_gather4(void* smem_dst, const CUtensorMap* map, int r0, int r1, int r2, int r3,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_addr(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(smem_addr(bar))
+        : "memory");
+}
+
 // Named barrier among the consumer warps only (the producer never joins).
 __device__ __forceinline__ void consumers_sync(int n_threads) {
     asm volatile("bar.sync 1, %0;" ::"r"(n_threads) : "memory");
@@ -216,6 +239,16 @@ struct SlotSel<true, TE, kModeChangeover> {
 };
 template <int KI, int CT, bool CO>
 struct CoExtra {};
+// TMA staging of the producer: two 4 KB buffers (one 128-entry EPJ tile of
+// 32-byte records or one 64-entry SPJ tile of 64-byte records each) and their
+// transaction barriers.
+template <bool TM>
+struct TmExtra {};
+template <>
+struct TmExtra<true> {
+    alignas(128) unsigned char stage[2][4096];
+    uint64_t bar[2];
+};
 template <int KI, int CT>
 struct CoExtra<KI, CT, true> {
     float2 dtot[KI][CT];   // (hi, lo) flushed neighbour-pair partials of pot_tot
@@ -233,8 +266,9 @@ struct Hdr {
     int64_t base;  // first list entry of the tile
 };
 
-template <int CW, int KI, bool PK, int TE, int NS, int MD>
+template <int CW, int KI, bool PK, int TE, int NS, int MD, bool TM = false>
 struct Smem {
+    TmExtra<TM> tm;
     typename SlotSel<PK, TE, MD>::type slot[NS];
     Hdr hdr[NS];
     uint64_t full[NS];
@@ -277,9 +311,11 @@ __device__ __forceinline__ void co_k_f32(float r, float r_in, float norm, float 
 
 // SR (neighbour search): EPJ tiles only, near entries only; far entries can
 // hold no neighbour and SPJ lists are skipped.
-template <int CW, int KI, bool PK, int MD, int TE, int NS>
-__device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int lane) {
+template <int CW, int KI, bool PK, int MD, int TE, int NS, bool TM>
+__device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, int lane, const CUtensorMap& tme,
+                         const CUtensorMap& tms) {
     constexpr bool SR = MD == kModeSearch, CO = MD == kModeChangeover;
+    static_assert(!TM || (MD == kModeForce && TE == 128), "TMA staging: force mode, 128-entry EP tiles");
     constexpr int kMaxPass = CW * 32 * KI;
     constexpr int kTileEP = TE, kTileSP = TE / 2, kSlots = NS;
     constexpr int QE = TE / 32, QS = TE / 64;  // EPJ and SPJ entries per lane and tile
@@ -287,6 +323,16 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int l
     const float eps2 = (float)p.eps2;
     const uint64_t stream_pol = l2_evict_first_policy();
     unsigned item = 0;
+    unsigned tm_phase = 0;     // parity of the two TMA staging barriers
+    unsigned tm_inflight = 0;  // staging buffers with a gather issued and not yet waited for
+    // On a failed wait: let this warp's gathers still in flight land (each
+    // wait bounded) before the CTA's shared memory goes away.
+    auto bail = [&]() {
+        if constexpr (TM) {
+            for (int b = 0; b < 2; ++b)
+                if (tm_inflight & (1u << b)) (void)mbar_wait(&s.tm.bar[b], (tm_phase >> b) & 1u, p.err);
+        }
+    };
     auto acquire = [&](int& sl) -> bool {
         sl = item % kSlots;
         const unsigned parity = ((item / kSlots) & 1u) ^ 1u;
@@ -303,7 +349,7 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int l
         w_q = __shfl_sync(0xffffffffu, w_q, 0);
         if (w_q >= p.n_walk) {
             int sl;
-            if (!acquire(sl)) return;
+            if (!acquire(sl)) return bail();
             if (lane == 0) s.hdr[sl].kind = kItemExit;
             publish(sl);
             return;
@@ -319,37 +365,98 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int l
         const float hmax = fmaxf(wd.hx, fmaxf(wd.hy, wd.hz));
         const int n_ept = (wd.n_epj + kTileEP - 1) / kTileEP;
         const int n_spt = SR ? 0 : (wd.n_spj + kTileSP - 1) / kTileSP;
+        const int n_tiles = n_ept + n_spt;
+        // TMA staging: tile u (EP tiles, then SP tiles) is gathered into
+        // stage[u & 1] while tile u - 1 is converted.  Lane l gathers entries
+        // 4l .. 4l + 3 (rows past the tile's end read row 0 and are ignored), so
+        // every tile moves exactly 4096 bytes.
+        auto tm_issue = [&](int u) {
+            if constexpr (TM) {
+                const int b = u & 1;
+                const bool ep = u < n_ept;
+                // the buffer's previous contents were read through the generic proxy
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                const int t = ep ? u : u - n_ept;
+                const int64_t base = ep ? wd.epj_begin + (int64_t)t * kTileEP : wd.spj_begin + (int64_t)t * kTileSP;
+                const int nt = ep ? min(kTileEP, wd.n_epj - t * kTileEP) : min(kTileSP, wd.n_spj - t * kTileSP);
+                const int32_t* ids = ep ? p.id_epj : p.id_spj;
+                const int n_lanes = ep ? kTileEP / 4 : kTileSP / 4;
+                int r[4] = {0, 0, 0, 0};
+                if (lane < n_lanes) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int e = 4 * lane + j;
+                        r[j] = e < nt ? ld_streamed(ids + base + e, stream_pol) : 0;
+                    }
+                }
+                if (lane == 0) mbar_arrive_expect_tx(&s.tm.bar[b], 4096u);
+                __syncwarp();
+                if (lane < n_lanes)
+                    tma_gather4(s.tm.stage[b] + lane * (ep ? 128 : 256), ep ? &tme : &tms, r[0], r[1], r[2], r[3],
+                                &s.tm.bar[b]);
+                tm_inflight |= 1u << b;
+            }
+        };
+        auto tm_wait = [&](int u) -> bool {
+            if constexpr (TM) {
+                const int b = u & 1;
+                const bool ok = mbar_wait(&s.tm.bar[b], (tm_phase >> b) & 1u, p.err);
+                if (ok) {
+                    tm_phase ^= 1u << b;
+                    tm_inflight &= ~(1u << b);
+                }
+                return ok;
+            } else {
+                return true;
+            }
+        };
         for (int ipass = 0; ipass < wd.n_i; ipass += kMaxPass) {
             int sl;
-            if (!acquire(sl)) return;
+            if (!acquire(sl)) return bail();
             if (lane == 0) {
                 s.hdr[sl].kind = kItemBegin;
                 s.hdr[sl].walk = widx;
                 s.hdr[sl].ipass = ipass;
             }
             publish(sl);
+            if constexpr (TM) {
+                if (n_tiles > 0) tm_issue(0);
+            }
             // EPJ tiles: ids and records for 4 entries per lane.
             for (int t = 0; t < n_ept; ++t) {
                 const int64_t base = wd.epj_begin + (int64_t)t * kTileEP;
                 const int nt = min(kTileEP, wd.n_epj - t * kTileEP);
                 int id[QE];
                 float4 r0[QE], r1[QE];
+                if constexpr (TM) {
+                    if (t + 1 < n_tiles) tm_issue(t + 1);
+                    if (!tm_wait(t)) return bail();
+                    const float4* st = reinterpret_cast<const float4*>(s.tm.stage[t & 1]);
 #pragma unroll
-                for (int q = 0; q < QE; ++q) {
-                    const int e = q * 32 + lane;
-                    id[q] = e < nt ? ld_streamed(p.id_epj + base + e, stream_pol) : -1;
-                }
+                    for (int q = 0; q < QE; ++q) {
+                        const int e = q * 32 + lane;
+                        id[q] = e < nt ? 0 : -1;
+                        r0[q] = st[2 * e];
+                        r1[q] = st[2 * e + 1];
+                    }
+                } else {
 #pragma unroll
-                for (int q = 0; q < QE; ++q) {
-                    if (id[q] >= 0) {
-                        const float4* src = reinterpret_cast<const float4*>(p.epj32 + id[q]);
-                        r0[q] = __ldg(src);
-                        r1[q] = __ldg(src + 1);
-                    } else {
-                        r0[q] = r1[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    for (int q = 0; q < QE; ++q) {
+                        const int e = q * 32 + lane;
+                        id[q] = e < nt ? ld_streamed(p.id_epj + base + e, stream_pol) : -1;
+                    }
+#pragma unroll
+                    for (int q = 0; q < QE; ++q) {
+                        if (id[q] >= 0) {
+                            const float4* src = reinterpret_cast<const float4*>(p.epj32 + id[q]);
+                            r0[q] = __ldg(src);
+                            r1[q] = __ldg(src + 1);
+                        } else {
+                            r0[q] = r1[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        }
                     }
                 }
-                if (!acquire(sl)) return;
+                if (!acquire(sl)) return bail();
                 auto& S = s.slot[sl].ep;
                 int nn = 0, nf = 0;
 #pragma unroll
@@ -432,20 +539,33 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int l
                 const int nt = min(kTileSP, wd.n_spj - t * kTileSP);
                 int id[QS];
                 float4 r[QS][4];
+                if constexpr (TM) {
+                    const int u = n_ept + t;
+                    if (u + 1 < n_tiles) tm_issue(u + 1);
+                    if (!tm_wait(u)) return bail();
+                    const float4* st = reinterpret_cast<const float4*>(s.tm.stage[u & 1]);
 #pragma unroll
-                for (int q = 0; q < QS; ++q) {
-                    const int e = q * 32 + lane;
-                    id[q] = e < nt ? ld_streamed(p.id_spj + base + e, stream_pol) : -1;
-                }
+                    for (int q = 0; q < QS; ++q) {
+                        const int e = q * 32 + lane;
 #pragma unroll
-                for (int q = 0; q < QS; ++q) {
-                    if (id[q] >= 0) {
-                        const float4* src = reinterpret_cast<const float4*>(p.spj32 + id[q]);
+                        for (int v = 0; v < 4; ++v) r[q][v] = st[4 * e + v];
+                    }
+                } else {
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) r[q][u] = __ldg(src + u);
+                    for (int q = 0; q < QS; ++q) {
+                        const int e = q * 32 + lane;
+                        id[q] = e < nt ? ld_streamed(p.id_spj + base + e, stream_pol) : -1;
+                    }
+#pragma unroll
+                    for (int q = 0; q < QS; ++q) {
+                        if (id[q] >= 0) {
+                            const float4* src = reinterpret_cast<const float4*>(p.spj32 + id[q]);
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) r[q][u] = __ldg(src + u);
+                        }
                     }
                 }
-                if (!acquire(sl)) return;
+                if (!acquire(sl)) return bail();
                 auto& S = s.slot[sl].sp;
 #pragma unroll
                 for (int q = 0; q < QS; ++q) {
@@ -492,7 +612,7 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int l
                 }
                 publish(sl);
             }
-            if (!acquire(sl)) return;
+            if (!acquire(sl)) return bail();
             if (lane == 0) s.hdr[sl].kind = kItemEnd;
             publish(sl);
         }
@@ -522,8 +642,8 @@ __device__ __forceinline__ float pass_cost(int nip, int ku, int ct_threads) {
 // coordinates and the pair accumulators.  The near-only data of each i (lo
 // coordinates, r_search^2, guard band) and the neighbour counts live in
 // shared memory and are read once per tile that has near entries.
-template <int CW, int KI, bool PK, int MD, int TE, int NS>
-__device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int ct) {
+template <int CW, int KI, bool PK, int MD, int TE, int NS, bool TM>
+__device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, int ct) {
     constexpr bool SR = MD == kModeSearch, CO = MD == kModeChangeover;
     constexpr int kSlots = NS;
     constexpr int CT = CW * 32;
@@ -1019,43 +1139,53 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD>& s, int c
     }
 }
 
-template <int CW, int KI, int MINB, bool PK, int MD, int TE, int NS>
-__global__ __launch_bounds__((CW + 1) * 32, MINB) void ws_kernel(Params p) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    Smem<CW, KI, PK, TE, NS, MD>& s = *reinterpret_cast<Smem<CW, KI, PK, TE, NS, MD>*>(smem_raw);
+template <int CW, int KI, int MINB, bool PK, int MD, int TE, int NS, bool TM>
+__global__ __launch_bounds__((CW + 1) * 32, MINB) void ws_kernel(Params p, const __grid_constant__ CUtensorMap tme,
+                                                                 const __grid_constant__ CUtensorMap tms) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    Smem<CW, KI, PK, TE, NS, MD, TM>& s = *reinterpret_cast<Smem<CW, KI, PK, TE, NS, MD, TM>*>(smem_raw);
     const int tid = threadIdx.x;
     if (tid == 0) {
         for (int i = 0; i < NS; ++i) {
             mbar_init(&s.full[i], 32);
             mbar_init(&s.empty[i], CW * 32);
         }
+        if constexpr (TM) {
+            mbar_init(&s.tm.bar[0], 1);
+            mbar_init(&s.tm.bar[1], 1);
+            // make the initialised barriers visible to the TMA (async) proxy
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
     }
     __syncthreads();
     if (tid >= CW * 32)
-        producer<CW, KI, PK, MD, TE, NS>(p, s, tid - CW * 32);
+        producer<CW, KI, PK, MD, TE, NS, TM>(p, s, tid - CW * 32, tme, tms);
     else
-        consumer<CW, KI, PK, MD, TE, NS>(p, s, tid);
+        consumer<CW, KI, PK, MD, TE, NS, TM>(p, s, tid);
 }
 
-template <int CW, int KI, int MINB, bool PK, int MD = kModeForce, int TE = 128, int NS = 4>
-cudaError_t launch_ws_t(const Params& p, cudaStream_t st, int num_sms) {
+template <int CW, int KI, int MINB, bool PK, int MD = kModeForce, int TE = 128, int NS = 4, bool TM = false>
+cudaError_t launch_ws_t(const Params& p, cudaStream_t st, int num_sms, const TensorMaps* tm = nullptr) {
     cudaError_t e = cudaMemsetAsync(p.queue_head, 0, sizeof(int32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), st);
     if (e != cudaSuccess) return e;
     if (p.n_walk <= 0) return cudaSuccess;
     static int per_sm = 0;
-    const size_t smem = sizeof(Smem<CW, KI, PK, TE, NS, MD>);
+    const size_t smem = sizeof(Smem<CW, KI, PK, TE, NS, MD, TM>);
+    static const CUtensorMap none{};
+    if (TM && (!tm || !tm->valid)) return cudaErrorInvalidValue;
     if (per_sm == 0) {
-        e = cudaFuncSetAttribute(ws_kernel<CW, KI, MINB, PK, MD, TE, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(ws_kernel<CW, KI, MINB, PK, MD, TE, NS, TM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ws_kernel<CW, KI, MINB, PK, MD, TE, NS>, (CW + 1) * 32, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ws_kernel<CW, KI, MINB, PK, MD, TE, NS, TM>, (CW + 1) * 32, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
     int grid = num_sms * per_sm;
     if (grid > p.n_walk) grid = p.n_walk;
-    ws_kernel<CW, KI, MINB, PK, MD, TE, NS><<<grid, (CW + 1) * 32, smem, st>>>(p);
+    ws_kernel<CW, KI, MINB, PK, MD, TE, NS, TM><<<grid, (CW + 1) * 32, smem, st>>>(p, TM ? tm->epj : none,
+                                                                                  TM ? tm->spj : none);
     return cudaGetLastError();
 }
 
@@ -1109,15 +1239,15 @@ cudaError_t launch_split_j(const EpjMix* epj, int64_t n_epj, EpjF32* epj32, cons
 // Variants of the warp-specialised kernel: consumer warps, i per consumer
 // thread, minimum CTAs per SM, packed FP32x2, and the ring geometry (EP tile
 // entries, slots).
-cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant) {
+cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant, const TensorMaps* tm) {
     switch (variant) {
         case 0: return launch_ws_t<4, 3, 4, false>(p, s, num_sms);
-        case 1: return launch_ws_t<4, 3, 4, false, kModeForce, 64, 8>(p, s, num_sms);
+        case 1: return launch_ws_t<4, 3, 4, true, kModeForce, 128, 3, true>(p, s, num_sms, tm);
         case 2: return launch_ws_t<4, 3, 4, true, kModeForce, 64, 8>(p, s, num_sms);
-        case 3: return launch_ws_t<4, 2, 4, true, kModeForce, 64, 8>(p, s, num_sms);
+        case 3: return launch_ws_t<4, 3, 3, true, kModeForce, 128, 4, true>(p, s, num_sms, tm);
         case 4: return launch_ws_t<4, 2, 4, true>(p, s, num_sms);
         case 5: return launch_ws_t<4, 3, 4, true>(p, s, num_sms);
-        case 6: return launch_ws_t<4, 4, 4, false, kModeForce, 64, 8>(p, s, num_sms);
+        case 6: return launch_ws_t<4, 2, 4, true, kModeForce, 128, 3, true>(p, s, num_sms, tm);
         case 7: return launch_ws_t<4, 3, 3, true, kModeForce, 128, 6>(p, s, num_sms);
         default: return cudaErrorInvalidValue;
     }
