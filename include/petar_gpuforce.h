@@ -304,6 +304,83 @@ int pgf_force_device_noalloc(int n_walk, const int64_t *walk_table, const double
 /* Releases device and pinned host memory. */
 int pgf_finalize(void);
 
+/* ---- Device-resident tree step ---------------------------------------------
+ *
+ * PeTar's tree step passes every particle through the host: treeSoftForce
+ * (src/petar.hpp:879-907) has FDPS build the tree and the interaction lists
+ * and hand them to the GPU functor, and kickOne (src/petar.hpp:1198-1212) and
+ * driftSingle (src/petar.hpp:1326-1340) update velocities and positions on the
+ * host.  A pgf_nbody keeps the particles on the device and runs the whole
+ * cycle there, for singles without a hard part:
+ *
+ *   kick(dt/2), drift(dt), tree + lists, soft force, kick(dt/2)
+ *
+ * The tree and lists are those of the host list builder that stands in for
+ * FDPS (Morton order, n_leaf_limit, n_group_limit, theta opening with the
+ * symmetric r_search test), built on the device entry for entry the same.
+ * pgf_nbody_run with use_graph != 0 captures its n_steps steps in one CUDA
+ * graph (kept for later calls with the same n_steps and dt).
+ *
+ * These calls report failures through pgf_nbody_last_error().  A handle
+ * belongs to the device that was current at creation; calls on one handle
+ * must not overlap. */
+typedef struct pgf_nbody pgf_nbody;
+
+typedef struct pgf_nbody_config {
+    double eps2;              /* softening squared (EPISoft::eps^2) */
+    double r_out;             /* changeover outer radius: the cutoff (rcut2 = r_out^2) */
+    double G;                 /* gravitational constant */
+    double theta;             /* opening angle; <= 0 opens every cell */
+    int n_leaf_limit;         /* a cell splits while it holds more particles */
+    int n_group_limit;        /* i-groups hold at most this many particles (or are leaves) */
+    int precision;            /* PGF_PRECISION_MIXED or PGF_PRECISION_FP64 */
+    int kernel_variant;       /* as pgf_set_kernel_variant, TMA variants excluded; -1 = default */
+    double list_capacity_factor; /* room kept for growth of cells and lists (>= 1; 0 = 2) */
+} pgf_nbody_config;
+
+typedef struct pgf_nbody_stats {
+    int64_t n_cells, n_groups;                  /* tree of the last build */
+    int64_t n_epj_entries, n_spj_entries;       /* list entries of the last build */
+    int64_t interactions_epep, interactions_epsp; /* sum over groups of n_i * n_j, last build */
+    int64_t total_epep, total_epsp;             /* the same summed over every build */
+    int64_t steps;                              /* steps run so far */
+    double last_tree_ms, last_force_ms;         /* split of the last pgf_nbody_force call */
+    int kernel_variant;
+    int cap_cells;
+    int64_t cap_epj_entries, cap_spj_entries;
+} pgf_nbody_stats;
+
+/* Copies the particles (pos/vel: 3 doubles each) to the device, builds the
+ * tree and lists once (sizing the list arrays from it) and evaluates the
+ * forces.  On success *out is the new handle. */
+int pgf_nbody_create(const pgf_nbody_config *cfg, int64_t n, const double *pos, const double *vel,
+                     const double *mass, const double *r_search, pgf_nbody **out);
+/* Tree, lists and forces at the current positions (no kick); waits. */
+int pgf_nbody_force(pgf_nbody *h);
+/* n_steps kick-drift-force-kick steps of size dt; waits.  *ms (optional)
+ * receives the device time of the whole run. */
+int pgf_nbody_run(pgf_nbody *h, int n_steps, double dt, int use_graph, double *ms);
+/* Copies state back (any pointer may be NULL): pos, vel, acc (3 doubles each),
+ * pot (G applied, self pair included as the kernels count it), n_ngb. */
+int pgf_nbody_get(pgf_nbody *h, double *pos, double *vel, double *acc, double *pot, int32_t *n_ngb);
+/* Replaces positions and/or velocities (NULL keeps them). */
+int pgf_nbody_set_state(pgf_nbody *h, const double *pos, const double *vel);
+/* Kinetic energy and soft potential energy 1/2 sum m (pot + G m / r_out) of
+ * the last forces. */
+int pgf_nbody_energy(pgf_nbody *h, double *kinetic, double *potential);
+int pgf_nbody_get_stats(pgf_nbody *h, pgf_nbody_stats *stats);
+/* The last build's tree and lists in the host builder's form: order[n]
+ * (sorted position -> particle index), group_begin, epj_disp and spj_disp
+ * [n_groups + 1], id_epj, id_spj, and per cell mass, centre of mass[3],
+ * second moment[6] and level.  Any pointer may be NULL. */
+int pgf_nbody_export_lists(pgf_nbody *h, int64_t *order, int64_t *group_begin, int64_t *epj_disp,
+                           int64_t *spj_disp, int32_t *id_epj, int32_t *id_spj, double *cell_mass,
+                           double *cell_pos, double *cell_quad, int32_t *cell_level);
+/* Times every available variant on the resident lists and keeps the fastest. */
+int pgf_nbody_autotune(pgf_nbody *h, int repeats, int *best_variant, double *best_ms);
+int pgf_nbody_destroy(pgf_nbody *h);
+const char *pgf_nbody_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,7 +60,13 @@ GPU_SOURCES = [
     "gpuforce/pgf_kernels_ws.cu",
     "gpuforce/pgf_noalloc.cu",
     "gpuforce/pgf_kernels_gradient.cu",
+    "gpuforce/pgf_nbody.cu",
 ]
+# Per-file flags: the device list builder repeats the host builder's FP64
+# arithmetic exactly, so nothing in it may be contracted into an FMA.
+GPU_FILE_FLAGS = {
+    "pgf_nbody": ["-fmad=false"],
+}
 GPU_HEADERS = [
     "gpuforce/pgf_internal.cuh",
 ]
@@ -84,7 +90,7 @@ def build_gpuforce(force: bool = False, verbose: bool = False) -> Path:
 
     def compile_one(src: Path) -> Path:
         obj = objdir / (src.stem + ".o")
-        _run(common + ["-c", str(src), "-o", str(obj)])
+        _run(common + GPU_FILE_FLAGS.get(src.stem, []) + ["-c", str(src), "-o", str(obj)])
         return obj
 
     with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
@@ -104,7 +110,8 @@ def build_harness(force: bool = False) -> Path:
     if not force and _newer(out, [src]):
         return out
     tmp = out.with_suffix(".so.tmp")
-    _run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", str(src), "-o", str(tmp)])
+    # No FMA contraction: the device list builder reproduces its FP64 results bit for bit.
+    _run(["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-fopenmp", str(src), "-o", str(tmp)])
     os.replace(tmp, out)
     return out
 

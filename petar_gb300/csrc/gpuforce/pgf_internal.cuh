@@ -161,7 +161,16 @@ struct Params {
     int32_t pad1;
     int32_t* err;          // device error word (0 = ok)
     int32_t* retest_total; // records re-tested since the host last read it (optional)
+    // Walk count written by an earlier kernel on the same stream (the device
+    // list builder), or null: the kernels then run min(*n_walk_dev, n_walk)
+    // walks, n_walk being the capacity of walks and order.
+    const int32_t* n_walk_dev;
 };
+
+// Number of walks of this launch.
+__device__ __forceinline__ int walk_count(const Params& p) {
+    return p.n_walk_dev ? min(*p.n_walk_dev, p.n_walk) : p.n_walk;
+}
 
 // Exact FP64 neighbour test of one pair, in the oracle's evaluation order
 // (src/force_gpu_cuda.cu:62-64 semantics, src/soft_force.hpp:58-64 order):
@@ -224,6 +233,8 @@ struct TensorMaps {
     bool valid = false;
 };
 cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant, const TensorMaps* tm);
+// Whether warp-specialised variant v stages its tiles with TMA (needs TensorMaps).
+bool ws_variant_uses_tma(int variant);
 // Neighbour search (counts only, SPJ lists ignored) with the warp-specialised kernel.
 cudaError_t launch_ws_search(const Params& p, cudaStream_t s, int num_sms);
 // Soft force with the changeover correction of neighbours fused in.

@@ -20,12 +20,13 @@ __global__ __launch_bounds__(kT) void fp64_kernel(Params p) {
     __shared__ int s_w;
     const int tid = threadIdx.x;
     const double eps2 = p.eps2;
+    const int n_walk = walk_count(p);
     for (;;) {
         if (tid == 0) s_w = atomicAdd(p.queue_head, 1);
         __syncthreads();
         const int wq = s_w;
         __syncthreads();
-        if (wq >= p.n_walk) break;
+        if (wq >= n_walk) break;
         const WalkDesc wd = p.walks[p.order[wq]];
         const double rcut2 = wd.rcut2;
         for (int ic = 0; ic < wd.n_i; ic += kT) {

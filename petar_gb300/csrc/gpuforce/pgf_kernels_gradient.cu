@@ -61,12 +61,13 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel(Params p) {
     SmemG& s = *reinterpret_cast<SmemG*>(smem_raw);
     const int tid = threadIdx.x;
     const float eps2 = (float)p.eps2;
+    const int n_walk = walk_count(p);
     for (;;) {
         __syncthreads();
         if (tid == 0) s.w = atomicAdd(p.queue_head, 1);
         __syncthreads();
         const int wq = s.w;
-        if (wq >= p.n_walk) break;
+        if (wq >= n_walk) break;
         const WalkDesc wd = p.walks[p.order[wq]];
         const float chx = (float)wd.cx, chy = (float)wd.cy, chz = (float)wd.cz;
         const float clx = (float)(wd.cx - (double)chx), cly = (float)(wd.cy - (double)chy),

@@ -176,12 +176,13 @@ __global__ __launch_bounds__(kThreads, PGF_MINB) void mixed_kernel(Params p) {
 
     for (int i = tid; i < kMaxPass; i += kThreads) s.flag[i] = 0u;
 
+    const int n_walk = walk_count(p);
     for (;;) {
         __syncthreads();
         if (tid == 0) s.w = atomicAdd(p.queue_head, 1);
         __syncthreads();
         const int wq = s.w;
-        if (wq >= p.n_walk) break;
+        if (wq >= n_walk) break;
         const int widx = p.order[wq];
         const WalkDesc wd = p.walks[widx];
         const double cx = wd.cx, cy = wd.cy, cz = wd.cz;

@@ -343,11 +343,12 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
         mbar_arrive(&s.full[sl]);  // 32 arrivals complete the phase
         ++item;
     };
+    const int n_walk = walk_count(p);
     for (;;) {
         int w_q = 0;
         if (lane == 0) w_q = atomicAdd(p.queue_head, 1);
         w_q = __shfl_sync(0xffffffffu, w_q, 0);
-        if (w_q >= p.n_walk) {
+        if (w_q >= n_walk) {
             int sl;
             if (!acquire(sl)) return bail();
             if (lane == 0) s.hdr[sl].kind = kItemExit;
@@ -1252,6 +1253,8 @@ cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant,
         default: return cudaErrorInvalidValue;
     }
 }
+
+bool ws_variant_uses_tma(int variant) { return variant == 1 || variant == 3 || variant == 6; }
 
 cudaError_t launch_ws_search(const Params& p, cudaStream_t s, int num_sms) {
     return launch_ws_t<4, 3, 4, false, kModeSearch>(p, s, num_sms);

@@ -11,7 +11,8 @@
 //     particles,
 //   * quadrupole moments per cell: mass, centre of mass and the raw second
 //     moment sum m (x - c)(x - c)^T about the centre of mass (the convention
-//     the quadrupole formulas in src/soft_force.hpp:160-200 assume),
+//     the quadrupole formulas in src/soft_force.hpp:160-200 assume), built
+//     bottom-up from the children's moments as FDPS's moment pass does,
 //   * i-groups: the first cells (top-down) holding at most n_group_limit
 //     particles,
 //   * per group, a walk that opens a cell when the squared distance from the
@@ -40,6 +41,7 @@ struct Cell {
     int child[8];
     double side;
     double mass;
+    double mx[3];    // mass moment sum m x
     double com[3];
     double quad[6];  // xx, yy, zz, xy, xz, yz
     double in_lo[3], in_hi[3];
@@ -172,41 +174,73 @@ void build(WalkSet& ws, const double* pos, const double* mass, const double* rs,
         ws.cells[c] = cc;
     }
 
-    // Moments and boxes straight from the particles of each cell.
+    // Moments and boxes, bottom-up.  A leaf sums its particles in sorted
+    // order; a parent combines its children in child order: mass and the mass
+    // moment m x are added, the centre of mass is their quotient, and the
+    // second moment about it follows from the children's by the parallel-axis
+    // term m_c (c_c - c)(c_c - c)^T.  Built without FMA contraction, so the
+    // device builder reproduces every bit of it.
     const int64_t nc = (int64_t)ws.cells.size();
-#pragma omp parallel for schedule(dynamic, 64)
-    for (int64_t c = 0; c < nc; ++c) {
+    for (int64_t c = nc - 1; c >= 0; --c) {
         Cell& cc = ws.cells[c];
-        double m = 0, mx[3] = {0, 0, 0};
+        double m = 0, mx[3] = {0, 0, 0}, q[6] = {0, 0, 0, 0, 0, 0};
         for (int d = 0; d < 3; ++d) {
             cc.in_lo[d] = cc.out_lo[d] = 1e300;
             cc.in_hi[d] = cc.out_hi[d] = -1e300;
         }
-        for (int64_t i = cc.begin; i < cc.end; ++i) {
-            m += sm[i];
-            for (int d = 0; d < 3; ++d) {
-                double x = sp[3 * i + d];
-                mx[d] += sm[i] * x;
-                cc.in_lo[d] = std::min(cc.in_lo[d], x);
-                cc.in_hi[d] = std::max(cc.in_hi[d], x);
-                cc.out_lo[d] = std::min(cc.out_lo[d], x - sr[i]);
-                cc.out_hi[d] = std::max(cc.out_hi[d], x + sr[i]);
+        if (cc.leaf) {
+            for (int64_t i = cc.begin; i < cc.end; ++i) {
+                m += sm[i];
+                for (int d = 0; d < 3; ++d) {
+                    const double x = sp[3 * i + d];
+                    mx[d] += sm[i] * x;
+                    cc.in_lo[d] = std::min(cc.in_lo[d], x);
+                    cc.in_hi[d] = std::max(cc.in_hi[d], x);
+                    cc.out_lo[d] = std::min(cc.out_lo[d], x - sr[i]);
+                    cc.out_hi[d] = std::max(cc.out_hi[d], x + sr[i]);
+                }
+            }
+        } else {
+            for (int k = 0; k < cc.n_child; ++k) {
+                const Cell& ch = ws.cells[cc.child[k]];
+                m += ch.mass;
+                for (int d = 0; d < 3; ++d) {
+                    mx[d] += ch.mx[d];
+                    cc.in_lo[d] = std::min(cc.in_lo[d], ch.in_lo[d]);
+                    cc.in_hi[d] = std::max(cc.in_hi[d], ch.in_hi[d]);
+                    cc.out_lo[d] = std::min(cc.out_lo[d], ch.out_lo[d]);
+                    cc.out_hi[d] = std::max(cc.out_hi[d], ch.out_hi[d]);
+                }
             }
         }
         cc.mass = m;
         for (int d = 0; d < 3; ++d) {
+            cc.mx[d] = mx[d];
             if (m > 0) cc.com[d] = mx[d] / m;
             else cc.com[d] = 0.5 * (cc.in_lo[d] + cc.in_hi[d]);
         }
-        double q[6] = {0, 0, 0, 0, 0, 0};
-        for (int64_t i = cc.begin; i < cc.end; ++i) {
-            double dx = sp[3 * i] - cc.com[0], dy = sp[3 * i + 1] - cc.com[1], dz = sp[3 * i + 2] - cc.com[2];
-            q[0] += sm[i] * dx * dx;
-            q[1] += sm[i] * dy * dy;
-            q[2] += sm[i] * dz * dz;
-            q[3] += sm[i] * dx * dy;
-            q[4] += sm[i] * dx * dz;
-            q[5] += sm[i] * dy * dz;
+        if (cc.leaf) {
+            for (int64_t i = cc.begin; i < cc.end; ++i) {
+                const double dx = sp[3 * i] - cc.com[0], dy = sp[3 * i + 1] - cc.com[1],
+                             dz = sp[3 * i + 2] - cc.com[2];
+                q[0] += sm[i] * dx * dx;
+                q[1] += sm[i] * dy * dy;
+                q[2] += sm[i] * dz * dz;
+                q[3] += sm[i] * dx * dy;
+                q[4] += sm[i] * dx * dz;
+                q[5] += sm[i] * dy * dz;
+            }
+        } else {
+            for (int k = 0; k < cc.n_child; ++k) {
+                const Cell& ch = ws.cells[cc.child[k]];
+                const double dx = ch.com[0] - cc.com[0], dy = ch.com[1] - cc.com[1], dz = ch.com[2] - cc.com[2];
+                q[0] += ch.quad[0] + ch.mass * dx * dx;
+                q[1] += ch.quad[1] + ch.mass * dy * dy;
+                q[2] += ch.quad[2] + ch.mass * dz * dz;
+                q[3] += ch.quad[3] + ch.mass * dx * dy;
+                q[4] += ch.quad[4] + ch.mass * dx * dz;
+                q[5] += ch.quad[5] + ch.mass * dy * dz;
+            }
         }
         for (int k = 0; k < 6; ++k) cc.quad[k] = q[k];
     }

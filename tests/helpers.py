@@ -33,3 +33,21 @@ def stats(e: np.ndarray) -> dict:
     if e.size == 0:
         return dict(median=0.0, p999=0.0, max=0.0)
     return dict(median=float(np.median(e)), p999=float(np.quantile(e, 0.999)), max=float(e.max()))
+
+
+def rows_batch(wb: WalkBatch, rows: np.ndarray) -> WalkBatch:
+    """One walk per given EPI row, each with the lists of the row's own walk:
+    the oracle on a sample of i-particles without evaluating whole walks."""
+    rows = np.asarray(rows, dtype=np.int64)
+    w = np.searchsorted(wb.epi_disp, rows, side="right") - 1
+    ej = [wb.id_epj[wb.epj_disp[k]:wb.epj_disp[k + 1]] for k in w]
+    sj = [wb.id_spj[wb.spj_disp[k]:wb.spj_disp[k + 1]] for k in w]
+    disp = lambda parts: np.concatenate([[0], np.cumsum([p.size for p in parts])]).astype(np.int64)
+    cat = lambda parts: np.concatenate(parts).astype(np.int32) if parts else np.zeros(0, np.int32)
+    return WalkBatch(
+        epi_pos=wb.epi_pos[rows], epi_rs=wb.epi_rs[rows], epi_disp=np.arange(rows.size + 1, dtype=np.int64),
+        epj_pos=wb.epj_pos, epj_mass=wb.epj_mass, epj_rs=wb.epj_rs, spj_pos=wb.spj_pos, spj_mass=wb.spj_mass,
+        spj_quad=wb.spj_quad, epj_disp=disp(ej), id_epj=cat(ej), spj_disp=disp(sj), id_spj=cat(sj),
+        eps2=wb.eps2, rcut2=wb.rcut2, G=wb.G,
+        walk_rcut2=None if wb.walk_rcut2 is None else wb.walk_rcut2[w],
+        epi_index=None if wb.epi_index is None else wb.epi_index[rows])

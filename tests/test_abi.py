@@ -74,3 +74,25 @@ def test_variant_count_matches_header():
     text = (ROOT / "include" / "petar_gpuforce.h").read_text()
     n = int(re.search(r"#define PGF_NUM_KERNEL_VARIANTS (\d+)", text).group(1))
     assert n == gpuforce.NUM_KERNEL_VARIANTS
+
+
+def test_nbody_entry_points_without_device():
+    from petar_gb300 import nbody
+    lib = nbody._lib()
+    cfg = nbody.Config(0.0, 0.01, 1.0, 0.3, 20, 512, 0, -1, 2.0)
+    h = ctypes.c_void_p()
+    import numpy as np
+    x = np.zeros(3)
+    assert lib.pgf_nbody_create(None, 1, None, None, None, None, ctypes.byref(h)) == 1
+    bad = nbody.Config(0.0, 0.0, 1.0, 0.3, 20, 512, 0, -1, 2.0)
+    assert lib.pgf_nbody_create(ctypes.byref(bad), 1, x.ctypes.data, x.ctypes.data, x.ctypes.data,
+                                x.ctypes.data, ctypes.byref(h)) == 1
+    assert b"r_out" in lib.pgf_nbody_last_error()
+    r = lib.pgf_nbody_create(ctypes.byref(cfg), 1, x.ctypes.data, x.ctypes.data, x.ctypes.data, x.ctypes.data,
+                             ctypes.byref(h))
+    if r == 0:
+        lib.pgf_nbody_destroy(h)
+        pytest.skip("a GPU is present")
+    assert r == 2  # PGF_ERR_NO_DEVICE
+    assert lib.pgf_nbody_force(None) == 1
+    assert lib.pgf_nbody_destroy(None) == 0

@@ -1,0 +1,135 @@
+"""Device-resident tree step (pgf_nbody_*): the device list builder against
+the host list builder, its forces against the dispatch path and the FP64
+oracle, CUDA-graph runs against eager runs, and the 100-step kick-drift-kick
+run of the King W0 = 7, N = 4,194,304 configuration (theta 0.4, r_out 0.0015,
+dt = 1/1024) with per-step force errors on a random 4096-particle sample."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import rel_err, rel_err_vec, rows_batch, stats
+from petar_gb300 import gpuforce, ics, nbody, walks
+from petar_gb300.gpuforce import PGF_PRECISION_FP64, PGF_PRECISION_MIXED
+
+pytestmark = pytest.mark.gpu
+
+MIXED_MEDIAN = 1e-6
+MIXED_P999 = 1e-5
+
+
+def _clusters():
+    yield "plummer2048", ics.make_plummer_cluster(1, 2048, 0.02, theta=0.3)
+    yield "plummer20k_bin50", ics.make_plummer_cluster(21, 20000, 0.004, binary_fraction=0.5)
+    yield "king30k", ics.make_king_cluster(3, 30000, 0.004, W0=7.0, theta=0.4)
+    yield "plummer3000_theta0", ics.make_plummer_cluster(4, 3000, 0.02, theta=0.0)
+
+
+@pytest.mark.parametrize("name", ["plummer2048", "plummer20k_bin50", "king30k", "plummer3000_theta0"])
+def test_device_lists_equal_host_builder(name):
+    cl = dict(_clusters())[name]
+    host = walks.build_walks(cl)
+    with nbody.DeviceNBody(cl) as h:
+        dev = h.lists()
+    np.testing.assert_array_equal(dev.epi_index, host.epi_index)
+    for k in ("epi_disp", "epj_disp", "spj_disp", "id_epj", "id_spj"):
+        np.testing.assert_array_equal(getattr(dev, k), getattr(host, k), err_msg=k)
+    # Moments bit for bit (same arithmetic, no FMA contraction on either side).
+    for k in ("spj_mass", "spj_pos", "spj_quad"):
+        np.testing.assert_array_equal(getattr(dev, k), getattr(host, k), err_msg=k)
+
+
+def _particle_order(res, wb):
+    """Dispatch results (EPI rows) in particle order."""
+    out = {k: np.empty_like(v) for k, v in res.items()}
+    for k, v in res.items():
+        out[k][wb.epi_index] = v
+    return out
+
+
+@pytest.mark.parametrize("precision", [PGF_PRECISION_MIXED, PGF_PRECISION_FP64])
+def test_device_force_matches_dispatch_and_oracle(precision):
+    cl = ics.make_plummer_cluster(21, 20000, 0.004, binary_fraction=0.5)
+    wb = walks.build_walks(cl)
+    with nbody.DeviceNBody(cl, precision=precision) as h:
+        st = h.state()
+        v = h.stats()["kernel_variant"]
+    gpuforce.set_kernel_variant(v)
+    ref = _particle_order(gpuforce.compute(wb, precision), wb)
+    np.testing.assert_array_equal(st["n_ngb"], ref["nnb"])
+    # Same lists, same kernel: equal up to the host packing's rounding of
+    # the quadrupoles, which the host compiler may contract differently.
+    assert rel_err_vec(st["acc"], ref["acc"]).max() <= 1e-9
+    assert rel_err(st["pot"], ref["pot"]).max() <= 1e-9
+    o = _particle_order(oracle.force(wb), wb)
+    np.testing.assert_array_equal(st["n_ngb"], o["nnb"])
+    sa, sp = stats(rel_err_vec(st["acc"], o["acc"])), stats(rel_err(st["pot"], o["pot"]))
+    tol = (MIXED_MEDIAN, MIXED_P999) if precision == PGF_PRECISION_MIXED else (1e-13, 1e-12)
+    assert sa["median"] <= tol[0] and sa["p999"] <= tol[1], sa
+    assert sp["median"] <= tol[0] and sp["p999"] <= tol[1], sp
+
+
+def test_graph_run_equals_eager_run():
+    cl = ics.make_king_cluster(5, 40000, 0.004, W0=7.0, theta=0.4)
+    with nbody.DeviceNBody(cl) as a, nbody.DeviceNBody(cl) as b:
+        a.run(6, 1.0 / 1024, graph=True)
+        b.run(6, 1.0 / 1024, graph=False)
+        sa, sb = a.state(), b.state()
+        for k in ("pos", "vel", "acc", "pot", "n_ngb"):
+            np.testing.assert_array_equal(sa[k], sb[k], err_msg=k)
+        # The cached graph replays: 6 more steps each way stay equal.
+        a.run(6, 1.0 / 1024, graph=True)
+        b.run(6, 1.0 / 1024, graph=False)
+        np.testing.assert_array_equal(a.state()["pos"], b.state()["pos"])
+        assert a.stats()["steps"] == 12
+
+
+def _sample_errors(h, rows_rng, k=4096):
+    """Force errors of the last evaluation on k random particles against the
+    FP64 oracle over the same lists, and the exact neighbour counts."""
+    wb = h.lists()
+    st = h.state()
+    rows = np.sort(rows_rng.choice(h.n, k, replace=False))  # sorted-order rows
+    o = oracle.force(rows_batch(wb, rows))
+    idx = wb.epi_index[rows]
+    np.testing.assert_array_equal(st["n_ngb"][idx], o["nnb"])
+    return stats(rel_err_vec(st["acc"][idx], o["acc"])), stats(rel_err(st["pot"][idx], o["pot"]))
+
+
+def test_king4m_kdk_100_steps_one_graph():
+    cl = ics.make_king_cluster(7, 4194304, 0.0015, W0=7.0, theta=0.4)
+    rng = np.random.default_rng(11)
+    with nbody.DeviceNBody(cl) as h:
+        sa, sp = _sample_errors(h, rng)
+        assert sa["median"] <= MIXED_MEDIAN and sa["p999"] <= MIXED_P999, sa
+        assert sp["median"] <= MIXED_MEDIAN and sp["p999"] <= MIXED_P999, sp
+        ek0, ep0 = h.energy()
+        h.run(100, 1.0 / 1024, graph=True)
+        assert h.stats()["steps"] == 100
+        sa, sp = _sample_errors(h, rng)
+        assert sa["median"] <= MIXED_MEDIAN and sa["p999"] <= MIXED_P999, sa
+        assert sp["median"] <= MIXED_MEDIAN and sp["p999"] <= MIXED_P999, sp
+        ek1, ep1 = h.energy()
+        e0, e1 = ek0 + ep0, ek1 + ep1
+        # Virial-like bound state, and the soft step alone keeps its energy
+        # to a small fraction over 100 steps of 1/1024.
+        assert e0 < 0 and abs((e1 - e0) / e0) < 1e-3, (e0, e1)
+
+
+def test_energy_drift_mixed_equals_fp64():
+    """The same 100-step run with the mixed and the plain FP64 kernels: the
+    energy histories agree far below the drift the integrator itself makes."""
+    cl = ics.make_king_cluster(9, 65536, 0.004, W0=7.0, theta=0.4)
+    out = {}
+    for prec in (PGF_PRECISION_MIXED, PGF_PRECISION_FP64):
+        with nbody.DeviceNBody(cl, precision=prec) as h:
+            e0 = sum(h.energy())
+            h.run(100, 1.0 / 1024, graph=True)
+            e1 = sum(h.energy())
+            out[prec] = (e0, e1, h.state()["pos"])
+    (m0, m1, mp), (d0, d1, dp) = out[PGF_PRECISION_MIXED], out[PGF_PRECISION_FP64]
+    assert abs(m0 - d0) <= 1e-6 * abs(d0)
+    drift_m, drift_d = (m1 - m0) / abs(m0), (d1 - d0) / abs(d0)
+    assert abs(drift_m - drift_d) <= 1e-6, (drift_m, drift_d)
+    assert np.abs(mp - dp).max() <= 1e-6 * np.abs(dp).max()
