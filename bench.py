@@ -21,7 +21,12 @@ Reported (one JSON line from rank 0):
   kernel per launch over its event-timed duration, against an FP32 FMA peak
   measured in the same run;
 * cpu_baseline: the FP64 oracle (a CPU port of the reference functors) on a
-  sample of the walks, with every host thread.
+  sample of the walks, with every host thread;
+* modes: neighbour search, fused changeover and KDKDK_4TH gradient passes on
+  the same lists;
+* kdk_graph: the King W0 = 7, N = 4,194,304 configuration (theta 0.4,
+  r_out 0.0015) run device-resident: tree, lists, force, kicks and drifts of
+  100 leapfrog steps of dt = 1/1024 in one CUDA graph.
 
 ``--impl reference`` times the reference's own CPU path instead (the
 reference functors compiled from its sources when they are present on this
@@ -518,6 +523,11 @@ def run_ours(args):
         modes["gradient_kdkdk"] = {"ms_per_step": t, "value": n_int / t / 1e6, "unit": "Ginteractions/s",
                                    "parity": "tests/test_gpu_parity.py::test_gradient_mode_*"}
 
+    # ---- device-resident tree step: King W0=7, 4M, 100 KDK steps in one CUDA graph ----
+    kdk = None
+    if not args.no_kdk:
+        kdk = run_kdk_graph()
+
     if rank != 0:
         torch.distributed.barrier()
         return
@@ -557,10 +567,39 @@ def run_ours(args):
         "kernel_variant": best_variant, "variant_main_ms": variant_ms,
         "fp64_plain": fp64, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
         "retest_records_per_step": n_retest, "wall_s_timed_region": wall, "modes": modes,
+        "kdk_graph": kdk,
     }
     print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.barrier()
+
+
+def run_kdk_graph(n: int = 4194304, steps: int = 100, dt: float = 1.0 / 1024) -> dict:
+    """The King W0 = 7 configuration as a device-resident run: tree, lists,
+    force, kicks and drifts of `steps` leapfrog steps in one CUDA graph.
+    Throughput counts the interactions of every step's lists over the graph's
+    device time (tree building included)."""
+    from petar_gb300 import ics, nbody
+    clk = ics.make_king_cluster(7, n, 0.0015, W0=7.0, theta=0.4)
+    with nbody.DeviceNBody(clk) as h:
+        variant, _ = h.autotune(2)
+        h.force()
+        st0 = h.stats()
+        e0 = sum(h.energy())
+        h.run(steps, dt, graph=True)  # capture, instantiate and run once
+        st1 = h.stats()
+        e1 = sum(h.energy())
+        ms = h.run(steps, dt, graph=True)  # replay of the instantiated graph
+        st2 = h.stats()
+    inter = (st2["total_epep"] - st1["total_epep"]) + (st2["total_epsp"] - st1["total_epsp"])
+    return {"config": {"model": "King W0=7", "n": n, "theta": 0.4, "r_out": 0.0015, "dt": dt,
+                       "n_leaf_limit": clk.n_leaf_limit, "n_group_limit": clk.n_group_limit},
+            "steps_per_graph": steps, "ms_per_step": ms / steps, "value": inter / (ms * 1e-3) / 1e9,
+            "unit": "Ginteractions/s over whole steps (tree, lists, force, kicks, drifts)",
+            "tree_ms": st0["last_tree_ms"], "force_ms": st0["last_force_ms"],
+            "interactions_per_step": inter / steps, "n_groups": st0["n_groups"], "n_cells": st0["n_cells"],
+            "energy_rel_change_first_graph": (e1 - e0) / abs(e0), "kernel_variant": variant,
+            "parity": "tests/test_gpu_nbody.py"}
 
 
 def main():
@@ -574,6 +613,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-modes", action="store_true", help="skip the search and changeover mode timings")
+    ap.add_argument("--no-kdk", action="store_true", help="skip the device-resident King 4M KDK run")
     ap.add_argument("--variant", type=int, default=-1,
                     help="use this kernel variant instead of the autotuner's choice")
     args = ap.parse_args()
