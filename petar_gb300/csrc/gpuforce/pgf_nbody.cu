@@ -36,12 +36,12 @@
 // creation with room to grow; a build that would overflow any capacity sets
 // an error bit, runs no force kernel and the host reports PGF_ERR_CAPACITY.
 //
-// The walks run as one thread per (group, frontier cell) pair.  The frontier
-// cells are the topmost cells with at most n / 256 particles (or leaves); they
-// partition the particles in Morton order, so the depth-first list of a group
-// is the concatenation, in frontier order, of the lists of the frontier
-// subtrees (a cell above the frontier that the group does not open is listed
-// once, by the first frontier cell below it).  The opening test runs in FP32
+// The walks run as one thread per (group, run of 8 frontier cells).  The
+// frontier cells are the topmost cells with at most n / 1024 particles (or
+// leaves); they partition the particles in Morton order, so the depth-first
+// list of a group is the concatenation, in frontier order, of the lists of
+// the frontier subtrees (a cell above the frontier that the group does not
+// open is listed once, by the first frontier cell below it).  The opening test runs in FP32
 // on rounded copies of the cell data with rigorous bounds on the rounding,
 // and falls back to the FP64 test only where the bounds cannot decide, so the
 // decisions, and the lists, are exactly those of the FP64 test.
@@ -601,21 +601,20 @@ __device__ __forceinline__ int overlap3(const float alo[3], const float ahi[3], 
 
 // r2 <= crit of the FP64 test from rounded data: 1 open, 0 not, 2 unknown.
 // Every coordinate is below X in magnitude, so each rounded input is off by
-// at most u X and each per-axis distance dd by e = 3 u X + u |dd|; the sum of
-// squares then differs from the FP64 one by at most sum e (2 |dd| + e) plus
-// 3 u r2 of its own rounding (bound doubled for the rounding of the bound).
+// at most u X and each per-axis distance dd by at most E = 3 u X + u S, with
+// S the sum of the three rounded distances; the sum of squares then differs
+// from the FP64 one by at most E (2 S + 3 E) plus 3 u r2 of its own rounding
+// (the bound is doubled to cover the rounding of the bound itself).
 __device__ __forceinline__ int dist3(const float glo[3], const float ghi[3], const TCellW& w, float X) {
-    float r2 = 0.f, B = 0.f;
+    float r2 = 0.f, S = 0.f;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        float dd = 0.f;
-        if (w.com[d] < glo[d]) dd = glo[d] - w.com[d];
-        else if (w.com[d] > ghi[d]) dd = w.com[d] - ghi[d];
+        const float dd = fmaxf(fmaxf(glo[d] - w.com[d], w.com[d] - ghi[d]), 0.f);
         r2 += dd * dd;
-        const float e = 3.f * kU * X + kU * dd;
-        B += e * (2.f * dd + e);
+        S += dd;
     }
-    B = 2.f * (B + 3.f * kU * r2);
+    const float E = 3.f * kU * X + kU * S;
+    const float B = 2.f * (E * (2.f * S + 3.f * E) + 3.f * kU * r2);
     if (r2 + B < w.crit * (1.f - 2.f * kU)) return 1;
     if (r2 - B > w.crit * (1.f + 2.f * kU)) return 0;
     return 2;
@@ -659,45 +658,123 @@ __device__ __forceinline__ bool open_cell(const WalkCtx& x, int c, const TCellW&
     return exact_open(x.cells[x.gcell], x.cells[c]);
 }
 
-// The part of a group's depth-first walk that lies in the subtree of frontier
-// cell f: counts (FILL false) or writes (FILL true) its EPJ and SPJ entries in
-// the host builder's order.  A cell above f that the group does not open ends
-// the walk; it is listed by the frontier cell that starts its range.
+// Lists of frontier cell f's subtree for the group of x, appended at ne / ns:
+// counts (FILL false) or writes (FILL true) the entries in the host builder's
+// depth-first order.
 template <bool FILL>
-__device__ void walk_task(const WalkCtx& x, int f, int& ne, int& ns, int32_t* __restrict__ oe,
-                          int32_t* __restrict__ os) {
-    ne = ns = 0;
-    const TCellW fw = x.cw[f];
-    int anc[kLevels];
-    int na = 0;
-    for (int c = fw.parent; c >= 0 && na < kLevels; c = x.cw[c].parent) anc[na++] = c;
-    for (int k = na - 1; k >= 0; --k) {
-        const int a = anc[k];
-        const TCellW aw = x.cw[a];
-        if (!open_cell(x, a, aw)) {
-            if (fw.begin == aw.begin) {
-                if (FILL) os[0] = a;
-                ns = 1;
+__device__ void walk_subtree(const WalkCtx& x, int f, const TCellW& fw, int& ne, int& ns, int32_t* __restrict__ oe,
+                             int32_t* __restrict__ os) {
+    // f itself, then depth-first below it.  Expanding an opened cell decides
+    // all its children at once (independent loads); closed cells and leaves
+    // are listed at once while no opened inner child precedes them, the walk
+    // descends into the first opened inner child, and the later siblings wait
+    // on the stack with their decision (2 low bits: 0 closed, 1 leaf, 2 inner).
+    if (!open_cell(x, f, fw)) {
+        if (FILL) os[ns] = f;
+        ++ns;
+        return;
+    }
+    if (fw.leaf) {
+        if (FILL)
+            for (int i = fw.begin; i < fw.end; ++i) oe[ne + (i - fw.begin)] = i;
+        ne += fw.end - fw.begin;
+        return;
+    }
+    uint32_t stack[kStack];
+    int sp = 0;
+    int fc = fw.first_child, nc = fw.n_child;
+    for (;;) {
+        uint32_t dec = 0;
+        int next = -1, next_fc = 0, next_nc = 0;
+        for (int k = 0; k < nc; ++k) {
+            const int c = fc + k;
+            const TCellW w = x.cw[c];
+            const int code = !open_cell(x, c, w) ? 0 : (w.leaf ? 1 : 2);
+            if (next < 0) {
+                if (code == 0) {
+                    if (FILL) os[ns] = c;
+                    ++ns;
+                } else if (code == 1) {
+                    if (FILL)
+                        for (int i = w.begin; i < w.end; ++i) oe[ne + (i - w.begin)] = i;
+                    ne += w.end - w.begin;
+                } else {
+                    next = k;
+                    next_fc = w.first_child;
+                    next_nc = w.n_child;
+                }
+            } else {
+                dec |= (uint32_t)code << (2 * k);
             }
-            return;
+        }
+        if (next >= 0) {
+            for (int k = nc - 1; k > next; --k) stack[sp++] = ((uint32_t)(fc + k) << 2) | ((dec >> (2 * k)) & 3u);
+            fc = next_fc;
+            nc = next_nc;
+            continue;
+        }
+        for (;;) {
+            if (sp == 0) return;
+            const uint32_t e = stack[--sp];
+            const int c = (int)(e >> 2);
+            const uint32_t code = e & 3u;
+            if (code == 0) {
+                if (FILL) os[ns] = c;
+                ++ns;
+            } else if (code == 1) {
+                const int b0 = x.cw[c].begin, b1 = x.cw[c].end;
+                if (FILL)
+                    for (int i = b0; i < b1; ++i) oe[ne + (i - b0)] = i;
+                ne += b1 - b0;
+            } else {
+                fc = x.cw[c].first_child;
+                nc = x.cw[c].n_child;
+                break;
+            }
         }
     }
-    int stack[kStack];
-    int sp = 0;
-    stack[sp++] = f;
-    while (sp > 0) {
-        const int c = stack[--sp];
-        const TCellW w = x.cw[c];
-        if (!open_cell(x, c, w)) {
-            if (FILL) os[ns] = c;
-            ++ns;
-        } else if (w.leaf) {
-            if (FILL)
-                for (int i = w.begin; i < w.end; ++i) oe[ne + (i - w.begin)] = i;
-            ne += w.end - w.begin;
-        } else {
-            for (int k = w.n_child - 1; k >= 0; --k) stack[sp++] = w.first_child + k;
+}
+
+// Frontier cells f0 .. f1-1 (consecutive in frontier order) for one group.
+// A frontier cell is walked if the group opens all its ancestors; a closed
+// ancestor ends it and is listed by the frontier cell that starts its range.
+// The decisions along the current ancestor chain are kept, so consecutive
+// frontier cells test only the ancestors they do not share.
+template <bool FILL>
+__device__ void walk_chunk(const WalkCtx& x, const int32_t* __restrict__ fronts, int f0, int f1, int& ne, int& ns,
+                           int32_t* __restrict__ oe, int32_t* __restrict__ os) {
+    ne = ns = 0;
+    int cache_c[kLevels];
+    bool cache_open[kLevels];
+    int n_cached = 0;
+    for (int fi = f0; fi < f1; ++fi) {
+        const int f = fronts[fi];
+        const TCellW fw = x.cw[f];
+        int chain[kLevels];  // ancestors, parent first
+        int na = 0;
+        for (int c = fw.parent; c >= 0 && na < kLevels; c = x.cw[c].parent) chain[na++] = c;
+        bool closed = false;
+        for (int k = 0; k < na; ++k) {  // root first
+            const int a = chain[na - 1 - k];
+            bool op;
+            if (k < n_cached && cache_c[k] == a) {
+                op = cache_open[k];
+            } else {
+                op = open_cell(x, a, x.cw[a]);
+                cache_c[k] = a;
+                cache_open[k] = op;
+                n_cached = k + 1;
+            }
+            if (!op) {
+                if (fw.begin == x.cw[a].begin) {
+                    if (FILL) os[ns] = a;
+                    ++ns;
+                }
+                closed = true;
+                break;
+            }
         }
+        if (!closed) walk_subtree<FILL>(x, f, fw, ne, ns, oe, os);
     }
 }
 
@@ -707,28 +784,33 @@ __device__ __forceinline__ int cost_bucket(float cost) {
     return b < kBuckets ? b : kBuckets - 1;
 }
 
+constexpr int kChunk = 8;  // frontier cells per task
+
+__device__ __forceinline__ int64_t n_chunks(const TreeHdr* h) { return (h->n_fronts + kChunk - 1) / kChunk; }
+
 __global__ void task_check_kernel(TreeHdr* h, int64_t cap_tasks) {
     if (threadIdx.x != 0 || h->err) return;
-    if ((int64_t)h->n_groups * h->n_fronts > cap_tasks) h->err |= kErrTasks;
+    if ((int64_t)h->n_groups * n_chunks(h) > cap_tasks) h->err |= kErrTasks;
 }
 
-// Task t = (frontier f = t / n_groups, group g = t % n_groups): the threads of
-// a warp walk one subtree for neighbouring groups.  Counts are stored at
-// f * n_groups + g.
+// Task t = (chunk q = t / n_groups, group g = t % n_groups) walks frontier
+// cells kChunk q .. kChunk q + kChunk - 1 for group g: the threads of a warp
+// walk the same subtrees for neighbouring groups.  Counts are stored at t.
 __global__ __launch_bounds__(128) void walk_task_count_kernel(const TreeHdr* h, const TCellW* __restrict__ cw,
                                                               const TCell* __restrict__ cells,
                                                               const int32_t* __restrict__ groups,
                                                               const int32_t* __restrict__ fronts, int32_t* task_e,
                                                               int32_t* task_s, bool open_all) {
     if (h->err) return;
-    const int64_t ng = h->n_groups, nf = h->n_fronts, T = ng * nf;
+    const int64_t ng = h->n_groups, nf = h->n_fronts, T = ng * n_chunks(h);
     const float X = h->xmax;
     for (int64_t t = gtid(); t < T; t += gstride()) {
-        const int f = (int)(t / ng), g = (int)(t - (int64_t)f * ng);
+        const int q = (int)(t / ng), g = (int)(t - (int64_t)q * ng);
         WalkCtx x;
         load_ctx(x, cw, cells, groups[g], X, open_all);
         int ne, ns;
-        walk_task<false>(x, fronts[f], ne, ns, nullptr, nullptr);
+        walk_chunk<false>(x, fronts, q * kChunk, (int)min(nf, (int64_t)(q + 1) * kChunk), ne, ns, nullptr,
+                          nullptr);
         task_e[t] = ne;
         task_s[t] = ns;
     }
@@ -741,11 +823,12 @@ __global__ __launch_bounds__(128) void group_reduce_kernel(TreeHdr* h, const TCe
                                                            int32_t* task_e, int32_t* task_s, int32_t* cnt_e,
                                                            int32_t* cnt_s, int32_t* bucket, double rcut2) {
     if (h->err) return;
-    const int64_t ng = h->n_groups, nf = h->n_fronts;
+    const int64_t ng = h->n_groups, nq = n_chunks(h);
     for (int64_t g = gtid(); g < ng; g += gstride()) {
         int64_t re = 0, rs = 0;
-        for (int64_t f = 0; f < nf; ++f) {
-            const int64_t t = f * ng + g;
+#pragma unroll 8
+        for (int64_t q = 0; q < nq; ++q) {
+            const int64_t t = q * ng + g;
             const int e = task_e[t], s = task_s[t];
             task_e[t] = (int32_t)re;
             task_s[t] = (int32_t)rs;
@@ -821,15 +904,16 @@ __global__ __launch_bounds__(128) void walk_task_fill_kernel(const TreeHdr* h, c
                                                              const int32_t* __restrict__ task_s, int32_t* id_epj,
                                                              int32_t* id_spj, bool open_all) {
     if (h->err) return;
-    const int64_t ng = h->n_groups, nf = h->n_fronts, T = ng * nf;
+    const int64_t ng = h->n_groups, nf = h->n_fronts, T = ng * n_chunks(h);
     const float X = h->xmax;
     for (int64_t t = gtid(); t < T; t += gstride()) {
-        const int f = (int)(t / ng), g = (int)(t - (int64_t)f * ng);
+        const int q = (int)(t / ng), g = (int)(t - (int64_t)q * ng);
         WalkCtx x;
         load_ctx(x, cw, cells, groups[g], X, open_all);
         const WalkDesc& d = walks[g];
         int ne, ns;
-        walk_task<true>(x, fronts[f], ne, ns, id_epj + d.epj_begin + task_e[t], id_spj + d.spj_begin + task_s[t]);
+        walk_chunk<true>(x, fronts, q * kChunk, (int)min(nf, (int64_t)(q + 1) * kChunk), ne, ns,
+                         id_epj + d.epj_begin + task_e[t], id_spj + d.spj_begin + task_s[t]);
     }
 }
 
@@ -1234,7 +1318,7 @@ int build_fit(pgf_nbody* h) {
                 NB_CUDA(h->id_spj.alloc(h->cap_s));
                 grown = true;
             }
-            const double tasks = (double)t.n_groups * (double)t.n_fronts;
+            const double tasks = (double)t.n_groups * (double)((t.n_fronts + kChunk - 1) / kChunk);
             if ((double)h->cap_tasks < f * tasks) {
                 NB_CUDA(alloc_tasks(h, (int64_t)(f * tasks) + 1024));
                 grown = true;
@@ -1258,7 +1342,8 @@ int build_fit(pgf_nbody* h) {
             h->cap_s = (int64_t)(f * (double)t.n_spj_entries) + 1024;
             NB_CUDA(h->id_spj.alloc(h->cap_s));
         }
-        if (t.err & kErrTasks) NB_CUDA(alloc_tasks(h, (int64_t)(f * (double)t.n_groups * (double)t.n_fronts) + 1024));
+        if (t.err & kErrTasks)
+            NB_CUDA(alloc_tasks(h, (int64_t)(f * (double)t.n_groups * (double)((t.n_fronts + kChunk - 1) / kChunk)) + 1024));
         bind_params(h);
     }
     return nb_fail(PGF_ERR_CAPACITY, "device list builder did not fit after 16 attempts");
@@ -1330,7 +1415,7 @@ int pgf_nbody_create(const pgf_nbody_config* cfg, int64_t n, const double* pos, 
     NB_TRY(alloc_cells(h, (int)std::min<int64_t>(4 * (n / (cfg->n_leaf_limit + 1)) + 1024, 1 << 30)));
     for (auto* a : {&h->group_at, &h->groups, &h->cnt_e, &h->cnt_s, &h->bucket, &h->queue, &h->front_at, &h->fronts})
         NB_TRY(a->alloc(n));
-    h->front_limit = (int)std::max<int64_t>(cfg->n_group_limit, n / 256);
+    h->front_limit = (int)std::max<int64_t>(cfg->n_group_limit, n / 1024);
     NB_TRY(alloc_tasks(h, 64 * (n / std::max(1, cfg->n_group_limit / 4) + 1) + 4096));
     NB_TRY(h->walks.alloc(n));
     h->cap_e = 64 * n + 1024;
