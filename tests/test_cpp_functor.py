@@ -56,3 +56,48 @@ def test_functor_matches_oracle(tmp_path):
     np.testing.assert_array_equal(nnb, o["nnb"])
     assert np.median(rel_err_vec(acc, o["acc"])) < 1e-6
     assert np.median(np.abs(pot - o["pot"]) / np.abs(o["pot"])) < 1e-6
+
+
+NBODY_SRC = ROOT / "tests" / "cpp" / "nbody_test.cpp"
+
+
+def compile_nbody_driver(tmp_path: Path) -> Path:
+    lib = build_gpuforce()
+    exe = tmp_path / "nbody_test"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(NBODY_SRC), "-o", str(exe),
+                    "-L", str(lib.parent), "-lpetar_gpuforce", f"-Wl,-rpath,{lib.parent}"], check=True)
+    return exe
+
+
+def test_nbody_wrapper_compiles(tmp_path):
+    assert compile_nbody_driver(tmp_path).exists()
+
+
+@pytest.mark.gpu
+def test_nbody_wrapper_matches_python_binding(tmp_path):
+    """The C++ DeviceTreeStep and the Python binding run the same steps on
+    the same library: results agree bit for bit."""
+    from petar_gb300 import ics, nbody
+    exe = compile_nbody_driver(tmp_path)
+    cl = ics.make_plummer_cluster(8, 8192, 0.01, binary_fraction=0.2)
+    steps, dt = 4, 1.0 / 1024
+    with open(tmp_path / "in.bin", "wb") as f:
+        np.array([cl.n, steps], np.int64).tofile(f)
+        np.array([dt, cl.eps ** 2, cl.r_out, cl.G, cl.theta], np.float64).tofile(f)
+        np.array([cl.n_leaf_limit, cl.n_group_limit], np.int32).tofile(f)
+        for a in (cl.pos, cl.vel, cl.mass, cl.r_search):
+            np.ascontiguousarray(a, np.float64).tofile(f)
+    subprocess.run([str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin")], check=True)
+    n = cl.n
+    raw = np.fromfile(tmp_path / "out.bin", np.uint8)
+    pos = raw[:24 * n].view(np.float64).reshape(n, 3)
+    acc = raw[24 * n:48 * n].view(np.float64).reshape(n, 3)
+    pot = raw[48 * n:56 * n].view(np.float64)
+    nnb = raw[56 * n:60 * n].view(np.int32)
+    with nbody.DeviceNBody(cl) as h:
+        h.run(steps, dt, graph=True)
+        st = h.state()
+    np.testing.assert_array_equal(pos, st["pos"])
+    np.testing.assert_array_equal(acc, st["acc"])
+    np.testing.assert_array_equal(pot, st["pot"])
+    np.testing.assert_array_equal(nnb, st["n_ngb"])
