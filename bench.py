@@ -24,6 +24,9 @@ Reported (one JSON line from rank 0):
   sample of the walks, with every host thread;
 * modes: neighbour search, fused changeover and KDKDK_4TH gradient passes on
   the same lists;
+* configs: Plummer N = 65,536 (mixed against the plain FP64 kernel) and the
+  64-cluster ensemble in one launch (against 64 sequential plain FP64
+  launches), each timed on its own resident lists;
 * kdk_graph: the King W0 = 7, N = 4,194,304 configuration (theta 0.4,
   r_out 0.0015) run device-resident: tree, lists, force, kicks and drifts of
   100 leapfrog steps of dt = 1/1024 in one CUDA graph.
@@ -523,6 +526,12 @@ def run_ours(args):
         modes["gradient_kdkdk"] = {"ms_per_step": t, "value": n_int / t / 1e6, "unit": "Ginteractions/s",
                                    "parity": "tests/test_gpu_parity.py::test_gradient_mode_*"}
 
+    # ---- the other named configurations: Plummer 65k and the 64-cluster ensemble ----
+    configs = None
+    if not args.no_configs:
+        configs = run_configs(stream, flush)
+        gpuforce.set_precision(PGF_PRECISION_MIXED)
+
     # ---- device-resident tree step: King W0=7, 4M, 100 KDK steps in one CUDA graph ----
     kdk = None
     if not args.no_kdk:
@@ -567,11 +576,86 @@ def run_ours(args):
         "kernel_variant": best_variant, "variant_main_ms": variant_ms,
         "fp64_plain": fp64, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
         "retest_records_per_step": n_retest, "wall_s_timed_region": wall, "modes": modes,
-        "kdk_graph": kdk,
+        "kdk_graph": kdk, "configs": configs,
     }
     print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.barrier()
+
+
+def _time_tag(tag: int, stream, flush, reps: int = 3) -> float:
+    """Mean event time (ms) of re-running a tag's kernels on resident data,
+    the L2 flushed before each run; the first run is a warm-up."""
+    import torch
+    from petar_gb300 import gpuforce
+    ts = []
+    for _ in range(reps + 1):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        gpuforce.recompute(tag)
+        e1.record(stream)
+        gpuforce.wait(tag)
+        ts.append(e0.elapsed_time(e1))
+    return statistics.mean(ts[1:])
+
+
+def run_configs(stream, flush) -> dict:
+    """Plummer N = 65,536 (theta 0.3, r_out 0.008): mixed against the plain
+    FP64 kernel on the same lists.  Ensemble: 64 Plummer clusters, N
+    log-uniform in [1024, 65536], 30% binaries, r_out = 0.05 N^(-1/3), all
+    walks in one mixed-precision launch against 64 sequential launches of the
+    plain FP64 kernel (and of the mixed one), one per cluster."""
+    from petar_gb300 import gpuforce, ics, walks
+    from petar_gb300.gpuforce import PGF_PRECISION_FP64, PGF_PRECISION_MIXED
+    out = {}
+    tag = 4
+    cl = ics.make_plummer_cluster(2, 65536, 0.008)
+    wb = walks.build_walks(cl)
+    rec = gpuforce.Records(wb)
+    n = sum(wb.interactions())
+    t = {}
+    for prec in (PGF_PRECISION_MIXED, PGF_PRECISION_FP64):
+        gpuforce.set_precision(prec)
+        gpuforce.dispatch(rec, tag=tag)
+        gpuforce.retrieve(rec, tag=tag)
+        t[prec] = _time_tag(tag, stream, flush)
+    out["plummer65k"] = {"n": int(cl.n), "n_walk": int(wb.n_walk), "interactions": int(n),
+                         "mixed_ms": t[PGF_PRECISION_MIXED], "fp64_ms": t[PGF_PRECISION_FP64],
+                         "mixed_value": n / t[PGF_PRECISION_MIXED] / 1e6, "fp64_value": n / t[PGF_PRECISION_FP64] / 1e6,
+                         "unit": "Ginteractions/s", "speedup_mixed_vs_fp64": t[PGF_PRECISION_FP64] / t[PGF_PRECISION_MIXED],
+                         "parity": "tests/test_gpu_configs.py::test_plummer65k_against_oracle_and_direct_sum"}
+    rng = np.random.default_rng(5)
+    ns = np.round(np.exp(rng.uniform(np.log(1024), np.log(65536), 64))).astype(int)
+    bs = []
+    for k, nk in enumerate(ns):
+        c = ics.make_plummer_cluster(500 + k, int(nk), 0.05 * nk ** (-1 / 3), binary_fraction=0.3)
+        b = walks.build_walks(c)
+        b.walk_rcut2 = np.full(b.n_walk, c.r_out ** 2)
+        bs.append(b)
+    seq = {PGF_PRECISION_MIXED: 0.0, PGF_PRECISION_FP64: 0.0}
+    for b in bs:
+        r = gpuforce.Records(b)
+        for prec in seq:
+            gpuforce.set_precision(prec)
+            gpuforce.dispatch(r, tag=tag)
+            gpuforce.retrieve(r, tag=tag)
+            seq[prec] += _time_tag(tag, stream, flush, reps=1)
+    wbe = walks.concat_batches(bs)
+    r = gpuforce.Records(wbe)
+    gpuforce.set_precision(PGF_PRECISION_MIXED)
+    gpuforce.dispatch(r, tag=tag)
+    gpuforce.retrieve(r, tag=tag)
+    t1 = _time_tag(tag, stream, flush)
+    n = sum(wbe.interactions())
+    out["ensemble64"] = {"n_clusters": 64, "n": int(sum(ns)), "n_walk": int(wbe.n_walk), "interactions": int(n),
+                         "mixed_one_launch_ms": t1, "fp64_64_launches_ms": seq[PGF_PRECISION_FP64],
+                         "mixed_64_launches_ms": seq[PGF_PRECISION_MIXED], "mixed_value": n / t1 / 1e6,
+                         "unit": "Ginteractions/s",
+                         "speedup_vs_64_fp64_launches": seq[PGF_PRECISION_FP64] / t1,
+                         "speedup_vs_64_mixed_launches": seq[PGF_PRECISION_MIXED] / t1,
+                         "parity": "tests/test_gpu_configs.py::test_ensemble64_one_launch"}
+    return out
 
 
 def run_kdk_graph(n: int = 4194304, steps: int = 100, dt: float = 1.0 / 1024) -> dict:
@@ -614,6 +698,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-modes", action="store_true", help="skip the search and changeover mode timings")
     ap.add_argument("--no-kdk", action="store_true", help="skip the device-resident King 4M KDK run")
+    ap.add_argument("--no-configs", action="store_true", help="skip the Plummer 65k and ensemble timings")
     ap.add_argument("--variant", type=int, default=-1,
                     help="use this kernel variant instead of the autotuner's choice")
     args = ap.parse_args()
