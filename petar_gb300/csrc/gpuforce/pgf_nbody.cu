@@ -1291,6 +1291,12 @@ cudaError_t alloc_tasks(pgf_nbody* h, int64_t cap) {
     return e;
 }
 
+void drop_graph(pgf_nbody* h) {
+    if (h->exec) cudaGraphExecDestroy(h->exec);
+    h->exec = nullptr;
+    h->graph_steps = 0;
+}
+
 // Eager build at the current positions, growing the capacities until the
 // tree and the lists fit (with the configured room on top).
 int build_fit(pgf_nbody* h) {
@@ -1302,33 +1308,40 @@ int build_fit(pgf_nbody* h) {
         TreeHdr t;
         if (int r = read_hdr(h, &t)) return r;
         if (t.err == 0) {
-            const int64_t nc = t.level_begin[kLevels];
-            bool grown = false;
-            if ((double)h->cap_cells < f * (double)nc) {
-                NB_CUDA(alloc_cells(h, (int)std::min<double>(f * (double)nc + 64, 2147483000.0)));
-                grown = true;
+            // Size every array to list_capacity_factor times what this build
+            // used (growing or shrinking), then build again into the new
+            // arrays; an array already within [1, 2] times that target stays.
+            auto off = [](double cap, double target) { return cap < target || cap > 2.0 * target; };
+            bool resized = false;
+            const double tc = f * (double)t.level_begin[kLevels] + 64;
+            if (off(h->cap_cells, tc)) {
+                NB_CUDA(alloc_cells(h, (int)std::min<double>(std::ceil(tc), 1073741824.0)));
+                resized = true;
             }
-            if ((double)h->cap_e < f * (double)t.n_epj_entries) {
-                h->cap_e = (int64_t)(f * (double)t.n_epj_entries) + 1024;
+            const double te = f * (double)t.n_epj_entries + 1024;
+            if (off((double)h->cap_e, te)) {
+                h->cap_e = (int64_t)std::ceil(te);
                 NB_CUDA(h->id_epj.alloc(h->cap_e));
-                grown = true;
+                resized = true;
             }
-            if ((double)h->cap_s < f * (double)t.n_spj_entries) {
-                h->cap_s = (int64_t)(f * (double)t.n_spj_entries) + 1024;
+            const double ts = f * (double)t.n_spj_entries + 1024;
+            if (off((double)h->cap_s, ts)) {
+                h->cap_s = (int64_t)std::ceil(ts);
                 NB_CUDA(h->id_spj.alloc(h->cap_s));
-                grown = true;
+                resized = true;
             }
-            const double tasks = (double)t.n_groups * (double)((t.n_fronts + kChunk - 1) / kChunk);
-            if ((double)h->cap_tasks < f * tasks) {
-                NB_CUDA(alloc_tasks(h, (int64_t)(f * tasks) + 1024));
-                grown = true;
+            const double tt = f * (double)t.n_groups * (double)((t.n_fronts + kChunk - 1) / kChunk) + 1024;
+            if (off((double)h->cap_tasks, tt)) {
+                NB_CUDA(alloc_tasks(h, (int64_t)std::ceil(tt)));
+                resized = true;
             }
-            if (!grown) {
+            if (!resized) {
                 NB_CUDA(cudaMemsetAsync(&h->hdr.d->err_sticky, 0, sizeof(int32_t), h->stream));
                 return PGF_OK;
             }
+            drop_graph(h);
             bind_params(h);
-            continue;  // rebuild into the new arrays
+            continue;
         }
         if (t.err & kErrCells) {
             if (h->cap_cells >= 1 << 30) return nb_fail(PGF_ERR_CAPACITY, "more than 2^30 tree cells");
@@ -1344,6 +1357,7 @@ int build_fit(pgf_nbody* h) {
         }
         if (t.err & kErrTasks)
             NB_CUDA(alloc_tasks(h, (int64_t)(f * (double)t.n_groups * (double)((t.n_fronts + kChunk - 1) / kChunk)) + 1024));
+        drop_graph(h);
         bind_params(h);
     }
     return nb_fail(PGF_ERR_CAPACITY, "device list builder did not fit after 16 attempts");
@@ -1418,8 +1432,8 @@ int pgf_nbody_create(const pgf_nbody_config* cfg, int64_t n, const double* pos, 
     h->front_limit = (int)std::max<int64_t>(cfg->n_group_limit, n / 1024);
     NB_TRY(alloc_tasks(h, 64 * (n / std::max(1, cfg->n_group_limit / 4) + 1) + 4096));
     NB_TRY(h->walks.alloc(n));
-    h->cap_e = 64 * n + 1024;
-    h->cap_s = 16 * n + 1024;
+    h->cap_e = 8 * n + 1024;  // first guesses; the first build sizes them
+    h->cap_s = 8 * n + 1024;
     NB_TRY(h->id_epj.alloc(h->cap_e));
     NB_TRY(h->id_spj.alloc(h->cap_s));
     NB_TRY(h->out_accp.alloc(n));
@@ -1451,8 +1465,15 @@ int pgf_nbody_create(const pgf_nbody_config* cfg, int64_t n, const double* pos, 
     return PGF_OK;
 }
 
-int pgf_nbody_force(pgf_nbody* h) {
-    if (!h) return nb_fail(PGF_ERR_ARG, "NULL handle");
+// Clears the sticky build error and the kernels' error word before a call.
+static int clear_errors(pgf_nbody* h) {
+    NB_CUDA(cudaMemsetAsync(&h->hdr.d->err_sticky, 0, sizeof(int32_t), h->stream));
+    NB_CUDA(cudaMemsetAsync(h->flags.d + 2, 0, sizeof(int32_t), h->stream));
+    return PGF_OK;
+}
+
+static int force_once(pgf_nbody* h) {
+    if (int r = clear_errors(h)) return r;
     NB_CUDA(cudaEventRecord(h->ev[0], h->stream));
     NB_CUDA(enqueue_build(h));
     NB_CUDA(cudaEventRecord(h->ev[1], h->stream));
@@ -1466,6 +1487,16 @@ int pgf_nbody_force(pgf_nbody* h) {
     h->last_tree_ms = a;
     h->last_force_ms = b;
     return check_errors(h);
+}
+
+int pgf_nbody_force(pgf_nbody* h) {
+    if (!h) return nb_fail(PGF_ERR_ARG, "NULL handle");
+    int r = force_once(h);
+    if (r != PGF_ERR_CAPACITY) return r;
+    // The lists outgrew their arrays: grow them (dropping any captured
+    // graph, which holds the old addresses) and evaluate again.
+    if ((r = build_fit(h)) != PGF_OK) return r;
+    return force_once(h);
 }
 
 int pgf_nbody_run(pgf_nbody* h, int n_steps, double dt, int use_graph, double* ms) {
@@ -1499,6 +1530,7 @@ int pgf_nbody_run(pgf_nbody* h, int n_steps, double dt, int use_graph, double* m
         h->graph_steps = n_steps;
         h->graph_dt = dt;
     }
+    if (int r = clear_errors(h)) return r;
     NB_CUDA(cudaEventRecord(h->ev[3], h->stream));
     if (use_graph) {
         NB_CUDA(cudaGraphLaunch(h->exec, h->stream));

@@ -133,3 +133,24 @@ def test_energy_drift_mixed_equals_fp64():
     drift_m, drift_d = (m1 - m0) / abs(m0), (d1 - d0) / abs(d0)
     assert abs(drift_m - drift_d) <= 1e-6, (drift_m, drift_d)
     assert np.abs(mp - dp).max() <= 1e-6 * np.abs(dp).max()
+
+
+def test_list_overflow_is_reported_and_force_recovers():
+    """Arrays sized exactly for the first build (capacity factor 1): a denser
+    configuration overflows them inside a graph run, which reports
+    PGF_ERR_CAPACITY without touching memory out of range; force() then grows
+    the arrays, and the lists equal the host builder's again."""
+    cl = ics.make_plummer_cluster(31, 20000, 0.004, binary_fraction=0.3)
+    with nbody.DeviceNBody(cl, list_capacity_factor=1.0) as h:
+        dense = cl.pos * 0.01  # r_search boxes now reach far more cells: EPJ lists double
+        h.set_state(pos=dense)
+        with pytest.raises(gpuforce.GpuForceError) as e:
+            h.run(1, 1e-9, graph=True)
+        assert e.value.code == 5, e.value
+        h.set_state(pos=dense, vel=cl.vel)
+        h.force()
+        dev = h.lists()
+    cl.pos = dense
+    host = walks.build_walks(cl)
+    for k in ("epi_index", "epi_disp", "epj_disp", "spj_disp", "id_epj", "id_spj"):
+        np.testing.assert_array_equal(getattr(dev, k), getattr(host, k), err_msg=k)
