@@ -11,8 +11,8 @@
 //
 // Design: a persistent CTA-synchronous kernel (one pass is as heavy as a force
 // evaluation, but it runs once per step).  256 threads pop walks from the
-// cost-sorted queue; a pass holds up to 256 i, one per thread, and
-// floor(256 / n_i) threads share each i as j-slices.  Threads stage 128-entry
+// cost-sorted queue; a pass holds up to 512 i, two per thread, and the
+// threads form floor(256 / ceil(n_i / 2)) j-slices.  Threads stage 128-entry
 // EPJ tiles (positions as walk-relative (hi, lo) pairs from the FP32 split
 // arrays, accelerations as (hi, lo) pairs) and 64-entry SPJ tiles in shared
 // memory.  Pair arithmetic is FP32 with both halves, so dr and da are accurate
@@ -40,13 +40,14 @@ __device__ __forceinline__ void two_sum_g(float a, float b, float& s, float& e) 
     e = (a - (s - bb)) + (b - bb);
 }
 
+template <int KU>
 struct SmemG {
     float4 ph[kTileEPG];  // EPJ: walk-relative position hi, mass
     float4 pl[kTileEPG];  // EPJ: walk-relative position lo
     float4 ah[kTileEPG];  // EPJ: acceleration hi
     float4 al[kTileEPG];  // EPJ: acceleration lo
     float4 sp[kTileSPG][3];
-    float2 acc[7][kThreadsG];  // flushed partials: acorr x, y, z, SP acc x, y, z, SP pot
+    float2 acc[KU][7][kThreadsG];  // flushed partials: acorr x, y, z, SP acc x, y, z, SP pot
     int w;
 };
 
@@ -56,9 +57,13 @@ __device__ __forceinline__ void flush_into(float2& v, float x) {
     v.y += e;
 }
 
+// KU i-particles per thread: i = li + k S (k < KU) of a pass of up to
+// 256 KU i, with S = ceil(n_i / KU) threads per j-slice; every j read from
+// shared memory serves KU pairs.
+template <int KU>
 __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel(Params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    SmemG& s = *reinterpret_cast<SmemG*>(smem_raw);
+    SmemG<KU>& s = *reinterpret_cast<SmemG<KU>*>(smem_raw);
     const int tid = threadIdx.x;
     const float eps2 = (float)p.eps2;
     const int n_walk = walk_count(p);
@@ -73,42 +78,57 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel(Params p) {
         const float clx = (float)(wd.cx - (double)chx), cly = (float)(wd.cy - (double)chy),
                     clz = (float)(wd.cz - (double)chz);
         const float rcut2 = (float)wd.rcut2;
-        for (int ipass = 0; ipass < wd.n_i; ipass += kThreadsG) {
-            const int nip = min(kThreadsG, wd.n_i - ipass);
-            const int n_js = kThreadsG / nip;
-            const int js = tid / nip;
-            const int li = tid - js * nip;
+        for (int ipass = 0; ipass < wd.n_i; ipass += kThreadsG * KU) {
+            const int nip = min(kThreadsG * KU, wd.n_i - ipass);
+            const int S = (nip + KU - 1) / KU;
+            const int n_js = kThreadsG / S;
+            const int js = tid / S;
+            const int li = tid - js * S;
             const bool active = js < n_js;
-            const int gi = wd.i_begin + ipass + li;
-            float xh = 0.f, yh = 0.f, zh = 0.f, xl = 0.f, yl = 0.f, zl = 0.f;
-            float axh = 0.f, ayh = 0.f, azh = 0.f, axl = 0.f, ayl = 0.f, azl = 0.f;
-            if (active) {
-                const EpiDev e = p.epi[gi];
-                const double dx = e.x - wd.cx, dy = e.y - wd.cy, dz = e.z - wd.cz;
-                xh = (float)dx;
-                yh = (float)dy;
-                zh = (float)dz;
-                xl = (float)(dx - (double)xh);
-                yl = (float)(dy - (double)yh);
-                zl = (float)(dz - (double)zh);
-                const Accp a = p.epi_acc64[gi];
-                axh = (float)a.x;
-                ayh = (float)a.y;
-                azh = (float)a.z;
-                axl = (float)(a.x - (double)axh);
-                ayl = (float)(a.y - (double)ayh);
-                azl = (float)(a.z - (double)azh);
+            float xh[KU], yh[KU], zh[KU], xl[KU], yl[KU], zl[KU];
+            float axh[KU], ayh[KU], azh[KU], axl[KU], ayl[KU], azl[KU];
+#pragma unroll
+            for (int k = 0; k < KU; ++k) {
+                xh[k] = yh[k] = zh[k] = xl[k] = yl[k] = zl[k] = 0.f;
+                axh[k] = ayh[k] = azh[k] = axl[k] = ayl[k] = azl[k] = 0.f;
+                const int ii = li + k * S;
+                if (active && ii < nip) {
+                    const int gi = wd.i_begin + ipass + ii;
+                    const EpiDev e = p.epi[gi];
+                    const double dx = e.x - wd.cx, dy = e.y - wd.cy, dz = e.z - wd.cz;
+                    xh[k] = (float)dx;
+                    yh[k] = (float)dy;
+                    zh[k] = (float)dz;
+                    xl[k] = (float)(dx - (double)xh[k]);
+                    yl[k] = (float)(dy - (double)yh[k]);
+                    zl[k] = (float)(dz - (double)zh[k]);
+                    const Accp a = p.epi_acc64[gi];
+                    axh[k] = (float)a.x;
+                    ayh[k] = (float)a.y;
+                    azh[k] = (float)a.z;
+                    axl[k] = (float)(a.x - (double)axh[k]);
+                    ayl[k] = (float)(a.y - (double)ayh[k]);
+                    azl[k] = (float)(a.z - (double)azh[k]);
+                }
             }
 #pragma unroll
-            for (int q = 0; q < 7; ++q) s.acc[q][tid] = make_float2(0.f, 0.f);
-            float g[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            for (int k = 0; k < KU; ++k)
+#pragma unroll
+                for (int q = 0; q < 7; ++q) s.acc[k][q][tid] = make_float2(0.f, 0.f);
+            float g[KU][7];
+#pragma unroll
+            for (int k = 0; k < KU; ++k)
+#pragma unroll
+                for (int q = 0; q < 7; ++q) g[k][q] = 0.f;
             int since = 0;
             auto flush = [&]() {
 #pragma unroll
-                for (int q = 0; q < 7; ++q) {
-                    flush_into(s.acc[q][tid], g[q]);
-                    g[q] = 0.f;
-                }
+                for (int k = 0; k < KU; ++k)
+#pragma unroll
+                    for (int q = 0; q < 7; ++q) {
+                        flush_into(s.acc[k][q][tid], g[k][q]);
+                        g[k][q] = 0.f;
+                    }
                 since = 0;
             };
             // EPJ tiles: the gradient correction of every pair.
@@ -135,28 +155,30 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel(Params p) {
                 if (active) {
                     const int pn = (nt + n_js - 1) / n_js;
                     const int j0 = min(nt, js * pn), j1 = min(nt, j0 + pn);
-#pragma unroll 2
                     for (int j = j0; j < j1; ++j) {
                         const float4 ph = s.ph[j], pl = s.pl[j], ah = s.ah[j], al = s.al[j];
-                        // x_j - x_i and a_j - a_i from both halves
-                        const float dx = (ph.x - xh) + (pl.x - xl);
-                        const float dy = (ph.y - yh) + (pl.y - yl);
-                        const float dz = (ph.z - zh) + (pl.z - zl);
-                        const float dax = (ah.x - axh) + (al.x - axl);
-                        const float day = (ah.y - ayh) + (al.y - ayl);
-                        const float daz = (ah.z - azh) + (al.z - azl);
-                        float r2 = fmaf(dx, dx, eps2);
-                        r2 = fmaf(dy, dy, r2);
-                        r2 = fmaf(dz, dz, r2);
-                        const float ri = rsqrt_approx_g(fmaxf(r2, rcut2));
-                        const float ri2 = ri * ri;
-                        const float mr3 = ph.w * ri * ri2;
-                        const float drda = fmaf(dx, dax, fmaf(dy, day, dz * daz));
-                        const float alpha = 3.f * drda * ri2;
-                        // -m/r^3 (da - alpha dr) with dr = -d, da = -(a_j - a_i)
-                        g[0] = fmaf(mr3, fmaf(-alpha, dx, dax), g[0]);
-                        g[1] = fmaf(mr3, fmaf(-alpha, dy, day), g[1]);
-                        g[2] = fmaf(mr3, fmaf(-alpha, dz, daz), g[2]);
+#pragma unroll
+                        for (int k = 0; k < KU; ++k) {
+                            // x_j - x_i and a_j - a_i from both halves
+                            const float dx = (ph.x - xh[k]) + (pl.x - xl[k]);
+                            const float dy = (ph.y - yh[k]) + (pl.y - yl[k]);
+                            const float dz = (ph.z - zh[k]) + (pl.z - zl[k]);
+                            const float dax = (ah.x - axh[k]) + (al.x - axl[k]);
+                            const float day = (ah.y - ayh[k]) + (al.y - ayl[k]);
+                            const float daz = (ah.z - azh[k]) + (al.z - azl[k]);
+                            float r2 = fmaf(dx, dx, eps2);
+                            r2 = fmaf(dy, dy, r2);
+                            r2 = fmaf(dz, dz, r2);
+                            const float ri = rsqrt_approx_g(fmaxf(r2, rcut2));
+                            const float ri2 = ri * ri;
+                            const float mr3 = ph.w * ri * ri2;
+                            const float drda = fmaf(dx, dax, fmaf(dy, day, dz * daz));
+                            const float alpha = 3.f * drda * ri2;
+                            // -m/r^3 (da - alpha dr) with dr = -d, da = -(a_j - a_i)
+                            g[k][0] = fmaf(mr3, fmaf(-alpha, dx, dax), g[k][0]);
+                            g[k][1] = fmaf(mr3, fmaf(-alpha, dy, day), g[k][1]);
+                            g[k][2] = fmaf(mr3, fmaf(-alpha, dz, daz), g[k][2]);
+                        }
                     }
                     since += j1 - j0;
                     if (since >= kFlushG) flush();
@@ -182,22 +204,25 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel(Params p) {
                     const int j0 = min(nt, js * ps), j1 = min(nt, j0 + ps);
                     for (int j = j0; j < j1; ++j) {
                         const float4 q0 = s.sp[j][0], qa = s.sp[j][1], qb = s.sp[j][2];
-                        const float dx = q0.x - xh, dy = q0.y - yh, dz = q0.z - zh;
-                        float r2 = fmaf(dx, dx, eps2);
-                        r2 = fmaf(dy, dy, r2);
-                        r2 = fmaf(dz, dz, r2);
-                        const float ri = rsqrt_approx_g(r2);
-                        const float qdx = fmaf(qa.x, dx, fmaf(qa.w, dy, qb.x * dz));
-                        const float qdy = fmaf(qa.w, dx, fmaf(qa.y, dy, qb.y * dz));
-                        const float qdz = fmaf(qb.x, dx, fmaf(qb.y, dy, qa.z * dz));
-                        const float sq = fmaf(qdx, dx, fmaf(qdy, dy, fmaf(qdz, dz, qb.z)));
-                        const float ri2 = ri * ri, ri3 = ri2 * ri, ri5 = ri3 * ri2;
-                        const float tq = sq * ri5;
-                        const float A = fmaf(tq * ri2, 2.5f, q0.w * ri3);
-                        g[3] = fmaf(A, dx, fmaf(-ri5, qdx, g[3]));
-                        g[4] = fmaf(A, dy, fmaf(-ri5, qdy, g[4]));
-                        g[5] = fmaf(A, dz, fmaf(-ri5, qdz, g[5]));
-                        g[6] = fmaf(-0.5f, tq, fmaf(-q0.w, ri, g[6]));
+#pragma unroll
+                        for (int k = 0; k < KU; ++k) {
+                            const float dx = q0.x - xh[k], dy = q0.y - yh[k], dz = q0.z - zh[k];
+                            float r2 = fmaf(dx, dx, eps2);
+                            r2 = fmaf(dy, dy, r2);
+                            r2 = fmaf(dz, dz, r2);
+                            const float ri = rsqrt_approx_g(r2);
+                            const float qdx = fmaf(qa.x, dx, fmaf(qa.w, dy, qb.x * dz));
+                            const float qdy = fmaf(qa.w, dx, fmaf(qa.y, dy, qb.y * dz));
+                            const float qdz = fmaf(qb.x, dx, fmaf(qb.y, dy, qa.z * dz));
+                            const float sq = fmaf(qdx, dx, fmaf(qdy, dy, fmaf(qdz, dz, qb.z)));
+                            const float ri2 = ri * ri, ri3 = ri2 * ri, ri5 = ri3 * ri2;
+                            const float tq = sq * ri5;
+                            const float A = fmaf(tq * ri2, 2.5f, q0.w * ri3);
+                            g[k][3] = fmaf(A, dx, fmaf(-ri5, qdx, g[k][3]));
+                            g[k][4] = fmaf(A, dy, fmaf(-ri5, qdy, g[k][4]));
+                            g[k][5] = fmaf(A, dz, fmaf(-ri5, qdz, g[k][5]));
+                            g[k][6] = fmaf(-0.5f, tq, fmaf(-q0.w, ri, g[k][6]));
+                        }
                     }
                     since += j1 - j0;
                     if (since >= kFlushG) flush();
@@ -206,21 +231,29 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel(Params p) {
             if (active) flush();
             __syncthreads();
             if (active && js == 0) {
-                double r[7] = {0, 0, 0, 0, 0, 0, 0};
-                for (int q = 0; q < n_js; ++q) {
-                    const int src = q * nip + li;
 #pragma unroll
-                    for (int c = 0; c < 7; ++c) r[c] += (double)s.acc[c][src].x + (double)s.acc[c][src].y;
+                for (int k = 0; k < KU; ++k) {
+                    const int ii = li + k * S;
+                    if (ii >= nip) continue;
+                    const int gi = wd.i_begin + ipass + ii;
+                    double r[7] = {0, 0, 0, 0, 0, 0, 0};
+                    for (int q = 0; q < n_js; ++q) {
+                        const int src = q * S + li;
+#pragma unroll
+                        for (int c = 0; c < 7; ++c) r[c] += (double)s.acc[k][c][src].x + (double)s.acc[k][c][src].y;
+                    }
+                    const Accp a = p.epi_acc64[gi];
+                    const double G = p.G;
+                    p.out_acorr[gi] = Accp{2.0 * r[0], 2.0 * r[1], 2.0 * r[2], 0.0};
+                    p.out_accp[gi] = Accp{a.x + G * r[3], a.y + G * r[4], a.z + G * r[5], G * r[6]};
+                    p.out_nnb[gi] = 0;
                 }
-                const Accp a = p.epi_acc64[gi];
-                const double G = p.G;
-                p.out_acorr[gi] = Accp{2.0 * r[0], 2.0 * r[1], 2.0 * r[2], 0.0};
-                p.out_accp[gi] = Accp{a.x + G * r[3], a.y + G * r[4], a.z + G * r[5], G * r[6]};
-                p.out_nnb[gi] = 0;
             }
         }
     }
 }
+
+constexpr int kKuG = 2;  // i per thread
 
 }  // namespace
 
@@ -230,15 +263,17 @@ cudaError_t launch_gradient(const Params& p, cudaStream_t s, int num_sms) {
     if (e != cudaSuccess || p.n_walk <= 0) return e;
     static int per_sm = 0;
     if (per_sm == 0) {
-        e = cudaFuncSetAttribute(gradient_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemG));
+        e = cudaFuncSetAttribute(gradient_kernel<kKuG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(SmemG<kKuG>));
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gradient_kernel, kThreadsG, sizeof(SmemG));
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gradient_kernel<kKuG>, kThreadsG,
+                                                          sizeof(SmemG<kKuG>));
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
     int grid = num_sms * per_sm;
     if (grid > p.n_walk) grid = p.n_walk;
-    gradient_kernel<<<grid, kThreadsG, sizeof(SmemG), s>>>(p);
+    gradient_kernel<kKuG><<<grid, kThreadsG, sizeof(SmemG<kKuG>), s>>>(p);
     return cudaGetLastError();
 }
 
