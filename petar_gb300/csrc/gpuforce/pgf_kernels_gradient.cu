@@ -12,7 +12,8 @@
 // Design: a persistent CTA-synchronous kernel (one pass is as heavy as a force
 // evaluation, but it runs once per step).  256 threads pop walks from the
 // cost-sorted queue; a pass holds up to 512 i, two per thread, and the
-// threads form floor(256 / ceil(n_i / 2)) j-slices.  Threads stage 128-entry
+// threads form floor(256 / ceil(n_i / 2)) j-slices.  The pair arithmetic is
+// packed FP32x2 over pairs of j.  Threads stage 128-entry
 // EPJ tiles (positions as walk-relative (hi, lo) pairs from the FP32 split
 // arrays, accelerations as (hi, lo) pairs) and 64-entry SPJ tiles in shared
 // memory.  Pair arithmetic is FP32 with both halves, so dr and da are accurate
@@ -40,17 +41,6 @@ __device__ __forceinline__ void two_sum_g(float a, float b, float& s, float& e) 
     e = (a - (s - bb)) + (b - bb);
 }
 
-template <int KU>
-struct SmemG {
-    float4 ph[kTileEPG];  // EPJ: walk-relative position hi, mass
-    float4 pl[kTileEPG];  // EPJ: walk-relative position lo
-    float4 ah[kTileEPG];  // EPJ: acceleration hi
-    float4 al[kTileEPG];  // EPJ: acceleration lo
-    float4 sp[kTileSPG][3];
-    float2 acc[KU][7][kThreadsG];  // flushed partials: acorr x, y, z, SP acc x, y, z, SP pot
-    int w;
-};
-
 __device__ __forceinline__ void flush_into(float2& v, float x) {
     float e;
     two_sum_g(v.x, x, v.x, e);
@@ -58,12 +48,28 @@ __device__ __forceinline__ void flush_into(float2& v, float x) {
 }
 
 // KU i-particles per thread: i = li + k S (k < KU) of a pass of up to
-// 256 KU i, with S = ceil(n_i / KU) threads per j-slice; every j read from
-// shared memory serves KU pairs.
+// 256 KU i, with S = ceil(n_i / KU) threads per j-slice.  Tiles are stored
+// as interleaved pairs of j, so that one FP32x2 instruction evaluates two
+// pairs (the FMA pipe throughput is the same, the issue slots halve).
+// EPJ pair: P = (xh, yh | zh, m | xl, yl | zl, -) and A = (axh, ayh | azh,
+// axl | ayl, azl), each field as (j0, j1).  SPJ pair: (x, y | z, m | -Qxx,
+// -Qyy | -Qzz, -Qxy | -Qxz, -Qyz | -c, -) with c = -tr(q) eps^2, so that
+// the quadrupole terms need no negation.
+constexpr float kDummyPosG = 1e15f;
+
 template <int KU>
-__global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel(Params p) {
+struct SmemGP {
+    float4 P[kTileEPG / 2][4];
+    float4 A[kTileEPG / 2][3];
+    float4 S[kTileSPG / 2][6];
+    float2 acc[KU][7][kThreadsG];
+    int w;
+};
+
+template <int KU>
+__global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    SmemG<KU>& s = *reinterpret_cast<SmemG<KU>*>(smem_raw);
+    SmemGP<KU>& s = *reinterpret_cast<SmemGP<KU>*>(smem_raw);
     const int tid = threadIdx.x;
     const float eps2 = (float)p.eps2;
     const int n_walk = walk_count(p);
@@ -85,52 +91,62 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel(Params p) {
             const int js = tid / S;
             const int li = tid - js * S;
             const bool active = js < n_js;
-            float xh[KU], yh[KU], zh[KU], xl[KU], yl[KU], zl[KU];
-            float axh[KU], ayh[KU], azh[KU], axl[KU], ayl[KU], azl[KU];
+            // (-x_i, -x_i) operands: position and acceleration, hi and lo
+            float2 nxh[KU], nyh[KU], nzh[KU], nxl[KU], nyl[KU], nzl[KU];
+            float2 nah[KU][3], nal[KU][3];
 #pragma unroll
             for (int k = 0; k < KU; ++k) {
-                xh[k] = yh[k] = zh[k] = xl[k] = yl[k] = zl[k] = 0.f;
-                axh[k] = ayh[k] = azh[k] = axl[k] = ayl[k] = azl[k] = 0.f;
+                float v[12] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                 const int ii = li + k * S;
                 if (active && ii < nip) {
                     const int gi = wd.i_begin + ipass + ii;
                     const EpiDev e = p.epi[gi];
-                    const double dx = e.x - wd.cx, dy = e.y - wd.cy, dz = e.z - wd.cz;
-                    xh[k] = (float)dx;
-                    yh[k] = (float)dy;
-                    zh[k] = (float)dz;
-                    xl[k] = (float)(dx - (double)xh[k]);
-                    yl[k] = (float)(dy - (double)yh[k]);
-                    zl[k] = (float)(dz - (double)zh[k]);
+                    const double d[3] = {e.x - wd.cx, e.y - wd.cy, e.z - wd.cz};
                     const Accp a = p.epi_acc64[gi];
-                    axh[k] = (float)a.x;
-                    ayh[k] = (float)a.y;
-                    azh[k] = (float)a.z;
-                    axl[k] = (float)(a.x - (double)axh[k]);
-                    ayl[k] = (float)(a.y - (double)ayh[k]);
-                    azl[k] = (float)(a.z - (double)azh[k]);
+                    const double aa[3] = {a.x, a.y, a.z};
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        v[c] = (float)d[c];
+                        v[3 + c] = (float)(d[c] - (double)v[c]);
+                        v[6 + c] = (float)aa[c];
+                        v[9 + c] = (float)(aa[c] - (double)v[6 + c]);
+                    }
+                }
+                nxh[k] = make_float2(-v[0], -v[0]);
+                nyh[k] = make_float2(-v[1], -v[1]);
+                nzh[k] = make_float2(-v[2], -v[2]);
+                nxl[k] = make_float2(-v[3], -v[3]);
+                nyl[k] = make_float2(-v[4], -v[4]);
+                nzl[k] = make_float2(-v[5], -v[5]);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    nah[k][c] = make_float2(-v[6 + c], -v[6 + c]);
+                    nal[k][c] = make_float2(-v[9 + c], -v[9 + c]);
                 }
             }
 #pragma unroll
             for (int k = 0; k < KU; ++k)
 #pragma unroll
                 for (int q = 0; q < 7; ++q) s.acc[k][q][tid] = make_float2(0.f, 0.f);
-            float g[KU][7];
+            // Pair accumulators: acorr x, y, z, SP acc x, y, z, minus SP pot.
+            float2 g[KU][7];
 #pragma unroll
             for (int k = 0; k < KU; ++k)
 #pragma unroll
-                for (int q = 0; q < 7; ++q) g[k][q] = 0.f;
+                for (int q = 0; q < 7; ++q) g[k][q] = make_float2(0.f, 0.f);
             int since = 0;
             auto flush = [&]() {
 #pragma unroll
                 for (int k = 0; k < KU; ++k)
 #pragma unroll
                     for (int q = 0; q < 7; ++q) {
-                        flush_into(s.acc[k][q][tid], g[k][q]);
-                        g[k][q] = 0.f;
+                        const float x = g[k][q].x + g[k][q].y;
+                        flush_into(s.acc[k][q][tid], q == 6 ? -x : x);
+                        g[k][q] = make_float2(0.f, 0.f);
                     }
                 since = 0;
             };
+            const float2 e2 = make_float2(eps2, eps2);
             // EPJ tiles: the gradient correction of every pair.
             for (int t = 0; t < wd.n_epj; t += kTileEPG) {
                 const int nt = min(kTileEPG, wd.n_epj - t);
@@ -146,85 +162,139 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel(Params p) {
                     two_sum_g(s_, e_ + (r.yl - cly), hy, ly);
                     two_sum_g(r.zh, -chz, s_, e_);
                     two_sum_g(s_, e_ + (r.zl - clz), hz, lz);
-                    s.ph[tid] = make_float4(hx, hy, hz, r.m);
-                    s.pl[tid] = make_float4(lx, ly, lz, 0.f);
-                    s.ah[tid] = make_float4(a.xh, a.yh, a.zh, 0.f);
-                    s.al[tid] = make_float4(a.xl, a.yl, a.zl, 0.f);
+                    float* P = reinterpret_cast<float*>(&s.P[tid >> 1][0]) + (tid & 1);
+                    P[0] = hx;
+                    P[2] = hy;
+                    P[4] = hz;
+                    P[6] = r.m;
+                    P[8] = lx;
+                    P[10] = ly;
+                    P[12] = lz;
+                    P[14] = 0.f;
+                    float* A = reinterpret_cast<float*>(&s.A[tid >> 1][0]) + (tid & 1);
+                    A[0] = a.xh;
+                    A[2] = a.yh;
+                    A[4] = a.zh;
+                    A[6] = a.xl;
+                    A[8] = a.yl;
+                    A[10] = a.zl;
+                } else if (tid == nt && (nt & 1)) {
+                    // massless partner of the last entry
+                    float* P = reinterpret_cast<float*>(&s.P[tid >> 1][0]) + 1;
+                    float* A = reinterpret_cast<float*>(&s.A[tid >> 1][0]) + 1;
+                    for (int u = 0; u < 16; u += 2) P[u] = 0.f;
+                    for (int u = 0; u < 12; u += 2) A[u] = 0.f;
                 }
                 __syncthreads();
                 if (active) {
-                    const int pn = (nt + n_js - 1) / n_js;
-                    const int j0 = min(nt, js * pn), j1 = min(nt, j0 + pn);
+                    const int np = (nt + 1) >> 1;
+                    const int pn = (np + n_js - 1) / n_js;
+                    const int j0 = min(np, js * pn), j1 = min(np, j0 + pn);
                     for (int j = j0; j < j1; ++j) {
-                        const float4 ph = s.ph[j], pl = s.pl[j], ah = s.ah[j], al = s.al[j];
+                        const float4 p0 = s.P[j][0], p1 = s.P[j][1], p2 = s.P[j][2], p3 = s.P[j][3];
+                        const float4 a0 = s.A[j][0], a1 = s.A[j][1], a2 = s.A[j][2];
+                        const float2 Xh = make_float2(p0.x, p0.y), Yh = make_float2(p0.z, p0.w);
+                        const float2 Zh = make_float2(p1.x, p1.y), M = make_float2(p1.z, p1.w);
+                        const float2 Xl = make_float2(p2.x, p2.y), Yl = make_float2(p2.z, p2.w);
+                        const float2 Zl = make_float2(p3.x, p3.y);
+                        const float2 AXh = make_float2(a0.x, a0.y), AYh = make_float2(a0.z, a0.w);
+                        const float2 AZh = make_float2(a1.x, a1.y), AXl = make_float2(a1.z, a1.w);
+                        const float2 AYl = make_float2(a2.x, a2.y), AZl = make_float2(a2.z, a2.w);
 #pragma unroll
                         for (int k = 0; k < KU; ++k) {
                             // x_j - x_i and a_j - a_i from both halves
-                            const float dx = (ph.x - xh[k]) + (pl.x - xl[k]);
-                            const float dy = (ph.y - yh[k]) + (pl.y - yl[k]);
-                            const float dz = (ph.z - zh[k]) + (pl.z - zl[k]);
-                            const float dax = (ah.x - axh[k]) + (al.x - axl[k]);
-                            const float day = (ah.y - ayh[k]) + (al.y - ayl[k]);
-                            const float daz = (ah.z - azh[k]) + (al.z - azl[k]);
-                            float r2 = fmaf(dx, dx, eps2);
-                            r2 = fmaf(dy, dy, r2);
-                            r2 = fmaf(dz, dz, r2);
-                            const float ri = rsqrt_approx_g(fmaxf(r2, rcut2));
-                            const float ri2 = ri * ri;
-                            const float mr3 = ph.w * ri * ri2;
-                            const float drda = fmaf(dx, dax, fmaf(dy, day, dz * daz));
-                            const float alpha = 3.f * drda * ri2;
-                            // -m/r^3 (da - alpha dr) with dr = -d, da = -(a_j - a_i)
-                            g[k][0] = fmaf(mr3, fmaf(-alpha, dx, dax), g[k][0]);
-                            g[k][1] = fmaf(mr3, fmaf(-alpha, dy, day), g[k][1]);
-                            g[k][2] = fmaf(mr3, fmaf(-alpha, dz, daz), g[k][2]);
+                            const float2 dx = __fadd2_rn(__fadd2_rn(Xh, nxh[k]), __fadd2_rn(Xl, nxl[k]));
+                            const float2 dy = __fadd2_rn(__fadd2_rn(Yh, nyh[k]), __fadd2_rn(Yl, nyl[k]));
+                            const float2 dz = __fadd2_rn(__fadd2_rn(Zh, nzh[k]), __fadd2_rn(Zl, nzl[k]));
+                            const float2 dax = __fadd2_rn(__fadd2_rn(AXh, nah[k][0]), __fadd2_rn(AXl, nal[k][0]));
+                            const float2 day = __fadd2_rn(__fadd2_rn(AYh, nah[k][1]), __fadd2_rn(AYl, nal[k][1]));
+                            const float2 daz = __fadd2_rn(__fadd2_rn(AZh, nah[k][2]), __fadd2_rn(AZl, nal[k][2]));
+                            float2 r2 = __ffma2_rn(dx, dx, e2);
+                            r2 = __ffma2_rn(dy, dy, r2);
+                            r2 = __ffma2_rn(dz, dz, r2);
+                            const float2 ri = make_float2(rsqrt_approx_g(fmaxf(r2.x, rcut2)),
+                                                          rsqrt_approx_g(fmaxf(r2.y, rcut2)));
+                            const float2 ri2 = __fmul2_rn(ri, ri);
+                            const float2 mr3 = __fmul2_rn(__fmul2_rn(M, ri), ri2);
+                            const float2 drda = __ffma2_rn(dx, dax, __ffma2_rn(dy, day, __fmul2_rn(dz, daz)));
+                            // -alpha = -3 (dr.da) / r^2
+                            const float2 nal_ = __fmul2_rn(__fmul2_rn(drda, ri2), make_float2(-3.f, -3.f));
+                            g[k][0] = __ffma2_rn(mr3, __ffma2_rn(nal_, dx, dax), g[k][0]);
+                            g[k][1] = __ffma2_rn(mr3, __ffma2_rn(nal_, dy, day), g[k][1]);
+                            g[k][2] = __ffma2_rn(mr3, __ffma2_rn(nal_, dz, daz), g[k][2]);
                         }
                     }
-                    since += j1 - j0;
+                    since += 2 * (j1 - j0);
                     if (since >= kFlushG) flush();
                 }
             }
-            // SPJ tiles: the quadrupole force (traceless Q, c = -tr(q) eps^2).
+            // SPJ tiles: the quadrupole force.
             for (int t = 0; t < wd.n_spj; t += kTileSPG) {
                 const int nt = min(kTileSPG, wd.n_spj - t);
                 __syncthreads();
                 if (tid < nt) {
                     const int id = p.id_spj[wd.spj_begin + t + tid];
                     const SpjF32 r = p.spj32[id];
-                    const float hx = (r.xh - chx) + (r.xl - clx);
-                    const float hy = (r.yh - chy) + (r.yl - cly);
-                    const float hz = (r.zh - chz) + (r.zl - clz);
-                    s.sp[tid][0] = make_float4(hx, hy, hz, r.m);
-                    s.sp[tid][1] = make_float4(r.Q[0], r.Q[1], r.Q[2], r.Q[3]);
-                    s.sp[tid][2] = make_float4(r.Q[4], r.Q[5], -r.tr * eps2, 0.f);
+                    float* f = reinterpret_cast<float*>(&s.S[tid >> 1][0]) + (tid & 1);
+                    f[0] = (r.xh - chx) + (r.xl - clx);
+                    f[2] = (r.yh - chy) + (r.yl - cly);
+                    f[4] = (r.zh - chz) + (r.zl - clz);
+                    f[6] = r.m;
+                    f[8] = -r.Q[0];
+                    f[10] = -r.Q[1];
+                    f[12] = -r.Q[2];
+                    f[14] = -r.Q[3];
+                    f[16] = -r.Q[4];
+                    f[18] = -r.Q[5];
+                    f[20] = r.tr * eps2;
+                    f[22] = 0.f;
+                } else if (tid == nt && (nt & 1)) {
+                    // massless, moment-free partner far away
+                    float* f = reinterpret_cast<float*>(&s.S[tid >> 1][0]) + 1;
+                    f[0] = f[2] = f[4] = kDummyPosG;
+                    for (int u = 6; u < 24; u += 2) f[u] = 0.f;
                 }
                 __syncthreads();
                 if (active) {
-                    const int ps = (nt + n_js - 1) / n_js;
-                    const int j0 = min(nt, js * ps), j1 = min(nt, j0 + ps);
+                    const int np = (nt + 1) >> 1;
+                    const int ps = (np + n_js - 1) / n_js;
+                    const int j0 = min(np, js * ps), j1 = min(np, j0 + ps);
+                    const float2 km25 = make_float2(-2.5f, -2.5f), km05 = make_float2(-0.5f, -0.5f);
                     for (int j = j0; j < j1; ++j) {
-                        const float4 q0 = s.sp[j][0], qa = s.sp[j][1], qb = s.sp[j][2];
+                        const float4 w0 = s.S[j][0], w1 = s.S[j][1], w2 = s.S[j][2];
+                        const float4 w3 = s.S[j][3], w4 = s.S[j][4], w5 = s.S[j][5];
+                        const float2 X = make_float2(w0.x, w0.y), Y = make_float2(w0.z, w0.w);
+                        const float2 Z = make_float2(w1.x, w1.y), M = make_float2(w1.z, w1.w);
+                        const float2 Qxx = make_float2(w2.x, w2.y), Qyy = make_float2(w2.z, w2.w);
+                        const float2 Qzz = make_float2(w3.x, w3.y), Qxy = make_float2(w3.z, w3.w);
+                        const float2 Qxz = make_float2(w4.x, w4.y), Qyz = make_float2(w4.z, w4.w);
+                        const float2 C = make_float2(w5.x, w5.y);
 #pragma unroll
                         for (int k = 0; k < KU; ++k) {
-                            const float dx = q0.x - xh[k], dy = q0.y - yh[k], dz = q0.z - zh[k];
-                            float r2 = fmaf(dx, dx, eps2);
-                            r2 = fmaf(dy, dy, r2);
-                            r2 = fmaf(dz, dz, r2);
-                            const float ri = rsqrt_approx_g(r2);
-                            const float qdx = fmaf(qa.x, dx, fmaf(qa.w, dy, qb.x * dz));
-                            const float qdy = fmaf(qa.w, dx, fmaf(qa.y, dy, qb.y * dz));
-                            const float qdz = fmaf(qb.x, dx, fmaf(qb.y, dy, qa.z * dz));
-                            const float sq = fmaf(qdx, dx, fmaf(qdy, dy, fmaf(qdz, dz, qb.z)));
-                            const float ri2 = ri * ri, ri3 = ri2 * ri, ri5 = ri3 * ri2;
-                            const float tq = sq * ri5;
-                            const float A = fmaf(tq * ri2, 2.5f, q0.w * ri3);
-                            g[k][3] = fmaf(A, dx, fmaf(-ri5, qdx, g[k][3]));
-                            g[k][4] = fmaf(A, dy, fmaf(-ri5, qdy, g[k][4]));
-                            g[k][5] = fmaf(A, dz, fmaf(-ri5, qdz, g[k][5]));
-                            g[k][6] = fmaf(-0.5f, tq, fmaf(-q0.w, ri, g[k][6]));
+                            const float2 dx = __fadd2_rn(X, nxh[k]);
+                            const float2 dy = __fadd2_rn(Y, nyh[k]);
+                            const float2 dz = __fadd2_rn(Z, nzh[k]);
+                            float2 r2 = __ffma2_rn(dx, dx, e2);
+                            r2 = __ffma2_rn(dy, dy, r2);
+                            r2 = __ffma2_rn(dz, dz, r2);
+                            const float2 ri = make_float2(rsqrt_approx_g(r2.x), rsqrt_approx_g(r2.y));
+                            // with -Q and -c: u = d.(-Q).d - c = -(d.Q.d + c), t = u / r^5
+                            const float2 qdx = __ffma2_rn(Qxx, dx, __ffma2_rn(Qxy, dy, __fmul2_rn(Qxz, dz)));
+                            const float2 qdy = __ffma2_rn(Qxy, dx, __ffma2_rn(Qyy, dy, __fmul2_rn(Qyz, dz)));
+                            const float2 qdz = __ffma2_rn(Qxz, dx, __ffma2_rn(Qyz, dy, __fmul2_rn(Qzz, dz)));
+                            const float2 sq = __ffma2_rn(qdx, dx, __ffma2_rn(qdy, dy, __ffma2_rn(qdz, dz, C)));
+                            const float2 ri2 = __fmul2_rn(ri, ri);
+                            const float2 ri3 = __fmul2_rn(ri2, ri);
+                            const float2 ri5 = __fmul2_rn(ri3, ri2);
+                            const float2 tq = __fmul2_rn(sq, ri5);
+                            const float2 A = __ffma2_rn(__fmul2_rn(tq, ri2), km25, __fmul2_rn(M, ri3));
+                            g[k][3] = __ffma2_rn(A, dx, __ffma2_rn(ri5, qdx, g[k][3]));
+                            g[k][4] = __ffma2_rn(A, dy, __ffma2_rn(ri5, qdy, g[k][4]));
+                            g[k][5] = __ffma2_rn(A, dz, __ffma2_rn(ri5, qdz, g[k][5]));
+                            g[k][6] = __ffma2_rn(tq, km05, __ffma2_rn(M, ri, g[k][6]));
                         }
                     }
-                    since += j1 - j0;
+                    since += 2 * (j1 - j0);
                     if (since >= kFlushG) flush();
                 }
             }
@@ -263,17 +333,17 @@ cudaError_t launch_gradient(const Params& p, cudaStream_t s, int num_sms) {
     if (e != cudaSuccess || p.n_walk <= 0) return e;
     static int per_sm = 0;
     if (per_sm == 0) {
-        e = cudaFuncSetAttribute(gradient_kernel<kKuG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sizeof(SmemG<kKuG>));
+        e = cudaFuncSetAttribute(gradient_kernel_pk<kKuG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(SmemGP<kKuG>));
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gradient_kernel<kKuG>, kThreadsG,
-                                                          sizeof(SmemG<kKuG>));
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gradient_kernel_pk<kKuG>, kThreadsG,
+                                                          sizeof(SmemGP<kKuG>));
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
     int grid = num_sms * per_sm;
     if (grid > p.n_walk) grid = p.n_walk;
-    gradient_kernel<kKuG><<<grid, kThreadsG, sizeof(SmemG<kKuG>), s>>>(p);
+    gradient_kernel_pk<kKuG><<<grid, kThreadsG, sizeof(SmemGP<kKuG>), s>>>(p);
     return cudaGetLastError();
 }
 
