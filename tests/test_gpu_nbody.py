@@ -154,3 +154,48 @@ def test_list_overflow_is_reported_and_force_recovers():
     host = walks.build_walks(cl)
     for k in ("epi_index", "epi_disp", "epj_disp", "spj_disp", "id_epj", "id_spj"):
         np.testing.assert_array_equal(getattr(dev, k), getattr(host, k), err_msg=k)
+
+
+def _cluster(pos, theta=0.3, n_leaf=20, n_group=512, r_out=0.01):
+    n = len(pos)
+    rng = np.random.default_rng(n)
+    return ics.Cluster(pos=np.ascontiguousarray(pos, dtype=np.float64), vel=rng.normal(size=(n, 3)) * 0.1,
+                       mass=np.full(n, 1.0 / n), r_out=r_out, r_in=0.1 * r_out, r_search=np.full(n, 1.5 * r_out),
+                       theta=theta, n_leaf_limit=n_leaf, n_group_limit=n_group)
+
+
+def _edge_cases():
+    rng = np.random.default_rng(77)
+    yield "single", _cluster(np.array([[0.1, -0.2, 0.3]]))
+    yield "two_coincident", _cluster(np.array([[0.5, 0.5, 0.5], [0.5, 0.5, 0.5]]))
+    # more coincident particles than a leaf holds: the cells split down to
+    # level 21 and the deepest cell stays a leaf above n_leaf_limit
+    yield "coincident_50_plus_field", _cluster(np.vstack([np.tile([[0.25, 0.25, 0.25]], (50, 1)),
+                                                          rng.normal(size=(500, 3))]))
+    yield "line", _cluster(np.column_stack([np.linspace(-1, 1, 3000), np.zeros(3000), np.zeros(3000)]))
+    yield "leaf1_group1", _cluster(rng.normal(size=(700, 3)), n_leaf=1, n_group=1)
+    yield "leaf8_group16", _cluster(rng.normal(size=(5000, 3)), n_leaf=8, n_group=16, theta=0.5)
+
+
+@pytest.mark.parametrize("name", ["single", "two_coincident", "coincident_50_plus_field", "line", "leaf1_group1",
+                                  "leaf8_group16"])
+def test_device_lists_edge_cases(name):
+    cl = dict(_edge_cases())[name]
+    host = walks.build_walks(cl)
+    with nbody.DeviceNBody(cl) as h:
+        dev = h.lists()
+        st = h.state()
+    for k in ("epi_index", "epi_disp", "epj_disp", "spj_disp", "id_epj", "id_spj", "spj_mass", "spj_pos",
+              "spj_quad"):
+        np.testing.assert_array_equal(getattr(dev, k), getattr(host, k), err_msg=k)
+    o = oracle.force(dev)
+    idx = dev.epi_index
+    np.testing.assert_array_equal(st["n_ngb"][idx], o["nnb"])
+    ea = rel_err_vec(st["acc"][idx], o["acc"])
+    ep = rel_err(st["pot"][idx], o["pot"])
+    # coincident pairs have zero separation: the cutoff makes them finite
+    assert np.isfinite(st["acc"]).all() and np.isfinite(st["pot"]).all()
+    # Degenerate geometries: on the line the net force on most particles is a
+    # near cancellation of its two sides, which multiplies relative errors,
+    # so these cases use a looser bound than the cluster configurations.
+    assert np.median(ea) <= 10 * MIXED_MEDIAN and np.median(ep) <= MIXED_MEDIAN, (np.median(ea), np.median(ep))
