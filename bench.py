@@ -665,24 +665,48 @@ def run_kdk_graph(n: int = 4194304, steps: int = 100, dt: float = 1.0 / 1024) ->
     device time (tree building included)."""
     from petar_gb300 import ics, nbody
     clk = ics.make_king_cluster(7, n, 0.0015, W0=7.0, theta=0.4)
+    rng = np.random.default_rng(11)
+    sample = np.sort(rng.choice(n, 4096, replace=False))
     with nbody.DeviceNBody(clk) as h:
         variant, _ = h.autotune(2)
+        # Accuracy run: every step records a random 4096-particle sample, mixed
+        # precision against an FP64 evaluation over the same lists.
+        h.set_sample(sample, steps + 1)
         h.force()
         st0 = h.stats()
         e0 = sum(h.energy())
-        h.run(steps, dt, graph=True)  # capture, instantiate and run once
-        st1 = h.stats()
+        h.run(steps, dt, graph=True)
         e1 = sum(h.energy())
-        ms = h.run(steps, dt, graph=True)  # replay of the instantiated graph
+        recs = h.samples()
+        # Timed runs without the sample: capture, then the replay is timed.
+        h.set_sample(np.zeros(0, np.int64), 0)
+        h.run(steps, dt, graph=True)
+        st1 = h.stats()
+        ms = h.run(steps, dt, graph=True)
         st2 = h.stats()
     inter = (st2["total_epep"] - st1["total_epep"]) + (st2["total_epsp"] - st1["total_epsp"])
+    per_step = []
+    for r in recs:
+        ea = np.linalg.norm(r["acc"] - r["acc64"], axis=1) / np.linalg.norm(r["acc64"], axis=1)
+        ep = np.abs(r["pot"] - r["pot64"]) / np.abs(r["pot64"])
+        per_step.append((float(np.median(ea)), float(np.quantile(ea, 0.999)), float(np.median(ep)),
+                         float(np.quantile(ep, 0.999)), int((r["n_ngb"] != r["n_ngb64"]).sum())))
+    ps = np.array(per_step)
     return {"config": {"model": "King W0=7", "n": n, "theta": 0.4, "r_out": 0.0015, "dt": dt,
                        "n_leaf_limit": clk.n_leaf_limit, "n_group_limit": clk.n_group_limit},
             "steps_per_graph": steps, "ms_per_step": ms / steps, "value": inter / (ms * 1e-3) / 1e9,
             "unit": "Ginteractions/s over whole steps (tree, lists, force, kicks, drifts)",
             "tree_ms": st0["last_tree_ms"], "force_ms": st0["last_force_ms"],
             "interactions_per_step": inter / steps, "n_groups": st0["n_groups"], "n_cells": st0["n_cells"],
-            "energy_rel_change_first_graph": (e1 - e0) / abs(e0), "kernel_variant": variant,
+            "energy_rel_change": (e1 - e0) / abs(e0), "kernel_variant": variant,
+            "per_step_error_vs_fp64": {
+                "sample": "4096 random particles, every one of the %d force evaluations" % len(per_step),
+                "reference": "FP64 evaluation of the same lists on the device (pinned to the oracle in tests)",
+                "force_rel_err_median_max_over_steps": float(ps[:, 0].max()),
+                "force_rel_err_p999_max_over_steps": float(ps[:, 1].max()),
+                "pot_rel_err_median_max_over_steps": float(ps[:, 2].max()),
+                "pot_rel_err_p999_max_over_steps": float(ps[:, 3].max()),
+                "n_ngb_mismatches_total": int(ps[:, 4].sum())},
             "parity": "tests/test_gpu_nbody.py"}
 
 

@@ -378,6 +378,22 @@ int pgf_nbody_export_lists(pgf_nbody *h, int64_t *order, int64_t *group_begin, i
                            double *cell_pos, double *cell_quad, int32_t *cell_level);
 /* Times every available variant on the resident lists and keeps the fastest. */
 int pgf_nbody_autotune(pgf_nbody *h, int repeats, int *best_variant, double *best_ms);
+/* Per-step sample: after every force evaluation (pgf_nbody_force and each
+ * step of pgf_nbody_run, graphs included) the n_sample given particles get a
+ * record with the mixed-precision result and an FP64 evaluation over the same
+ * lists (the plain FP64 kernel's pair formulas), up to max_records
+ * evaluations.  n_sample = 0 turns it off.  Changing it drops a captured
+ * graph. */
+typedef struct pgf_nbody_sample {
+    double acc[3], pot;        /* mixed precision, as pgf_nbody_get returns them */
+    double acc64[3], pot64;    /* FP64 over the same lists */
+    int32_t n_ngb, n_ngb64;
+    int32_t record, pad;       /* evaluation index since pgf_nbody_set_sample */
+} pgf_nbody_sample;
+int pgf_nbody_set_sample(pgf_nbody *h, int n_sample, const int64_t *particles, int max_records);
+/* *n_records evaluations recorded so far; out (optional) receives them,
+ * record-major: out[r * n_sample + q] (room for max_records * n_sample). */
+int pgf_nbody_get_sample(pgf_nbody *h, int *n_records, pgf_nbody_sample *out);
 int pgf_nbody_destroy(pgf_nbody *h);
 const char *pgf_nbody_last_error(void);
 

@@ -89,6 +89,8 @@ struct TreeHdr {
     unsigned long long total_epep, total_epsp;
     int32_t hist[kBuckets];
     int32_t cursor[kBuckets];
+    int32_t sample_slot;  // next record slot of the per-step sample
+    int32_t pad2;
 };
 
 // Cell fields the walk reads.
@@ -292,9 +294,10 @@ __global__ __launch_bounds__(256) void gather_kernel(const int32_t* __restrict__
                                                      const double* __restrict__ mass, const double* __restrict__ rs,
                                                      int64_t n, EpiDev* __restrict__ epi, EpjMix* __restrict__ epj,
                                                      double* __restrict__ m64, double* __restrict__ rs64,
-                                                     EpjF32* __restrict__ epj32) {
+                                                     EpjF32* __restrict__ epj32, int32_t* __restrict__ inv) {
     for (int64_t s = gtid(); s < n; s += gstride()) {
         const int64_t o = order[s];
+        inv[o] = (int32_t)s;
         const double x = pos[3 * o], y = pos[3 * o + 1], z = pos[3 * o + 2];
         const double m = mass[o], r = rs[o];
         epi[s] = EpiDev{x, y, z, r};
@@ -1016,6 +1019,122 @@ __global__ void energy_final_kernel(const double* __restrict__ part, int nb, dou
     out[1] = ep;
 }
 
+// ---------------------------------------------------------------- per-step sample
+
+// One sampled particle at one step: the mixed-precision result and an FP64
+// evaluation over the same lists (the plain FP64 kernel's pair formulas,
+// summed over the lanes of a warp).
+struct SampleRec {
+    double acc[3], pot;
+    double acc64[3], pot64;
+    int32_t n_ngb, n_ngb64, step, pad;
+};
+static_assert(sizeof(SampleRec) == 80, "SampleRec layout");
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ __launch_bounds__(128) void sample_kernel(const TreeHdr* h, const int64_t* __restrict__ sample,
+                                                     int n_sample, const int32_t* __restrict__ inv,
+                                                     const WalkDesc* __restrict__ walks,
+                                                     const EpiDev* __restrict__ epi, const EpjMix* __restrict__ epj,
+                                                     const double* __restrict__ m64, const double* __restrict__ rs64,
+                                                     const SpjMix* __restrict__ spj, const SpjQ64* __restrict__ spjq,
+                                                     const int32_t* __restrict__ id_epj,
+                                                     const int32_t* __restrict__ id_spj, double eps2, double G,
+                                                     const Accp* __restrict__ accp, const int32_t* __restrict__ nnb,
+                                                     SampleRec* hist, int hist_steps) {
+    if (h->n_walk == 0) return;
+    const int slot = h->sample_slot;
+    if (slot < 0 || slot >= hist_steps) return;
+    const int lane = threadIdx.x & 31;
+    const int ng = h->n_walk;
+    for (int64_t q = gtid() >> 5; q < n_sample; q += gstride() >> 5) {
+        const int s = inv[sample[q]];
+        int lo = 0, hi = ng - 1;  // the group holding sorted row s: last i_begin <= s
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (walks[mid].i_begin <= s) lo = mid;
+            else hi = mid - 1;
+        }
+        const WalkDesc wd = walks[lo];
+        const EpiDev ei = epi[s];
+        double ax = 0, ay = 0, az = 0, pe = 0;
+        int cnt = 0;
+        for (int k = lane; k < wd.n_epj; k += 32) {
+            const int id = id_epj[wd.epj_begin + k];
+            const EpjMix e = epj[id];
+            const double rsj = rs64[id];
+            cnt += exact_neighbour(ei.x, ei.y, ei.z, ei.rs, e.x, e.y, e.z, rsj, eps2);
+            const double dx = ei.x - e.x, dy = ei.y - e.y, dz = ei.z - e.z;
+            const double r2e = dx * dx + dy * dy + dz * dz + eps2;
+            const double r2c = r2e > wd.rcut2 ? r2e : wd.rcut2;
+            const double ri = rsqrt(r2c);
+            const double mr = m64[id] * ri;
+            const double mr3 = mr * ri * ri;
+            ax -= mr3 * dx;
+            ay -= mr3 * dy;
+            az -= mr3 * dz;
+            pe -= mr;
+        }
+        for (int k = lane; k < wd.n_spj; k += 32) {
+            const int id = id_spj[wd.spj_begin + k];
+            const SpjMix j = spj[id];
+            const SpjQ64 qq = spjq[id];
+            const double rx = ei.x - j.x, ry = ei.y - j.y, rz = ei.z - j.z;
+            const double r2 = rx * rx + ry * ry + rz * rz + eps2;
+            const double qxx = qq.q[0], qyy = qq.q[1], qzz = qq.q[2], qxy = qq.q[3], qxz = qq.q[4], qyz = qq.q[5];
+            const double tr = qxx + qyy + qzz;
+            const double qrx = qxx * rx + qxy * ry + qxz * rz;
+            const double qry = qyy * ry + qyz * rz + qxy * rx;
+            const double qrz = qzz * rz + qxz * rx + qyz * ry;
+            const double qrr = qrx * rx + qry * ry + qrz * rz;
+            const double r_inv = rsqrt(r2);
+            const double r2_inv = r_inv * r_inv;
+            const double r3_inv = r2_inv * r_inv;
+            const double r5_inv = r2_inv * r3_inv * 1.5;
+            const double qrr_r5 = r5_inv * qrr;
+            const double qrr_r7 = r2_inv * qrr_r5;
+            const double A = qq.m * r3_inv - tr * r5_inv + 5.0 * qrr_r7;
+            const double B = -2.0 * r5_inv;
+            ax -= A * rx + B * qrx;
+            ay -= A * ry + B * qry;
+            az -= A * rz + B * qrz;
+            pe -= qq.m * r_inv - 0.5 * tr * r3_inv + qrr_r5;
+        }
+        ax = warp_sum(ax);
+        ay = warp_sum(ay);
+        az = warp_sum(az);
+        pe = warp_sum(pe);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        if (lane == 0) {
+            SampleRec r;
+            const Accp a = accp[s];
+            r.acc[0] = a.x;
+            r.acc[1] = a.y;
+            r.acc[2] = a.z;
+            r.pot = a.w;
+            r.acc64[0] = G * ax;
+            r.acc64[1] = G * ay;
+            r.acc64[2] = G * az;
+            r.pot64 = G * pe;
+            r.n_ngb = nnb[s];
+            r.n_ngb64 = cnt;
+            r.step = slot;
+            r.pad = 0;
+            hist[(int64_t)slot * n_sample + q] = r;
+        }
+    }
+}
+
+__global__ void sample_advance_kernel(TreeHdr* h) {
+    if (threadIdx.x == 0) h->sample_slot += 1;
+}
+
 // ---------------------------------------------------------------- host side
 
 thread_local std::string t_error;
@@ -1065,6 +1184,10 @@ struct DArr {
 
 using namespace pgf;
 
+static_assert(sizeof(pgf_nbody_sample) == sizeof(SampleRec), "pgf_nbody_sample layout");
+static_assert(offsetof(pgf_nbody_sample, acc64) == offsetof(SampleRec, acc64), "pgf_nbody_sample layout");
+static_assert(offsetof(pgf_nbody_sample, n_ngb) == offsetof(SampleRec, n_ngb), "pgf_nbody_sample layout");
+
 struct pgf_nbody {
     int device = 0;
     int num_sms = 1;
@@ -1096,6 +1219,10 @@ struct pgf_nbody {
     DArr<SpjQ64> spjq;
     // groups and walks
     DArr<int32_t> group_at, groups, cnt_e, cnt_s, bucket, queue;
+    DArr<int32_t> inv_order;       // particle index -> sorted row
+    DArr<int64_t> sample_idx;      // per-step sample: particles
+    DArr<SampleRec> sample_hist;   // records [max_records][n_sample]
+    int n_sample = 0, sample_records = 0;
     DArr<int32_t> front_at, fronts;  // frontier cells of the task split
     int front_limit = 1;              // frontier: topmost cells with at most this many particles
     int64_t cap_tasks = 0;
@@ -1167,7 +1294,7 @@ cudaError_t enqueue_build(pgf_nbody* h) {
     size_t bytes = h->cub_bytes;
     if ((e = cub_sort(h, h->cub_tmp.d, bytes)) != cudaSuccess) return e;
     gather_kernel<<<gn, 256, 0, s>>>(h->order.d, h->pos.d, h->mass.d, h->rs.d, n, h->epi.d, h->epj.d, h->epj_m64.d,
-                                     h->epj_rs64.d, h->epj32.d);
+                                     h->epj_rs64.d, h->epj32.d, h->inv_order.d);
     const int gc = grid_for(h, h->cap_cells, 256);
     for (int L = 0; L < kLevels; ++L) {
         split_kernel<<<gc, 256, 0, s>>>(hd, h->cells.d, h->nch.d, h->key_out.d, L, h->cfg.n_leaf_limit);
@@ -1212,6 +1339,14 @@ cudaError_t enqueue_force(pgf_nbody* h) {
 }
 
 cudaError_t enqueue_finish(pgf_nbody* h, double dt_kick) {
+    if (h->n_sample > 0) {
+        const int blocks = (int)std::min<int64_t>((h->n_sample + 3) / 4, (int64_t)h->num_sms * 8);
+        sample_kernel<<<blocks, 128, 0, h->stream>>>(
+            h->hdr.d, h->sample_idx.d, h->n_sample, h->inv_order.d, h->walks.d, h->epi.d, h->epj.d, h->epj_m64.d,
+            h->epj_rs64.d, h->spj.d, h->spjq.d, h->id_epj.d, h->id_spj.d, h->cfg.eps2, h->cfg.G, h->out_accp.d,
+            h->out_nnb.d, h->sample_hist.d, h->sample_records);
+        sample_advance_kernel<<<1, 32, 0, h->stream>>>(h->hdr.d);
+    }
     finish_kernel<<<grid_for(h, h->n, 256), 256, 0, h->stream>>>(h->hdr.d, h->order.d, h->out_accp.d, h->out_nnb.d,
                                                                  h->n, h->acc.d, h->pot.d, h->n_ngb.d, h->vel.d,
                                                                  dt_kick);
@@ -1427,7 +1562,8 @@ int pgf_nbody_create(const pgf_nbody_config* cfg, int64_t n, const double* pos, 
     NB_TRY(h->epj_rs64.alloc(n));
     NB_TRY(h->epj32.alloc(n));
     NB_TRY(alloc_cells(h, (int)std::min<int64_t>(4 * (n / (cfg->n_leaf_limit + 1)) + 1024, 1 << 30)));
-    for (auto* a : {&h->group_at, &h->groups, &h->cnt_e, &h->cnt_s, &h->bucket, &h->queue, &h->front_at, &h->fronts})
+    for (auto* a : {&h->group_at, &h->groups, &h->cnt_e, &h->cnt_s, &h->bucket, &h->queue, &h->front_at, &h->fronts,
+                    &h->inv_order})
         NB_TRY(a->alloc(n));
     h->front_limit = (int)std::max<int64_t>(cfg->n_group_limit, n / 1024);
     NB_TRY(alloc_tasks(h, 64 * (n / std::max(1, cfg->n_group_limit / 4) + 1) + 4096));
@@ -1680,6 +1816,39 @@ int pgf_nbody_autotune(pgf_nbody* h, int repeats, int* best_variant, double* bes
     NB_CUDA(enqueue_finish(h, 0.0));
     NB_CUDA(cudaStreamSynchronize(h->stream));
     return check_errors(h);
+}
+
+int pgf_nbody_set_sample(pgf_nbody* h, int n_sample, const int64_t* particles, int max_records) {
+    if (!h) return nb_fail(PGF_ERR_ARG, "NULL handle");
+    if (n_sample < 0 || max_records < 0 || (n_sample > 0 && (!particles || max_records == 0)))
+        return nb_fail(PGF_ERR_ARG, "bad sample arguments");
+    for (int q = 0; q < n_sample; ++q)
+        if (particles[q] < 0 || particles[q] >= h->n) return nb_fail(PGF_ERR_ARG, "sample particle %d out of range", q);
+    NB_CUDA(cudaStreamSynchronize(h->stream));
+    drop_graph(h);  // the captured steps change
+    h->n_sample = 0;
+    h->sample_records = 0;
+    if (n_sample == 0) return PGF_OK;
+    NB_CUDA(h->sample_idx.alloc(n_sample));
+    NB_CUDA(h->sample_hist.alloc((size_t)n_sample * max_records));
+    NB_CUDA(cudaMemcpy(h->sample_idx.d, particles, n_sample * sizeof(int64_t), cudaMemcpyHostToDevice));
+    NB_CUDA(cudaMemset(h->sample_hist.d, 0, (size_t)n_sample * max_records * sizeof(SampleRec)));
+    NB_CUDA(cudaMemset(&h->hdr.d->sample_slot, 0, sizeof(int32_t)));
+    h->n_sample = n_sample;
+    h->sample_records = max_records;
+    return PGF_OK;
+}
+
+int pgf_nbody_get_sample(pgf_nbody* h, int* n_records, pgf_nbody_sample* out) {
+    if (!h || !n_records) return nb_fail(PGF_ERR_ARG, "NULL argument");
+    NB_CUDA(cudaStreamSynchronize(h->stream));
+    TreeHdr t;
+    if (int r = read_hdr(h, &t)) return r;
+    const int n = std::min(t.sample_slot, h->sample_records);
+    *n_records = n;
+    if (out && n > 0 && h->n_sample > 0)
+        NB_CUDA(cudaMemcpy(out, h->sample_hist.d, (size_t)n * h->n_sample * sizeof(SampleRec), cudaMemcpyDeviceToHost));
+    return PGF_OK;
 }
 
 int pgf_nbody_destroy(pgf_nbody* h) {

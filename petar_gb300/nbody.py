@@ -39,6 +39,11 @@ class Stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+# pgf_nbody_sample: one sampled particle at one force evaluation.
+SAMPLE_DTYPE = np.dtype([("acc", "<f8", 3), ("pot", "<f8"), ("acc64", "<f8", 3), ("pot64", "<f8"),
+                         ("n_ngb", "<i4"), ("n_ngb64", "<i4"), ("record", "<i4"), ("pad", "<i4")])
+assert SAMPLE_DTYPE.itemsize == 80
+
 _BOUND = False
 
 
@@ -57,6 +62,8 @@ def _lib() -> ctypes.CDLL:
             "pgf_nbody_get_stats": [vp, vp],
             "pgf_nbody_export_lists": [vp] + [vp] * 10,
             "pgf_nbody_autotune": [vp, ci, vp, vp],
+            "pgf_nbody_set_sample": [vp, ci, vp, ci],
+            "pgf_nbody_get_sample": [vp, vp, vp],
             "pgf_nbody_destroy": [vp],
         }
         for name, args in sig.items():
@@ -150,6 +157,21 @@ class DeviceNBody:
         v, ms = ctypes.c_int(), ctypes.c_double()
         _check(_lib().pgf_nbody_autotune(self._h, repeats, ctypes.byref(v), ctypes.byref(ms)))
         return v.value, ms.value
+
+    def set_sample(self, particles: np.ndarray, max_records: int) -> None:
+        """Record, after every force evaluation, the mixed-precision result of
+        the given particles next to an FP64 evaluation over the same lists."""
+        idx = np.ascontiguousarray(particles, dtype=np.int64)
+        self._sample_n = idx.size
+        self._sample_max = int(max_records)
+        _check(_lib().pgf_nbody_set_sample(self._h, idx.size, _p(idx) if idx.size else None, int(max_records)))
+
+    def samples(self) -> np.ndarray:
+        """Records so far, shaped (evaluations, sampled particles)."""
+        n = ctypes.c_int()
+        out = np.zeros(self._sample_max * self._sample_n, SAMPLE_DTYPE)
+        _check(_lib().pgf_nbody_get_sample(self._h, ctypes.byref(n), _p(out)))
+        return out[:n.value * self._sample_n].reshape(n.value, self._sample_n)
 
     def lists(self) -> WalkBatch:
         """The last build as a WalkBatch over the current positions."""

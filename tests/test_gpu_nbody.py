@@ -98,22 +98,47 @@ def _sample_errors(h, rows_rng, k=4096):
 
 
 def test_king4m_kdk_100_steps_one_graph():
+    """C4 as specified: 100 steps in one graph, the force error of a random
+    4096-particle sample at every step (mixed precision against an FP64
+    evaluation over the same lists, recorded inside the graph), that FP64
+    evaluation pinned to the oracle at the first and the last step, and the
+    energy change over the run."""
     cl = ics.make_king_cluster(7, 4194304, 0.0015, W0=7.0, theta=0.4)
     rng = np.random.default_rng(11)
+    sample = np.sort(rng.choice(cl.n, 4096, replace=False))
     with nbody.DeviceNBody(cl) as h:
-        sa, sp = _sample_errors(h, rng)
-        assert sa["median"] <= MIXED_MEDIAN and sa["p999"] <= MIXED_P999, sa
-        assert sp["median"] <= MIXED_MEDIAN and sp["p999"] <= MIXED_P999, sp
+        h.set_sample(sample, 101)
+        h.force()  # record 0: the initial forces
+
+        def pin_fp64(rec):
+            wb = h.lists()
+            inv = np.empty(cl.n, np.int64)
+            inv[wb.epi_index] = np.arange(cl.n)
+            rows = inv[sample]
+            o = oracle.force(rows_batch(wb, rows))
+            np.testing.assert_array_equal(rec["n_ngb64"], o["nnb"])
+            np.testing.assert_array_equal(rec["n_ngb"], o["nnb"])
+            assert rel_err_vec(rec["acc64"], o["acc"]).max() <= 1e-12
+            assert rel_err(rec["pot64"], o["pot"]).max() <= 1e-12
+
+        pin_fp64(h.samples()[0])
         ek0, ep0 = h.energy()
         h.run(100, 1.0 / 1024, graph=True)
         assert h.stats()["steps"] == 100
-        sa, sp = _sample_errors(h, rng)
-        assert sa["median"] <= MIXED_MEDIAN and sa["p999"] <= MIXED_P999, sa
-        assert sp["median"] <= MIXED_MEDIAN and sp["p999"] <= MIXED_P999, sp
+        recs = h.samples()
+        assert recs.shape == (101, 4096)
+        pin_fp64(recs[100])
+        for k in range(101):
+            r = recs[k]
+            np.testing.assert_array_equal(r["n_ngb"], r["n_ngb64"], err_msg=f"step {k}")
+            sa = stats(rel_err_vec(r["acc"], r["acc64"]))
+            sp = stats(rel_err(r["pot"], r["pot64"]))
+            assert sa["median"] <= MIXED_MEDIAN and sa["p999"] <= MIXED_P999, (k, sa)
+            assert sp["median"] <= MIXED_MEDIAN and sp["p999"] <= MIXED_P999, (k, sp)
         ek1, ep1 = h.energy()
         e0, e1 = ek0 + ep0, ek1 + ep1
-        # Virial-like bound state, and the soft step alone keeps its energy
-        # to a small fraction over 100 steps of 1/1024.
+        # Bound state, and the soft step alone keeps its energy to a small
+        # fraction over 100 steps of 1/1024.
         assert e0 < 0 and abs((e1 - e0) / e0) < 1e-3, (e0, e1)
 
 
