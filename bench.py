@@ -527,14 +527,15 @@ def run_ours(args):
                                    "parity": "tests/test_gpu_parity.py::test_gradient_mode_*"}
 
     # ---- the other named configurations: Plummer 65k and the 64-cluster ensemble ----
+    # (rank 0 only: the other ranks' lines are not printed)
     configs = None
-    if not args.no_configs:
+    if not args.no_configs and rank == 0:
         configs = run_configs(stream, flush)
         gpuforce.set_precision(PGF_PRECISION_MIXED)
 
     # ---- device-resident tree step: King W0=7, 4M, 100 KDK steps in one CUDA graph ----
     kdk = None
-    if not args.no_kdk:
+    if not args.no_kdk and rank == 0:
         kdk = run_kdk_graph()
 
     if rank != 0:
