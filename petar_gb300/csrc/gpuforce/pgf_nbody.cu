@@ -336,11 +336,51 @@ __device__ __forceinline__ void octants(const uint64_t* __restrict__ skey, int b
     }
 }
 
-__global__ __launch_bounds__(256) void split_kernel(TreeHdr* h, TCell* cells, int32_t* nch,
+// The cells of a level are split into kLevelBlocks contiguous chunks, one
+// per CTA, so that the child numbering (children of a level in their parents'
+// order) is a two-level scan: CTA sums here, their scan by one CTA, and the
+// CTA-local scans when the children are written.
+constexpr int kLevelBlocks = 1024;
+
+__device__ __forceinline__ void level_chunk(const TreeHdr* h, int L, int& c0, int& c1) {
+    const int lb = h->level_begin[L], le = h->level_begin[L + 1];
+    const int per = (le - lb + kLevelBlocks - 1) / kLevelBlocks;
+    c0 = min(le, lb + (int)blockIdx.x * per);
+    c1 = min(le, c0 + per);
+}
+
+// Exclusive scan of one value per thread over a 256-thread CTA; *total gets
+// the sum.  Every thread of the CTA must call it.
+__device__ __forceinline__ int cta256_excl_scan(int v, int* total) {
+    __shared__ int ws[8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += u;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    int base = 0, tot = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        base += k < w ? ws[k] : 0;
+        tot += ws[k];
+    }
+    __syncthreads();
+    *total = tot;
+    return base + x - v;
+}
+
+__global__ __launch_bounds__(256) void split_kernel(TreeHdr* h, TCell* cells, int32_t* nch, int32_t* blocksum,
                                                     const uint64_t* __restrict__ skey, int L, int n_leaf) {
     if (h->err) return;
-    const int lb = h->level_begin[L], le = h->level_begin[L + 1];
-    for (int64_t c = lb + gtid(); c < le; c += gstride()) {
+    int c0, c1;
+    level_chunk(h, L, c0, c1);
+    const int lb = h->level_begin[L];
+    int sum = 0;
+    for (int c = c0 + (int)threadIdx.x; c < c1; c += blockDim.x) {
         TCell& cc = cells[c];
         const int cnt = cc.end - cc.begin;
         const bool leaf = cnt <= n_leaf || L >= kMaxLevel;
@@ -353,16 +393,19 @@ __global__ __launch_bounds__(256) void split_kernel(TreeHdr* h, TCell* cells, in
         cc.leaf = leaf;
         cc.n_child = k;
         nch[c - lb] = k;
+        sum += k;
     }
+    int tot;
+    (void)cta256_excl_scan(sum, &tot);
+    if (threadIdx.x == 0) blocksum[blockIdx.x] = tot;
 }
 
-__global__ __launch_bounds__(kScanThreads) void level_scan_kernel(TreeHdr* h, TCell* cells, const int32_t* nch, int L,
-                                                                  int cap) {
+__global__ __launch_bounds__(kScanThreads) void level_scan_kernel(TreeHdr* h, int32_t* blocksum, int L, int cap) {
     if (h->err) return;
-    const int lb = h->level_begin[L], le = h->level_begin[L + 1];
+    const int le = h->level_begin[L + 1];
     const int64_t tot = cta_exclusive_scan(
-        le - lb, [&](int i) { return (int64_t)nch[i]; },
-        [&](int i, int64_t v) { cells[lb + i].first_child = le + (int)min(v, (int64_t)cap); });
+        kLevelBlocks, [&](int i) { return (int64_t)blocksum[i]; },
+        [&](int i, int64_t v) { blocksum[i] = (int32_t)min(v, (int64_t)cap); });
     if (threadIdx.x == 0) {
         if ((int64_t)le + tot > cap) {
             h->err |= kErrCells;
@@ -373,39 +416,58 @@ __global__ __launch_bounds__(kScanThreads) void level_scan_kernel(TreeHdr* h, TC
     }
 }
 
-__global__ __launch_bounds__(256) void fill_kernel(TreeHdr* h, TCell* cells, const uint64_t* __restrict__ skey, int L) {
+__global__ __launch_bounds__(256) void fill_kernel(TreeHdr* h, TCell* cells, const int32_t* __restrict__ nch,
+                                                   const int32_t* __restrict__ blockoff,
+                                                   const uint64_t* __restrict__ skey, int L) {
     if (h->err) return;
+    int c0, c1;
+    level_chunk(h, L, c0, c1);
     const int lb = h->level_begin[L], le = h->level_begin[L + 1];
-    for (int64_t c = lb + gtid(); c < le; c += gstride()) {
-        const TCell cc = cells[c];
-        if (cc.leaf) continue;
-        int b[9];
-        octants(skey, cc.begin, cc.end, L, b);
-        int k = 0;
-        for (int o = 0; o < 8; ++o) {
-            if (b[o + 1] <= b[o]) continue;
-            TCell& ch = cells[cc.first_child + k++];
-            ch.begin = b[o];
-            ch.end = b[o + 1];
-            ch.level = L + 1;
-            ch.parent = (int32_t)c;
-            ch.first_child = 0;
-            ch.n_child = 0;
-            ch.leaf = 0;
+    int run = le + blockoff[blockIdx.x];
+    for (int t0 = c0; t0 < c1; t0 += blockDim.x) {  // uniform trip count over the CTA
+        const int c = t0 + (int)threadIdx.x;
+        const int k_c = c < c1 ? nch[c - lb] : 0;
+        int tot;
+        const int off = cta256_excl_scan(k_c, &tot);
+        if (c < c1 && k_c > 0) {
+            TCell& cc = cells[c];
+            const int first = run + off;
+            cc.first_child = first;
+            int b[9];
+            octants(skey, cc.begin, cc.end, L, b);
+            int k = 0;
+            for (int o = 0; o < 8; ++o) {
+                if (b[o + 1] <= b[o]) continue;
+                TCell& ch = cells[first + k++];
+                ch.begin = b[o];
+                ch.end = b[o + 1];
+                ch.level = L + 1;
+                ch.parent = c;
+                ch.first_child = 0;
+                ch.n_child = 0;
+                ch.leaf = 0;
+            }
+        } else if (c < c1) {
+            cells[c].first_child = run + off;
         }
+        run += tot;
     }
 }
 
-// Moments, boxes and the SPJ records of the cells of level L (children done).
+// Moments, boxes and the SPJ records: LEAVES, every leaf of the tree from
+// its particles; otherwise the inner cells of level L from their children
+// (run deepest level first).
+template <bool LEAVES>
 __global__ __launch_bounds__(256) void moments_kernel(const TreeHdr* h, TCell* cells, TCellW* cw, CMom* mom,
                                                       const EpiDev* __restrict__ epi, const double* __restrict__ m64,
                                                       int L, double inv_theta2, SpjMix* spj, SpjF32* spj32,
                                                       SpjQ64* spjq) {
     if (h->err) return;
-    const int lb = h->level_begin[L], le = h->level_begin[L + 1];
-    const double side = ldexp(h->side0, -L);
+    const int lb = LEAVES ? 0 : h->level_begin[L], le = LEAVES ? h->level_begin[kLevels] : h->level_begin[L + 1];
     for (int64_t c = lb + gtid(); c < le; c += gstride()) {
         TCell& cc = cells[c];
+        if (cc.leaf != (int)LEAVES) continue;
+        const double side = ldexp(h->side0, -cc.level);
         double m = 0, mx[3] = {0, 0, 0}, q[6] = {0, 0, 0, 0, 0, 0};
         double ilo[3], ihi[3], olo[3], ohi[3];
         for (int d = 0; d < 3; ++d) {
@@ -1214,6 +1276,7 @@ struct pgf_nbody {
     DArr<TCellW> cw;
     DArr<CMom> mom;
     DArr<int32_t> nch;
+    DArr<int32_t> blocksum;  // per-CTA child counts of one level, then their offsets
     DArr<SpjMix> spj;
     DArr<SpjF32> spj32;
     DArr<SpjQ64> spjq;
@@ -1297,13 +1360,17 @@ cudaError_t enqueue_build(pgf_nbody* h) {
                                      h->epj_rs64.d, h->epj32.d, h->inv_order.d);
     const int gc = grid_for(h, h->cap_cells, 256);
     for (int L = 0; L < kLevels; ++L) {
-        split_kernel<<<gc, 256, 0, s>>>(hd, h->cells.d, h->nch.d, h->key_out.d, L, h->cfg.n_leaf_limit);
-        level_scan_kernel<<<1, kScanThreads, 0, s>>>(hd, h->cells.d, h->nch.d, L, h->cap_cells);
-        fill_kernel<<<gc, 256, 0, s>>>(hd, h->cells.d, h->key_out.d, L);
+        split_kernel<<<kLevelBlocks, 256, 0, s>>>(hd, h->cells.d, h->nch.d, h->blocksum.d, h->key_out.d, L,
+                                                  h->cfg.n_leaf_limit);
+        level_scan_kernel<<<1, kScanThreads, 0, s>>>(hd, h->blocksum.d, L, h->cap_cells);
+        fill_kernel<<<kLevelBlocks, 256, 0, s>>>(hd, h->cells.d, h->nch.d, h->blocksum.d, h->key_out.d, L);
     }
+    moments_kernel<true><<<gc, 256, 0, s>>>(hd, h->cells.d, h->cw.d, h->mom.d, h->epi.d, h->epj_m64.d, 0,
+                                            h->inv_theta2, h->spj.d, h->spj32.d, h->spjq.d);
+    const int gm = h->num_sms * 2;
     for (int L = kLevels - 1; L >= 0; --L)
-        moments_kernel<<<gc, 256, 0, s>>>(hd, h->cells.d, h->cw.d, h->mom.d, h->epi.d, h->epj_m64.d, L,
-                                          h->inv_theta2, h->spj.d, h->spj32.d, h->spjq.d);
+        moments_kernel<false><<<gm, 256, 0, s>>>(hd, h->cells.d, h->cw.d, h->mom.d, h->epi.d, h->epj_m64.d, L,
+                                                 h->inv_theta2, h->spj.d, h->spj32.d, h->spjq.d);
     if ((e = cudaMemsetAsync(h->group_at.d, 0xff, sizeof(int32_t) * n, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(h->front_at.d, 0xff, sizeof(int32_t) * n, s)) != cudaSuccess) return e;
     group_mark_kernel<<<gc, 256, 0, s>>>(hd, h->cells.d, h->group_at.d, h->cfg.n_group_limit);
@@ -1572,6 +1639,7 @@ int pgf_nbody_create(const pgf_nbody_config* cfg, int64_t n, const double* pos, 
     h->cap_s = 8 * n + 1024;
     NB_TRY(h->id_epj.alloc(h->cap_e));
     NB_TRY(h->id_spj.alloc(h->cap_s));
+    NB_TRY(h->blocksum.alloc(kLevelBlocks));
     NB_TRY(h->out_accp.alloc(n));
     NB_TRY(h->out_nnb.alloc(n));
     NB_TRY(h->flags.alloc(8));
