@@ -48,6 +48,15 @@ public:
         nbody_check(pgf_nbody_get_stats(h_, &s), "pgf_nbody_get_stats");
         return s;
     }
+    // Per-step sample: see pgf_nbody_set_sample / pgf_nbody_get_sample.
+    void set_sample(int n_sample, const int64_t* particles, int max_records) {
+        nbody_check(pgf_nbody_set_sample(h_, n_sample, particles, max_records), "pgf_nbody_set_sample");
+    }
+    int get_sample(pgf_nbody_sample* out) {
+        int n = 0;
+        nbody_check(pgf_nbody_get_sample(h_, &n, out), "pgf_nbody_get_sample");
+        return n;
+    }
     pgf_nbody* handle() { return h_; }
 
 private:

@@ -53,7 +53,20 @@ int main(int argc, char** argv) {
     cfg.kernel_variant = -1;
     cfg.list_capacity_factor = 2.0;
     petar_gpuforce::DeviceTreeStep step(cfg, n, pos.data(), vel.data(), mass.data(), rs.data());
+    const int64_t probe[2] = {0, n - 1};
+    step.set_sample(2, probe, (int)hdr[1] + 1);
     step.run((int)hdr[1], par[0], true);
+    std::vector<pgf_nbody_sample> rec(2 * (hdr[1] + 1));
+    const int n_rec = step.get_sample(rec.data());
+    if (n_rec != (int)hdr[1]) {
+        std::fprintf(stderr, "expected %lld sample records, got %d\n", (long long)hdr[1], n_rec);
+        return 3;
+    }
+    for (int r = 0; r < 2 * n_rec; ++r)
+        if (rec[r].n_ngb != rec[r].n_ngb64) {
+            std::fprintf(stderr, "sample %d: neighbour counts differ\n", r);
+            return 3;
+        }
     std::vector<double> acc(3 * n), pot(n);
     std::vector<int32_t> nnb(n);
     step.get(pos.data(), nullptr, acc.data(), pot.data(), nnb.data());
