@@ -648,20 +648,17 @@ __device__ __forceinline__ bool exact_open(const TCell& gc, const TCell& cc) {
            box_overlap(gc.in_lo, gc.in_hi, cc.out_lo, cc.out_hi);
 }
 
-// a > b on the FP64 values behind the rounded a, b: 1 true, 0 false, 2 unknown
-// (rounding to nearest is monotonic, so only equal rounded values are unsure).
-__device__ __forceinline__ int gt3(float a, float b) { return a > b ? 1 : (a < b ? 0 : 2); }
-
-// box_overlap on rounded boxes: 1 overlap, 0 none, 2 unknown.
+// box_overlap on rounded boxes: 1 overlap, 0 none, 2 unknown.  Rounding to
+// nearest is monotonic, so a strict inequality between rounded values holds
+// for the FP64 values too: one rounded a > b separates the boxes, and strict
+// a < b on every pair proves the overlap; only ties are left to FP64.
 __device__ __forceinline__ int overlap3(const float alo[3], const float ahi[3], const float blo[3], const float bhi[3]) {
-    int r = 1;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const int c1 = gt3(alo[d], bhi[d]), c2 = gt3(blo[d], ahi[d]);
-        if (c1 == 1 || c2 == 1) return 0;
-        if (c1 == 2 || c2 == 2) r = 2;
-    }
-    return r;
+    const bool sep = (alo[0] > bhi[0]) | (blo[0] > ahi[0]) | (alo[1] > bhi[1]) | (blo[1] > ahi[1]) |
+                     (alo[2] > bhi[2]) | (blo[2] > ahi[2]);
+    if (sep) return 0;
+    const bool ovl = (alo[0] < bhi[0]) & (blo[0] < ahi[0]) & (alo[1] < bhi[1]) & (blo[1] < ahi[1]) &
+                     (alo[2] < bhi[2]) & (blo[2] < ahi[2]);
+    return ovl ? 1 : 2;
 }
 
 // r2 <= crit of the FP64 test from rounded data: 1 open, 0 not, 2 unknown.
