@@ -161,3 +161,15 @@ def test_gradient_correction_matches_reference():
     np.testing.assert_array_equal(o["acorr"], d["ref__acorr"])
     np.testing.assert_array_equal(o["acc"], d["ref__acc"])
     np.testing.assert_array_equal(o["pot"], d["ref__pot"])
+
+
+def test_rows_batch_equals_full_walks():
+    """The single-row walks of tests.helpers.rows_batch (used to check a
+    particle sample against the oracle) give bit-identical oracle results."""
+    from helpers import rows_batch
+    wb, _ = load_golden("plummer2048_walks")
+    rows = np.array([0, 5, 100, 777, wb.epi_rs.size - 1])
+    full = oracle.force(wb)
+    part = oracle.force(rows_batch(wb, rows))
+    for k in ("acc", "pot", "nnb"):
+        np.testing.assert_array_equal(part[k], full[k][rows], err_msg=k)
