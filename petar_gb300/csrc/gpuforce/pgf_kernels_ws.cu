@@ -118,12 +118,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int32_
     if (done) return true;
     const unsigned long long t0 = globaltimer();
     for (;;) {
+        // Suspend (up to the hint, 100 us) until the phase completes, so
+        // that waiting warps leave the issue slots to the warps that work.
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}"
             : "=r"(done)
-            : "r"(a), "r"(parity)
+            : "r"(a), "r"(parity), "r"(100000u)
             : "memory");
         if (done) return true;
         if (globaltimer() - t0 > kWaitLimitNs) {
