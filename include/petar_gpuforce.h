@@ -190,6 +190,14 @@ int pgf_get_kernel_variant(int *variant);
  * stage use one).  Results do not depend on the stage count. */
 int pgf_set_dispatch_stages(int stages);
 
+/* Walk splitting in single-launch dispatches (1, the default, or 0 = off).
+ * When a dispatch has few walks for the GPU's CTAs, each walk costing more
+ * than twice an even share runs as up to 16 parts over slices of its EPJ and
+ * SPJ lists, and the parts are added in a fixed order; results then differ
+ * from an unsplit launch by FP32 summation order only (counts are exact).
+ * Force and neighbour-search modes; no counterpart in the reference. */
+int pgf_set_walk_split(int enable);
+
 /* Autotuner: times every kernel variant `repeats` times on the data of the
  * tag's last index dispatch (already on the device), keeps the fastest for
  * later dispatches and reports it and its mean main-kernel time.  The results

@@ -139,6 +139,10 @@ struct TagState {
     std::vector<int64_t> stage_i;  // and in EPI rows
     bool times_pending = false;  // kernel events recorded, not yet added to the profile
     Params params{};
+    // Walks split over several CTAs (single-launch dispatches only).
+    int n_split = 0;
+    DevBuf<SplitRec> splits;
+    HostBuf<SplitRec> h_splits;
 };
 
 struct State {
@@ -155,6 +159,7 @@ struct State {
     int precision = PGF_PRECISION_MIXED;
     int variant = 0;  // mixed-precision kernel variant (pgf_set_kernel_variant)
     int stages = 0;   // dispatch pipeline stages (pgf_set_dispatch_stages); 0 = by size
+    bool walk_split = true;  // split the largest walks of small dispatches (pgf_set_walk_split)
     int mode = PGF_MODE_FORCE;
     // shared j data
     DevBuf<EpjMix> epj;
@@ -510,6 +515,10 @@ int launch_kernels(const TagState& t, const Params& p, cudaStream_t s, cudaEvent
 int launch_tag(TagState& t) {
     bind_scratch(t.params);
     if (int r = launch_kernels(t, t.params, g.stream, t.ev[1], t.ev[2])) return r;
+    if (t.n_split > 0) {
+        const cudaError_t e = launch_combine_parts(t.splits.d, t.n_split, t.params.out_accp, t.params.out_nnb, g.stream);
+        if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "combine kernel failed: %s", cudaGetErrorString(e));
+    }
     PGF_CUDA(cudaEventRecord(t.ev[3], g.stream));
     t.n_chunks = 0;
     t.dispatched = true;
@@ -689,24 +698,62 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
         PGF_CUDA(t.epi_co.ensure(ni));
         PGF_CUDA(t.pot_soft.ensure(ni));
     }
-    PGF_CUDA(t.h_epi.ensure(ni));
-    PGF_CUDA(t.h_id_epj.ensure(ne));
-    PGF_CUDA(t.h_id_spj.ensure(ns));
-    PGF_CUDA(t.h_walks.ensure(n_walk));
-    PGF_CUDA(t.h_order.ensure(n_walk));
-    PGF_CUDA(t.epi.ensure(ni));
-    PGF_CUDA(t.id_epj.ensure(ne));
-    PGF_CUDA(t.id_spj.ensure(ns));
-    PGF_CUDA(t.walks.ensure(n_walk));
-    PGF_CUDA(t.order.ensure(n_walk));
-    PGF_CUDA(t.accp.ensure(ni));
-    PGF_CUDA(t.nnb.ensure(ni));
-
     // Stages: contiguous ranges of the sorted layout.  The first has half the
     // list entries of the others, so the GPU starts sooner; the rest share
     // the remainder equally.
     int n_chunks = g.stages > 0 ? g.stages : (int)std::min<int64_t>(kMaxChunks, (ne + ns) / kChunkIdEntries + 1);
     if (n_walk < 8 * n_chunks) n_chunks = 1;
+
+    // Split plan.  In a single launch the most expensive walks bound the
+    // launch time when there are few walks per CTA; each walk that costs
+    // more than twice an even share of the GPU's CTAs runs as up to 16 parts,
+    // each with a slice of its EPJ and SPJ lists and its own copy of the
+    // walk's EPI rows, and a combine kernel adds the parts up.  Force and
+    // neighbour-search modes only: the other modes add per-i terms once.
+    struct SplitPlan {
+        int k, parts;
+        int64_t rows1;  // first EPI row of part 1
+        int desc1;      // layout position of part 1's descriptor
+    };
+    std::vector<SplitPlan> plan;
+    int64_t ni_all = ni;
+    int n_desc = n_walk;
+    if (n_chunks == 1 && g.walk_split && n_walk > 0 &&
+        (g.mode == PGF_MODE_FORCE || g.mode == PGF_MODE_NEIGHBOR_SEARCH)) {
+        double total = 0.0;
+        for (int k = 0; k < n_walk; ++k) total += cost(ord[k]);
+        const double target = total / (4.0 * (double)g.num_sms);
+        for (int k = 0; k < n_walk; ++k) {
+            const int w = ord[k];
+            const double c = cost(w);
+            if (!(c > 2.0 * target)) break;  // the layout is sorted by cost
+            const int64_t entries = (int64_t)n_epj[w] + n_spj[w];
+            const int parts = (int)std::min<double>({16.0, std::ceil(c / target), (double)(entries / 256)});
+            if (parts < 2) continue;
+            plan.push_back(SplitPlan{k, parts, ni_all, n_desc});
+            ni_all += (int64_t)(parts - 1) * n_epi[w];
+            n_desc += parts - 1;
+        }
+        if (ni_all > kMaxRows) {
+            plan.clear();
+            ni_all = ni;
+            n_desc = n_walk;
+        }
+    }
+    t.n_split = 0;
+
+    PGF_CUDA(t.h_epi.ensure(ni_all));
+    PGF_CUDA(t.h_id_epj.ensure(ne));
+    PGF_CUDA(t.h_id_spj.ensure(ns));
+    PGF_CUDA(t.h_walks.ensure(n_desc));
+    PGF_CUDA(t.h_order.ensure(n_desc));
+    PGF_CUDA(t.epi.ensure(ni_all));
+    PGF_CUDA(t.id_epj.ensure(ne));
+    PGF_CUDA(t.id_spj.ensure(ns));
+    PGF_CUDA(t.walks.ensure(n_desc));
+    PGF_CUDA(t.order.ensure(n_desc));
+    PGF_CUDA(t.accp.ensure(ni_all));
+    PGF_CUDA(t.nnb.ensure(ni_all));
     std::vector<int> cb(n_chunks + 1, n_walk);
     cb[0] = 0;
     for (int c = 1, k = 0; c < n_chunks; ++c) {
@@ -744,7 +791,7 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     p.id_spj = t.id_spj.d;
     p.walks = t.walks.d;
     p.order = t.order.d;
-    p.n_walk = n_walk;
+    p.n_walk = n_desc;
     // The neighbour search tests r^2 < max(rs_i, rs_j)^2 without softening
     // (src/soft_force.hpp:11-34); the force kernels include eps^2.
     p.eps2 = t.mode == PGF_MODE_NEIGHBOR_SEARCH ? 0.0 : g.eps2;
@@ -795,10 +842,61 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
 
     if (n_chunks == 1) {
         const int bad_walk = pack_range(0, n_walk);
+        if (bad_walk >= 0) {
+            g.prof.copy += now_s() - t0;
+            return fail(PGF_ERR_ARG, "walk %d has an EPJ/SPJ id outside the sent arrays", bad_walk);
+        }
+        if (!plan.empty()) {
+            PGF_CUDA(t.h_splits.ensure(plan.size()));
+            PGF_CUDA(t.splits.ensure(plan.size()));
+            for (size_t q = 0; q < plan.size(); ++q) {
+                const SplitPlan& sp = plan[q];
+                const WalkDesc d0 = t.h_walks.h[sp.k];
+                for (int j = 0; j < sp.parts; ++j) {
+                    WalkDesc d = d0;
+                    const int e0 = (int)((int64_t)d0.n_epj * j / sp.parts);
+                    const int e1 = (int)((int64_t)d0.n_epj * (j + 1) / sp.parts);
+                    const int s0 = (int)((int64_t)d0.n_spj * j / sp.parts);
+                    const int s1 = (int)((int64_t)d0.n_spj * (j + 1) / sp.parts);
+                    d.epj_begin = d0.epj_begin + e0;
+                    d.n_epj = e1 - e0;
+                    d.spj_begin = d0.spj_begin + s0;
+                    d.n_spj = s1 - s0;
+                    if (j == 0) {
+                        t.h_walks.h[sp.k] = d;
+                        continue;
+                    }
+                    d.i_begin = (int32_t)(sp.rows1 + (int64_t)(j - 1) * d0.n_i);
+                    t.h_walks.h[sp.desc1 + j - 1] = d;
+                    std::memcpy(t.h_epi.h + d.i_begin, t.h_epi.h + d0.i_begin, (size_t)d0.n_i * sizeof(EpiDev));
+                }
+                t.h_splits.h[q] = SplitRec{d0.i_begin, (int32_t)sp.rows1, d0.n_i, sp.parts};
+            }
+            // Work queue over walks and parts, by descending cost.
+            std::vector<std::pair<double, int>> cq(n_desc);
+            for (int k = 0; k < n_desc; ++k) {
+                const WalkDesc& d = t.h_walks.h[k];
+                cq[k] = {(double)d.n_i * ((double)d.n_epj + 2.0 * (double)d.n_spj), k};
+            }
+            std::stable_sort(cq.begin(), cq.end(), [](const std::pair<double, int>& a, const std::pair<double, int>& b) {
+                return a.first > b.first;
+            });
+            for (int k = 0; k < n_desc; ++k) t.h_order.h[k] = cq[k].second;
+        }
         g.prof.copy += now_s() - t0;
-        if (bad_walk >= 0) return fail(PGF_ERR_ARG, "walk %d has an EPJ/SPJ id outside the sent arrays", bad_walk);
         PGF_CUDA(cudaEventRecord(t.ev[0], g.stream));
         if (int r = copy_range(0, n_walk, g.stream)) return r;
+        if (!plan.empty()) {
+            PGF_CUDA(cudaMemcpyAsync(t.epi.d + ni, t.h_epi.h + ni, (ni_all - ni) * sizeof(EpiDev),
+                                     cudaMemcpyHostToDevice, g.stream));
+            PGF_CUDA(cudaMemcpyAsync(t.walks.d, t.h_walks.h, n_desc * sizeof(WalkDesc), cudaMemcpyHostToDevice,
+                                     g.stream));
+            PGF_CUDA(cudaMemcpyAsync(t.order.d, t.h_order.h, n_desc * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                     g.stream));
+            PGF_CUDA(cudaMemcpyAsync(t.splits.d, t.h_splits.h, plan.size() * sizeof(SplitRec),
+                                     cudaMemcpyHostToDevice, g.stream));
+            t.n_split = (int)plan.size();
+        }
         return launch_tag(t);
     }
 
@@ -1015,6 +1113,11 @@ int pgf_set_changeover_layout(const pgf_changeover_layout* layout) {
     }
     g.co = *layout;
     g.co_set = true;
+    return PGF_OK;
+}
+
+int pgf_set_walk_split(int enable) {
+    g.walk_split = enable != 0;
     return PGF_OK;
 }
 

@@ -216,10 +216,20 @@ __device__ __forceinline__ void co_pair_diff(const EpiDev& ei, const CoRec& ci, 
     out[4] = -meff * (1.0 - wpot) * ri + (double)mj * rimax;
 }
 
+// A walk whose list was split into n_parts parts (small dispatches, to spread
+// the largest walks over several CTAs): part 0 writes the walk's own EPI rows
+// from row0, part k >= 1 a copy of them from rows1 + (k - 1) n_i.
+struct SplitRec {
+    int32_t row0, rows1, n_i, n_parts;
+};
+
 // Launchers (stream-ordered, asynchronous).
 cudaError_t launch_fp64(const Params& p, cudaStream_t s, int num_sms);
 cudaError_t launch_mixed(const Params& p, cudaStream_t s, int num_sms);
 cudaError_t launch_retest(const Params& p, cudaStream_t s, int num_sms);
+// Adds the results of every split walk's parts into its own rows, parts in
+// order (deterministic).
+cudaError_t launch_combine_parts(const SplitRec* recs, int n_recs, Accp* accp, int32_t* nnb, cudaStream_t s);
 // Builds the (hi, lo) FP32 copies of the EPJ / SPJ arrays.
 cudaError_t launch_split_j(const EpjMix* epj, int64_t n_epj, EpjF32* epj32, const SpjMix* spj, int64_t n_spj,
                            SpjF32* spj32, cudaStream_t s);

@@ -577,6 +577,32 @@ cudaError_t launch_mixed(const Params& p, cudaStream_t s, int num_sms) {
     return cudaGetLastError();
 }
 
+__global__ __launch_bounds__(256) void combine_parts_kernel(const SplitRec* __restrict__ recs, Accp* accp,
+                                                            int32_t* nnb) {
+    const SplitRec r = recs[blockIdx.x];
+    for (int i = threadIdx.x; i < r.n_i; i += blockDim.x) {
+        Accp a = accp[r.row0 + i];
+        int c = nnb[r.row0 + i];
+        for (int k = 1; k < r.n_parts; ++k) {
+            const int64_t row = (int64_t)r.rows1 + (int64_t)(k - 1) * r.n_i + i;
+            const Accp b = accp[row];
+            a.x += b.x;
+            a.y += b.y;
+            a.z += b.z;
+            a.w += b.w;
+            c += nnb[row];
+        }
+        accp[r.row0 + i] = a;
+        nnb[r.row0 + i] = c;
+    }
+}
+
+cudaError_t launch_combine_parts(const SplitRec* recs, int n_recs, Accp* accp, int32_t* nnb, cudaStream_t s) {
+    if (n_recs <= 0) return cudaSuccess;
+    combine_parts_kernel<<<n_recs, 256, 0, s>>>(recs, accp, nnb);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_retest(const Params& p, cudaStream_t s, int num_sms) {
     retest_kernel<<<num_sms * 2, 256, 0, s>>>(p);
     return cudaGetLastError();

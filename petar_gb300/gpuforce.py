@@ -155,6 +155,7 @@ def load(build: bool = True) -> ctypes.CDLL:
         "pgf_recompute": [ci],
         "pgf_set_kernel_variant": [ci],
         "pgf_set_dispatch_stages": [ci],
+        "pgf_set_walk_split": [ci],
         "pgf_set_mode": [ci],
         "pgf_set_changeover_layout": [vp],
         "pgf_set_gradient_layout": [vp],
@@ -228,6 +229,12 @@ def set_mode(mode: int) -> None:
 def set_dispatch_stages(stages: int) -> None:
     """Pipeline stages of index dispatches (0: by size, 1: none, 2..8: forced)."""
     _check(load().pgf_set_dispatch_stages(stages))
+
+
+def set_walk_split(enable: bool) -> None:
+    """Split the most expensive walks of small single-launch dispatches over
+    several CTAs (default on)."""
+    _check(load().pgf_set_walk_split(1 if enable else 0))
 
 
 def get_kernel_variant() -> int:

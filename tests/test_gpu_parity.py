@@ -262,6 +262,7 @@ def test_pipelined_dispatch_matches_single_launch(variant):
     rec = gpuforce.Records(wb)
     gpuforce.set_precision(PGF_PRECISION_MIXED)
     gpuforce.set_kernel_variant(variant)
+    gpuforce.set_walk_split(False)  # single launches would split walks; stages do not
     out = {}
     try:
         for stages in (1, 2, 3, 8):
@@ -278,6 +279,7 @@ def test_pipelined_dispatch_matches_single_launch(variant):
     finally:
         gpuforce.set_dispatch_stages(0)
         gpuforce.set_kernel_variant(0)
+        gpuforce.set_walk_split(True)
     f1, r1 = out[1]
     for key in (2, 3, 8, "recompute"):
         f, r = out[key]
@@ -458,3 +460,33 @@ def test_gradient_mode_binaries_with_true_accelerations():
     acc = oracle.force(wb)["acc"]
     res = gpuforce.compute_gradient(wb, acc, acc)
     _gradient_check(res, oracle.gradient(wb, acc, acc), "binaries")
+
+
+@pytest.mark.parametrize("precision", [PGF_PRECISION_MIXED, PGF_PRECISION_FP64])
+def test_walk_split_matches_unsplit_and_oracle(precision):
+    """A small dispatch (Plummer 65,536: 556 walks for about 600 CTAs) runs
+    its most expensive walks as several parts; the result agrees with the
+    unsplit launch up to summation order, counts exactly, and with the
+    oracle; recompute reproduces it bit for bit."""
+    cl = ics.make_plummer_cluster(2, 65536, 0.008)
+    wb = walks.build_walks(cl)
+    rec = gpuforce.Records(wb)
+    try:
+        gpuforce.set_walk_split(False)
+        plain = gpuforce.compute(wb, precision, rec=rec)
+        gpuforce.set_walk_split(True)
+        split = gpuforce.compute(wb, precision, rec=rec)
+        gpuforce.recompute(0)
+        again = gpuforce.retrieve(rec, tag=0)
+    finally:
+        gpuforce.set_walk_split(True)
+    np.testing.assert_array_equal(split["nnb"], plain["nnb"])
+    np.testing.assert_array_equal(again["acc"], split["acc"])
+    np.testing.assert_array_equal(again["n_ngb"], split["nnb"])
+    for e in (rel_err_vec(split["acc"], plain["acc"]), rel_err(split["pot"], plain["pot"])):
+        if precision == PGF_PRECISION_MIXED:
+            st = stats(e)
+            assert st["median"] <= MIXED_MEDIAN and st["p999"] <= MIXED_P999, st
+        else:
+            assert e.max() <= 1e-13
+    check(wb, split, precision, label="split")
