@@ -24,7 +24,8 @@ Reported (one JSON line from rank 0):
   sample of the walks, with every host thread;
 * modes: neighbour search, fused changeover and KDKDK_4TH gradient passes on
   the same lists;
-* configs: Plummer N = 65,536 (mixed against the plain FP64 kernel) and the
+* configs: the bench workload through the functors in PeTar's unchanged
+  batches of 200 walks per call; Plummer N = 65,536 (mixed against the plain FP64 kernel) and the
   64-cluster ensemble in one launch (against 64 sequential plain FP64
   launches), each timed on its own resident lists;
 * kdk_graph: the King W0 = 7, N = 4,194,304 configuration (theta 0.4,
@@ -530,7 +531,8 @@ def run_ours(args):
     # (rank 0 only: the other ranks' lines are not printed)
     configs = None
     if not args.no_configs and rank == 0:
-        configs = run_configs(stream, flush)
+        configs = {"fdps_batches_200": run_fdps_batches(wb, rec, n_int)}
+        configs.update(run_configs(stream, flush))
         gpuforce.set_precision(PGF_PRECISION_MIXED)
 
     # ---- device-resident tree step: King W0=7, 4M, 100 KDK steps in one CUDA graph ----
@@ -582,6 +584,43 @@ def run_ours(args):
     print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.barrier()
+
+
+def run_fdps_batches(wb, rec, n_int: int, batch: int = 200, reps: int = 3) -> dict:
+    """The bench workload through the functors as PeTar calls them unchanged:
+    FDPS hands over n_walk_limit = 200 walks per call (src/petar.hpp:888)
+    with one tag, so each batch is dispatched and retrieved before the next
+    (send once, then 55 dispatch/retrieve pairs), with and without walk
+    splitting.  Host records, copies and unpacking included."""
+    from petar_gb300 import gpuforce
+    gpuforce.set_precision(gpuforce.PGF_PRECISION_MIXED)
+    f = gpuforce.CalcForceWithLinearCutoffCUDAMultiWalk(0, rec.eps2, rec.rcut2, rec.G)
+    nw = rec.n_walk
+
+    def one_eval():
+        f(0, 0, None, None, None, None, None, None, rec.epj, rec.epj.size, rec.spj, rec.spj.size, True)
+        for w0 in range(0, nw, batch):
+            w1 = min(nw, w0 + batch)
+            f(0, w1 - w0, rec.p_epi[w0:w1], rec.n_epi[w0:w1], rec.p_id_epj[w0:w1], rec.n_epj[w0:w1],
+              rec.p_id_spj[w0:w1], rec.n_spj[w0:w1], None, 0, None, 0, False, epi_dtype=rec.epi.dtype)
+            gpuforce.RetrieveForceCUDA(0, w1 - w0, rec.n_epi[w0:w1], rec.p_force[w0:w1],
+                                       force_dtype=rec.force.dtype)
+
+    out = {"walks_per_call": batch, "calls_per_evaluation": (nw + batch - 1) // batch, "unit": "Ginteractions/s"}
+    try:
+        for split in (True, False):
+            gpuforce.set_walk_split(split)
+            one_eval()
+            ts = []
+            for _ in range(reps):
+                t = time.time()
+                one_eval()
+                ts.append(time.time() - t)
+            key = "split" if split else "no_split"
+            out[key] = {"ms_per_evaluation": 1e3 * min(ts), "value": n_int / min(ts) / 1e9}
+    finally:
+        gpuforce.set_walk_split(True)
+    return out
 
 
 def _time_tag(tag: int, stream, flush, reps: int = 3) -> float:
