@@ -195,7 +195,7 @@ int pgf_set_dispatch_stages(int stages);
  * than twice an even share runs as up to 16 parts over slices of its EPJ and
  * SPJ lists, and the parts are added in a fixed order; results then differ
  * from an unsplit launch by FP32 summation order only (counts are exact).
- * Force and neighbour-search modes; no counterpart in the reference. */
+ * All modes; no counterpart in the reference. */
 int pgf_set_walk_split(int enable);
 
 /* Autotuner: times every kernel variant `repeats` times on the data of the

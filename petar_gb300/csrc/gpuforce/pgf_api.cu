@@ -516,7 +516,8 @@ int launch_tag(TagState& t) {
     bind_scratch(t.params);
     if (int r = launch_kernels(t, t.params, g.stream, t.ev[1], t.ev[2])) return r;
     if (t.n_split > 0) {
-        const cudaError_t e = launch_combine_parts(t.splits.d, t.n_split, t.params.out_accp, t.params.out_nnb, g.stream);
+        const cudaError_t e = launch_combine_parts(t.splits.d, t.n_split, t.params.out_accp, t.params.out_nnb,
+                                                   t.params.out_pot_soft, t.params.out_acorr, g.stream);
         if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "combine kernel failed: %s", cudaGetErrorString(e));
     }
     PGF_CUDA(cudaEventRecord(t.ev[3], g.stream));
@@ -631,7 +632,8 @@ bool pack_walk(TagState& t, int k, int w, const Slot3& o, const void* const* epi
         d.cx = d.cy = d.cz = 0.0;
         d.hx = d.hy = d.hz = d.rs_max = 0.f;
     }
-    d.pad[0] = d.pad[1] = d.pad[2] = d.pad[3] = 0.f;
+    d.part = 0;
+        d.pad[0] = d.pad[1] = d.pad[2] = 0.f;
     d.rcut2 = g.walk_rcut2.empty() ? g.rcut2 : g.walk_rcut2[w];
     t.h_walks.h[k] = d;
     t.h_order.h[k] = k;
@@ -688,16 +690,6 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     if (gr_mode && ne > 0 && !g.j_gr_sent)
         return fail(PGF_ERR_STATE, "gradient mode: the EPJ array was sent before the gradient layout was set");
     t.mode = g.mode;
-    if (gr_mode) {
-        PGF_CUDA(t.h_epi_acc.ensure(ni));
-        PGF_CUDA(t.epi_acc.ensure(ni));
-        PGF_CUDA(t.acorr.ensure(ni));
-    }
-    if (co_mode) {
-        PGF_CUDA(t.h_epi_co.ensure(ni));
-        PGF_CUDA(t.epi_co.ensure(ni));
-        PGF_CUDA(t.pot_soft.ensure(ni));
-    }
     // Stages: contiguous ranges of the sorted layout.  The first has half the
     // list entries of the others, so the GPU starts sooner; the rest share
     // the remainder equally.
@@ -708,8 +700,9 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     // launch time when there are few walks per CTA; each walk that costs
     // more than twice an even share of the GPU's CTAs runs as up to 16 parts,
     // each with a slice of its EPJ and SPJ lists and its own copy of the
-    // walk's EPI rows, and a combine kernel adds the parts up.  Force and
-    // neighbour-search modes only: the other modes add per-i terms once.
+    // walk's EPI rows, and a combine kernel adds the parts up.  The kernels
+    // add per-i terms (changeover self-potential, the gradient pass's a_i)
+    // in part 0 only.
     struct SplitPlan {
         int k, parts;
         int64_t rows1;  // first EPI row of part 1
@@ -718,8 +711,7 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     std::vector<SplitPlan> plan;
     int64_t ni_all = ni;
     int n_desc = n_walk;
-    if (n_chunks == 1 && g.walk_split && n_walk > 0 &&
-        (g.mode == PGF_MODE_FORCE || g.mode == PGF_MODE_NEIGHBOR_SEARCH)) {
+    if (n_chunks == 1 && g.walk_split && n_walk > 0) {
         double total = 0.0;
         for (int k = 0; k < n_walk; ++k) total += cost(ord[k]);
         const double target = total / (4.0 * (double)g.num_sms);
@@ -741,6 +733,16 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
         }
     }
     t.n_split = 0;
+    if (gr_mode) {
+        PGF_CUDA(t.h_epi_acc.ensure(ni_all));
+        PGF_CUDA(t.epi_acc.ensure(ni_all));
+        PGF_CUDA(t.acorr.ensure(ni_all));
+    }
+    if (co_mode) {
+        PGF_CUDA(t.h_epi_co.ensure(ni_all));
+        PGF_CUDA(t.epi_co.ensure(ni_all));
+        PGF_CUDA(t.pot_soft.ensure(ni_all));
+    }
 
     PGF_CUDA(t.h_epi.ensure(ni_all));
     PGF_CUDA(t.h_id_epj.ensure(ne));
@@ -867,8 +869,13 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
                         continue;
                     }
                     d.i_begin = (int32_t)(sp.rows1 + (int64_t)(j - 1) * d0.n_i);
+                    d.part = j;
                     t.h_walks.h[sp.desc1 + j - 1] = d;
                     std::memcpy(t.h_epi.h + d.i_begin, t.h_epi.h + d0.i_begin, (size_t)d0.n_i * sizeof(EpiDev));
+                    if (co_mode)
+                        std::memcpy(t.h_epi_co.h + d.i_begin, t.h_epi_co.h + d0.i_begin, (size_t)d0.n_i * sizeof(CoRec));
+                    if (gr_mode)
+                        std::memcpy(t.h_epi_acc.h + d.i_begin, t.h_epi_acc.h + d0.i_begin, (size_t)d0.n_i * sizeof(Accp));
                 }
                 t.h_splits.h[q] = SplitRec{d0.i_begin, (int32_t)sp.rows1, d0.n_i, sp.parts};
             }
@@ -889,6 +896,12 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
         if (!plan.empty()) {
             PGF_CUDA(cudaMemcpyAsync(t.epi.d + ni, t.h_epi.h + ni, (ni_all - ni) * sizeof(EpiDev),
                                      cudaMemcpyHostToDevice, g.stream));
+            if (co_mode)
+                PGF_CUDA(cudaMemcpyAsync(t.epi_co.d + ni, t.h_epi_co.h + ni, (ni_all - ni) * sizeof(CoRec),
+                                         cudaMemcpyHostToDevice, g.stream));
+            if (gr_mode)
+                PGF_CUDA(cudaMemcpyAsync(t.epi_acc.d + ni, t.h_epi_acc.h + ni, (ni_all - ni) * sizeof(Accp),
+                                         cudaMemcpyHostToDevice, g.stream));
             PGF_CUDA(cudaMemcpyAsync(t.walks.d, t.h_walks.h, n_desc * sizeof(WalkDesc), cudaMemcpyHostToDevice,
                                      g.stream));
             PGF_CUDA(cudaMemcpyAsync(t.order.d, t.h_order.h, n_desc * sizeof(int32_t), cudaMemcpyHostToDevice,

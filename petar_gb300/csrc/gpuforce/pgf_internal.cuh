@@ -108,7 +108,8 @@ struct __align__(32) WalkDesc {
     double rcut2;       // r_out^2 of the walk
     float hx, hy, hz;   // EPI box half-extents, rounded up
     float rs_max;       // largest r_search of the walk's EPI, rounded up
-    float pad[4];
+    int32_t part;       // 0, or k >= 1 for part k of a split walk (adds no per-i terms)
+    float pad[3];
 };
 static_assert(sizeof(WalkDesc) == 96, "WalkDesc layout");
 
@@ -229,7 +230,9 @@ cudaError_t launch_mixed(const Params& p, cudaStream_t s, int num_sms);
 cudaError_t launch_retest(const Params& p, cudaStream_t s, int num_sms);
 // Adds the results of every split walk's parts into its own rows, parts in
 // order (deterministic).
-cudaError_t launch_combine_parts(const SplitRec* recs, int n_recs, Accp* accp, int32_t* nnb, cudaStream_t s);
+// pot_soft and acorr (optional) are the changeover and gradient modes' outputs.
+cudaError_t launch_combine_parts(const SplitRec* recs, int n_recs, Accp* accp, int32_t* nnb, double* pot_soft,
+                                 Accp* acorr, cudaStream_t s);
 // Builds the (hi, lo) FP32 copies of the EPJ / SPJ arrays.
 cudaError_t launch_split_j(const EpjMix* epj, int64_t n_epj, EpjF32* epj32, const SpjMix* spj, int64_t n_spj,
                            SpjF32* spj32, cudaStream_t s);

@@ -312,7 +312,8 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
 #pragma unroll
                         for (int c = 0; c < 7; ++c) r[c] += (double)s.acc[k][c][src].x + (double)s.acc[k][c][src].y;
                     }
-                    const Accp a = p.epi_acc64[gi];
+                    // a_i once: parts of a split walk add their pairs only
+                    const Accp a = wd.part == 0 ? p.epi_acc64[gi] : Accp{0.0, 0.0, 0.0, 0.0};
                     const double G = p.G;
                     p.out_acorr[gi] = Accp{2.0 * r[0], 2.0 * r[1], 2.0 * r[2], 0.0};
                     p.out_accp[gi] = Accp{a.x + G * r[3], a.y + G * r[4], a.z + G * r[5], G * r[6]};

@@ -578,11 +578,14 @@ cudaError_t launch_mixed(const Params& p, cudaStream_t s, int num_sms) {
 }
 
 __global__ __launch_bounds__(256) void combine_parts_kernel(const SplitRec* __restrict__ recs, Accp* accp,
-                                                            int32_t* nnb) {
+                                                            int32_t* nnb, double* pot_soft, Accp* acorr) {
     const SplitRec r = recs[blockIdx.x];
     for (int i = threadIdx.x; i < r.n_i; i += blockDim.x) {
-        Accp a = accp[r.row0 + i];
-        int c = nnb[r.row0 + i];
+        const int64_t r0 = (int64_t)r.row0 + i;
+        Accp a = accp[r0];
+        int c = nnb[r0];
+        double ps = pot_soft ? pot_soft[r0] : 0.0;
+        Accp g = acorr ? acorr[r0] : Accp{0.0, 0.0, 0.0, 0.0};
         for (int k = 1; k < r.n_parts; ++k) {
             const int64_t row = (int64_t)r.rows1 + (int64_t)(k - 1) * r.n_i + i;
             const Accp b = accp[row];
@@ -591,15 +594,25 @@ __global__ __launch_bounds__(256) void combine_parts_kernel(const SplitRec* __re
             a.z += b.z;
             a.w += b.w;
             c += nnb[row];
+            if (pot_soft) ps += pot_soft[row];
+            if (acorr) {
+                const Accp h = acorr[row];
+                g.x += h.x;
+                g.y += h.y;
+                g.z += h.z;
+            }
         }
-        accp[r.row0 + i] = a;
-        nnb[r.row0 + i] = c;
+        accp[r0] = a;
+        nnb[r0] = c;
+        if (pot_soft) pot_soft[r0] = ps;
+        if (acorr) acorr[r0] = g;
     }
 }
 
-cudaError_t launch_combine_parts(const SplitRec* recs, int n_recs, Accp* accp, int32_t* nnb, cudaStream_t s) {
+cudaError_t launch_combine_parts(const SplitRec* recs, int n_recs, Accp* accp, int32_t* nnb, double* pot_soft,
+                                 Accp* acorr, cudaStream_t s) {
     if (n_recs <= 0) return cudaSuccess;
-    combine_parts_kernel<<<n_recs, 256, 0, s>>>(recs, accp, nnb);
+    combine_parts_kernel<<<n_recs, 256, 0, s>>>(recs, accp, nnb, pot_soft, acorr);
     return cudaGetLastError();
 }
 

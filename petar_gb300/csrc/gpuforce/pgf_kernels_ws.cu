@@ -671,7 +671,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
     // Changeover: pot_tot and pot_soft partials of neighbour pairs (all other
     // pairs add the same term to both, in a[k][3]).
     float dt[CO ? KI : 1], ds[CO ? KI : 1];
-    double r_out_walk = 0.0, rcut2d = 0.0;
+    double r_out_walk = 0.0, rcut2d = 0.0, self_scale = 1.0;
     int walk_cur = 0;
     int since = 0;
 #pragma unroll
@@ -1041,6 +1041,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
                 r_out_walk = sqrt(wd.rcut2);
                 rcut2d = wd.rcut2;
                 walk_cur = h.walk;
+                self_scale = wd.part == 0 ? 1.0 : 0.0;  // parts of a split walk add it once
             }
 #pragma unroll
             for (int k = 0; k < KI; ++k) {
@@ -1126,7 +1127,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
                     const int gi = gbase + k * S;
                     if constexpr (CO) {
                         // self-potential G m / r_out removed (src/hard.hpp:1663-1674)
-                        const double self = (double)s.co.coi[k][slot].mass / r_out_walk;
+                        const double self = self_scale * (double)s.co.coi[k][slot].mass / r_out_walk;
                         p.out_accp[gi] = Accp{G * r[0], G * r[1], G * r[2], G * ((r[3] + rt) + self)};
                         p.out_pot_soft[gi] = G * ((r[3] + rs) + self);
                     } else if constexpr (!SR) {

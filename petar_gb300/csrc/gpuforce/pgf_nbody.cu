@@ -914,7 +914,8 @@ __global__ __launch_bounds__(128) void group_reduce_kernel(TreeHdr* h, const TCe
         d.hz = __double2float_ru(dmax(gc.in_hi[2] - d.cz, d.cz - gc.in_lo[2]));
         d.rs_max = gc.rs_max;
         d.rcut2 = rcut2;
-        d.pad[0] = d.pad[1] = d.pad[2] = d.pad[3] = 0.f;
+        d.part = 0;
+        d.pad[0] = d.pad[1] = d.pad[2] = 0.f;
         walks[g] = d;
         cnt_e[g] = ne;
         cnt_s[g] = ns;

@@ -134,7 +134,8 @@ __global__ __launch_bounds__(128) void walk_prep_kernel(int n_walk, const int64_
             d.cx = d.cy = d.cz = 0.0;
             d.hx = d.hy = d.hz = d.rs_max = 0.f;
         }
-        d.pad[0] = d.pad[1] = d.pad[2] = d.pad[3] = 0.f;
+        d.part = 0;
+        d.pad[0] = d.pad[1] = d.pad[2] = 0.f;
         d.rcut2 = rcut2;
         desc[w] = d;
         order[w] = w;

@@ -413,12 +413,14 @@ def test_changeover_mode_pipelined_and_without_layout():
     cl = ics.make_plummer_cluster(33, 20000, 0.004, binary_fraction=0.5)
     wb, co = walks.make_changeover(walks.build_walks(cl), cl.r_in, cl.r_out, seed=4)
     out = {}
+    gpuforce.set_walk_split(False)  # single launches would split walks; stages do not
     try:
         for stages in (1, 4):
             gpuforce.set_dispatch_stages(stages)
             out[stages] = gpuforce.compute_changeover(wb, co)
     finally:
         gpuforce.set_dispatch_stages(0)
+        gpuforce.set_walk_split(True)
     for k in ("acc", "pot", "pot_soft", "nnb"):
         np.testing.assert_array_equal(out[1][k], out[4][k])
     rec = gpuforce.Records(wb, co)
@@ -490,3 +492,44 @@ def test_walk_split_matches_unsplit_and_oracle(precision):
         else:
             assert e.max() <= 1e-13
     check(wb, split, precision, label="split")
+
+
+def test_walk_split_changeover_and_gradient_modes():
+    """Split walks in the modes with per-i terms: the changeover
+    self-potential and the gradient pass's a_i are added once; results agree
+    with the unsplit launch up to summation order and with the oracle."""
+    cl = ics.make_plummer_cluster(33, 20000, 0.004, binary_fraction=0.5)
+    wb, co = walks.make_changeover(walks.build_walks(cl), cl.r_in, cl.r_out, seed=4)
+    out = {}
+    try:
+        for split in (False, True):
+            gpuforce.set_walk_split(split)
+            out[split] = gpuforce.compute_changeover(wb, co)
+    finally:
+        gpuforce.set_walk_split(True)
+    np.testing.assert_array_equal(out[True]["nnb"], out[False]["nnb"])
+    for k in ("pot", "pot_soft"):
+        st = stats(rel_err(out[True][k], out[False][k]))
+        assert st["median"] <= MIXED_MEDIAN and st["p999"] <= MIXED_P999, (k, st)
+    check_changeover(wb, co, out[True], label="split")
+    acc = oracle.force(wb)["acc"]
+    gr = {}
+    try:
+        for split in (False, True):
+            gpuforce.set_walk_split(split)
+            gr[split] = gpuforce.compute_gradient(wb, acc, acc)
+    finally:
+        gpuforce.set_walk_split(True)
+    for k in ("acorr", "acc"):
+        st = stats(rel_err_vec(gr[True][k], gr[False][k]))
+        assert st["median"] <= MIXED_MEDIAN and st["p999"] <= MIXED_P999, (k, st)
+    # Against the oracle the split pass is as accurate as the unsplit one.
+    # (On this binary-rich workload acorr reaches p99.9 1.1e-5 either way:
+    # the sum over j cancels strongly for members of close binaries.)
+    o = oracle.gradient(wb, acc, acc)
+    for k in ("acorr", "acc"):
+        e1 = stats(rel_err_vec(gr[True][k], o[k]))
+        e0 = stats(rel_err_vec(gr[False][k], o[k]))
+        for q in ("median", "p999"):
+            assert e1[q] <= max(1.05 * e0[q], MIXED_MEDIAN if q == "median" else MIXED_P999), (k, q, e1, e0)
+    assert (gr[True]["nnb"] == 0).all()
