@@ -690,9 +690,9 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     if (gr_mode && ne > 0 && !g.j_gr_sent)
         return fail(PGF_ERR_STATE, "gradient mode: the EPJ array was sent before the gradient layout was set");
     t.mode = g.mode;
-    // Stages: contiguous ranges of the sorted layout.  The first has half the
-    // list entries of the others, so the GPU starts sooner; the rest share
-    // the remainder equally.
+    // Stages: contiguous ranges of the sorted layout.  The first has a quarter
+    // of the list entries of the others, so the GPU starts sooner; the rest
+    // share the remainder equally.
     int n_chunks = g.stages > 0 ? g.stages : (int)std::min<int64_t>(kMaxChunks, (ne + ns) / kChunkIdEntries + 1);
     if (n_walk < 8 * n_chunks) n_chunks = 1;
 
@@ -759,7 +759,7 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     std::vector<int> cb(n_chunks + 1, n_walk);
     cb[0] = 0;
     for (int c = 1, k = 0; c < n_chunks; ++c) {
-        const int64_t target = (ne + ns) * (2 * c - 1) / (2 * n_chunks - 1);
+        const int64_t target = (ne + ns) * (4 * c - 3) / (4 * n_chunks - 3);
         while (k < n_walk && off[k].e + off[k].s < target) ++k;
         cb[c] = k;
     }
