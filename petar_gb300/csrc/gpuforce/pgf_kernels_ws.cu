@@ -321,6 +321,8 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
     constexpr int kMaxPass = CW * 32 * KI;
     constexpr int kTileEP = TE, kTileSP = TE / 2, kSlots = NS;
     constexpr int QE = TE / 32, QS = TE / 64;  // EPJ and SPJ entries per lane and tile
+    constexpr int QB = QE < 4 ? QE : 4, QSB = QS < 2 ? QS : 2;  // ... converted at a time
+    static_assert(QE % QB == 0 && QS % QSB == 0, "tiles of whole sub-batches");
     static_assert(QS >= 1 && TE % 64 == 0, "EP tiles of a multiple of 64 entries");
     const float eps2 = (float)p.eps2;
     const uint64_t stream_pol = l2_evict_first_policy();
@@ -425,58 +427,64 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
             if constexpr (TM) {
                 if (n_tiles > 0) tm_issue(0);
             }
-            // EPJ tiles: ids and records for 4 entries per lane.
+            // EPJ tiles: ids and records, converted QB entries per lane at a
+            // time (the producer's registers stay those of a 128-entry tile).
             for (int t = 0; t < n_ept; ++t) {
                 const int64_t base = wd.epj_begin + (int64_t)t * kTileEP;
                 const int nt = min(kTileEP, wd.n_epj - t * kTileEP);
-                int id[QE];
-                float4 r0[QE], r1[QE];
                 if constexpr (TM) {
                     if (t + 1 < n_tiles) tm_issue(t + 1);
                     if (!tm_wait(t)) return bail();
+                }
+                int nn = 0, nf = 0;
+#pragma unroll
+                for (int qb = 0; qb < QE; qb += QB) {
+                int id[QB];
+                float4 r0[QB], r1[QB];
+                if constexpr (TM) {
                     const float4* st = reinterpret_cast<const float4*>(s.tm.stage[t & 1]);
 #pragma unroll
-                    for (int q = 0; q < QE; ++q) {
-                        const int e = q * 32 + lane;
-                        id[q] = e < nt ? 0 : -1;
-                        r0[q] = st[2 * e];
-                        r1[q] = st[2 * e + 1];
+                    for (int qq = 0; qq < QB; ++qq) {
+                        const int e = (qb + qq) * 32 + lane;
+                        id[qq] = e < nt ? 0 : -1;
+                        r0[qq] = st[2 * e];
+                        r1[qq] = st[2 * e + 1];
                     }
                 } else {
 #pragma unroll
-                    for (int q = 0; q < QE; ++q) {
-                        const int e = q * 32 + lane;
-                        id[q] = e < nt ? ld_streamed(p.id_epj + base + e, stream_pol) : -1;
+                    for (int qq = 0; qq < QB; ++qq) {
+                        const int e = (qb + qq) * 32 + lane;
+                        id[qq] = e < nt ? ld_streamed(p.id_epj + base + e, stream_pol) : -1;
                     }
 #pragma unroll
-                    for (int q = 0; q < QE; ++q) {
-                        if (id[q] >= 0) {
-                            const float4* src = reinterpret_cast<const float4*>(p.epj32 + id[q]);
-                            r0[q] = __ldg(src);
-                            r1[q] = __ldg(src + 1);
+                    for (int qq = 0; qq < QB; ++qq) {
+                        if (id[qq] >= 0) {
+                            const float4* src = reinterpret_cast<const float4*>(p.epj32 + id[qq]);
+                            r0[qq] = __ldg(src);
+                            r1[qq] = __ldg(src + 1);
                         } else {
-                            r0[q] = r1[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+                            r0[qq] = r1[qq] = make_float4(0.f, 0.f, 0.f, 0.f);
                         }
                     }
                 }
-                if (!acquire(sl)) return bail();
+                if (qb == 0 && !acquire(sl)) return bail();
                 auto& S = s.slot[sl].ep;
-                int nn = 0, nf = 0;
 #pragma unroll
-                for (int q = 0; q < QE; ++q) {
+                for (int qq = 0; qq < QB; ++qq) {
+                    const int q = qb + qq;
                     const int e = q * 32 + lane;
                     const bool valid = e < nt;
                     bool near = false;
                     float hx = 0.f, hy = 0.f, hz = 0.f, m = 0.f, rs2 = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
                     if (valid) {
                         // x - c to within about 1 ulp; exact (hi, lo) below for near entries
-                        const float sx = r0[q].x - chx, sy = r0[q].y - chy, sz = r0[q].z - chz;
-                        const float tx = r1[q].x - clx, ty = r1[q].y - cly, tz = r1[q].z - clz;
+                        const float sx = r0[qq].x - chx, sy = r0[qq].y - chy, sz = r0[qq].z - chz;
+                        const float tx = r1[qq].x - clx, ty = r1[qq].y - cly, tz = r1[qq].z - clz;
                         hx = sx + tx;
                         hy = sy + ty;
                         hz = sz + tz;
-                        m = r0[q].w;
-                        rs2 = r1[q].w;
+                        m = r0[qq].w;
+                        rs2 = r1[qq].w;
                         const float ex = fmaxf(fabsf(hx) - wd.hx, 0.f);
                         const float ey = fmaxf(fabsf(hy) - wd.hy, 0.f);
                         const float ez = fmaxf(fabsf(hz) - wd.hz, 0.f);
@@ -489,11 +497,11 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
                             // (x_hi - c_hi) exactly as s + e, then (s, e + x_lo - c_lo)
                             // renormalised: hi + lo = x - c to about 2^-48 |x|.
                             float s_, e_;
-                            two_sum(r0[q].x, -chx, s_, e_);
+                            two_sum(r0[qq].x, -chx, s_, e_);
                             two_sum(s_, e_ + tx, hx, lx);
-                            two_sum(r0[q].y, -chy, s_, e_);
+                            two_sum(r0[qq].y, -chy, s_, e_);
                             two_sum(s_, e_ + ty, hy, ly);
-                            two_sum(r0[q].z, -chz, s_, e_);
+                            two_sum(r0[qq].z, -chz, s_, e_);
                             two_sum(s_, e_ + tz, hz, lz);
                         }
                     }
@@ -505,7 +513,7 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
                         S.nh[pos] = make_float4(hx, hy, hz, m);
                         S.nl[pos] = make_float4(lx, ly, lz, rs2);
                         S.nidx[pos] = e;
-                        if constexpr (CO) S.nco[pos] = p.epj_co[id[q]];
+                        if constexpr (CO) S.nco[pos] = p.epj_co[id[qq]];
                     } else if (valid && !SR) {
                         const int pos = nf + __popc(bf & lt);
                         if constexpr (PK) {
@@ -521,6 +529,8 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
                     nn += __popc(bn);
                     nf += __popc(bf);
                 }
+                }  // sub-batches
+                auto& S = s.slot[sl].ep;
                 if constexpr (PK && !SR) {
                     if ((nf & 1) && lane == 0) {
                         float* f = reinterpret_cast<float*>(&S.fp[nf >> 1][0]) + 1;
@@ -536,70 +546,77 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
                 }
                 publish(sl);
             }
-            // SPJ tiles: 2 entries per lane, 64-byte records.
+            // SPJ tiles: 64-byte records, QSB entries per lane at a time.
             for (int t = 0; t < n_spt; ++t) {
                 const int64_t base = wd.spj_begin + (int64_t)t * kTileSP;
                 const int nt = min(kTileSP, wd.n_spj - t * kTileSP);
-                int id[QS];
-                float4 r[QS][4];
                 if constexpr (TM) {
                     const int u = n_ept + t;
                     if (u + 1 < n_tiles) tm_issue(u + 1);
                     if (!tm_wait(u)) return bail();
-                    const float4* st = reinterpret_cast<const float4*>(s.tm.stage[u & 1]);
+                }
 #pragma unroll
-                    for (int q = 0; q < QS; ++q) {
-                        const int e = q * 32 + lane;
+                for (int qb = 0; qb < QS; qb += QSB) {
+                int id[QSB];
+                float4 r[QSB][4];
+                if constexpr (TM) {
+                    const float4* st = reinterpret_cast<const float4*>(s.tm.stage[(n_ept + t) & 1]);
 #pragma unroll
-                        for (int v = 0; v < 4; ++v) r[q][v] = st[4 * e + v];
+                    for (int qq = 0; qq < QSB; ++qq) {
+                        const int e = (qb + qq) * 32 + lane;
+#pragma unroll
+                        for (int v = 0; v < 4; ++v) r[qq][v] = st[4 * e + v];
                     }
                 } else {
 #pragma unroll
-                    for (int q = 0; q < QS; ++q) {
-                        const int e = q * 32 + lane;
-                        id[q] = e < nt ? ld_streamed(p.id_spj + base + e, stream_pol) : -1;
+                    for (int qq = 0; qq < QSB; ++qq) {
+                        const int e = (qb + qq) * 32 + lane;
+                        id[qq] = e < nt ? ld_streamed(p.id_spj + base + e, stream_pol) : -1;
                     }
 #pragma unroll
-                    for (int q = 0; q < QS; ++q) {
-                        if (id[q] >= 0) {
-                            const float4* src = reinterpret_cast<const float4*>(p.spj32 + id[q]);
+                    for (int qq = 0; qq < QSB; ++qq) {
+                        if (id[qq] >= 0) {
+                            const float4* src = reinterpret_cast<const float4*>(p.spj32 + id[qq]);
 #pragma unroll
-                            for (int u = 0; u < 4; ++u) r[q][u] = __ldg(src + u);
+                            for (int u = 0; u < 4; ++u) r[qq][u] = __ldg(src + u);
                         }
                     }
                 }
-                if (!acquire(sl)) return bail();
+                if (qb == 0 && !acquire(sl)) return bail();
                 auto& S = s.slot[sl].sp;
 #pragma unroll
-                for (int q = 0; q < QS; ++q) {
+                for (int qq = 0; qq < QSB; ++qq) {
+                    const int q = qb + qq;
                     const int e = q * 32 + lane;
                     if (e < nt) {
                         // SpjF32: (xh yh zh m) (xl yl zl tr) (Qxx Qyy Qzz Qxy) (Qxz Qyz pad pad)
-                        const float hx = (r[q][0].x - chx) + (r[q][1].x - clx);
-                        const float hy = (r[q][0].y - chy) + (r[q][1].y - cly);
-                        const float hz = (r[q][0].z - chz) + (r[q][1].z - clz);
-                        const float m = r[q][0].w;
-                        const float c = -r[q][1].w * eps2;
+                        const float hx = (r[qq][0].x - chx) + (r[qq][1].x - clx);
+                        const float hy = (r[qq][0].y - chy) + (r[qq][1].y - cly);
+                        const float hz = (r[qq][0].z - chz) + (r[qq][1].z - clz);
+                        const float m = r[qq][0].w;
+                        const float c = -r[qq][1].w * eps2;
                         if constexpr (PK) {
                             float* f = reinterpret_cast<float*>(&S.sp[e >> 1][0]) + (e & 1);
                             f[0] = hx;
                             f[2] = hy;
                             f[4] = hz;
                             f[6] = m;
-                            f[8] = -r[q][2].x;
-                            f[10] = -r[q][2].y;
-                            f[12] = -r[q][2].z;
-                            f[14] = -r[q][2].w;
-                            f[16] = -r[q][3].x;
-                            f[18] = -r[q][3].y;
+                            f[8] = -r[qq][2].x;
+                            f[10] = -r[qq][2].y;
+                            f[12] = -r[qq][2].z;
+                            f[14] = -r[qq][2].w;
+                            f[16] = -r[qq][3].x;
+                            f[18] = -r[qq][3].y;
                             f[20] = -c;
                         } else {
                             S.sp[e][0] = make_float4(hx, hy, hz, m);
-                            S.sp[e][1] = r[q][2];
-                            S.sp[e][2] = make_float4(r[q][3].x, r[q][3].y, c, 0.f);
+                            S.sp[e][1] = r[qq][2];
+                            S.sp[e][2] = make_float4(r[qq][3].x, r[qq][3].y, c, 0.f);
                         }
                     }
                 }
+                }  // sub-batches
+                auto& S = s.slot[sl].sp;
                 if constexpr (PK) {
                     if ((nt & 1) && lane == 0) {
                         float* f = reinterpret_cast<float*>(&S.sp[nt >> 1][0]) + 1;
@@ -1247,17 +1264,17 @@ cudaError_t launch_ws(const Params& p, cudaStream_t s, int num_sms, int variant,
     switch (variant) {
         case 0: return launch_ws_t<4, 3, 4, false>(p, s, num_sms);
         case 1: return launch_ws_t<4, 3, 4, true, kModeForce, 128, 3, true>(p, s, num_sms, tm);
-        case 2: return launch_ws_t<4, 3, 4, true, kModeForce, 64, 8>(p, s, num_sms);
-        case 3: return launch_ws_t<4, 3, 3, true, kModeForce, 128, 4, true>(p, s, num_sms, tm);
-        case 4: return launch_ws_t<4, 2, 4, true>(p, s, num_sms);
+        case 2: return launch_ws_t<4, 2, 3, true, kModeForce, 256, 4>(p, s, num_sms);
+        case 3: return launch_ws_t<4, 3, 4, true, kModeForce, 256, 4>(p, s, num_sms);
+        case 4: return launch_ws_t<4, 3, 3, true, kModeForce, 256, 3>(p, s, num_sms);
         case 5: return launch_ws_t<4, 3, 4, true>(p, s, num_sms);
-        case 6: return launch_ws_t<4, 2, 4, true, kModeForce, 128, 3, true>(p, s, num_sms, tm);
+        case 6: return launch_ws_t<4, 3, 3, true, kModeForce, 256, 4>(p, s, num_sms);
         case 7: return launch_ws_t<4, 3, 3, true, kModeForce, 128, 6>(p, s, num_sms);
         default: return cudaErrorInvalidValue;
     }
 }
 
-bool ws_variant_uses_tma(int variant) { return variant == 1 || variant == 3 || variant == 6; }
+bool ws_variant_uses_tma(int variant) { return variant == 1; }
 
 cudaError_t launch_ws_search(const Params& p, cudaStream_t s, int num_sms) {
     return launch_ws_t<4, 3, 4, false, kModeSearch>(p, s, num_sms);
