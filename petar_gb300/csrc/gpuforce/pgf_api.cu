@@ -633,7 +633,7 @@ bool pack_walk(TagState& t, int k, int w, const Slot3& o, const void* const* epi
         d.hx = d.hy = d.hz = d.rs_max = 0.f;
     }
     d.part = 0;
-        d.pad[0] = d.pad[1] = d.pad[2] = 0.f;
+    d.pad[0] = d.pad[1] = d.pad[2] = 0.f;
     d.rcut2 = g.walk_rcut2.empty() ? g.rcut2 : g.walk_rcut2[w];
     t.h_walks.h[k] = d;
     t.h_order.h[k] = k;
