@@ -180,6 +180,10 @@ int pgf_set_mode(int mode);
  * with different consumer-warp counts, i-particles per thread and scalar or
  * packed FP32x2 arithmetic.  The choice applies to later dispatches. */
 #define PGF_NUM_KERNEL_VARIANTS 9
+/* The variant used until one is chosen: the warp-specialised kernel with
+ * 256-entry EP tiles, the fastest on the 1M binary Plummer and the King 4M
+ * workloads on GB300.  pgf_autotune picks per workload. */
+#define PGF_DEFAULT_KERNEL_VARIANT 7
 int pgf_set_kernel_variant(int variant);
 int pgf_get_kernel_variant(int *variant);
 
@@ -342,7 +346,7 @@ typedef struct pgf_nbody_config {
     int n_leaf_limit;         /* a cell splits while it holds more particles */
     int n_group_limit;        /* i-groups hold at most this many particles (or are leaves) */
     int precision;            /* PGF_PRECISION_MIXED or PGF_PRECISION_FP64 */
-    int kernel_variant;       /* as pgf_set_kernel_variant, TMA variants excluded; -1 = default */
+    int kernel_variant;       /* as pgf_set_kernel_variant, TMA variants excluded; -1 = PGF_DEFAULT_KERNEL_VARIANT */
     double list_capacity_factor; /* room kept for growth of cells and lists (>= 1; 0 = 2) */
 } pgf_nbody_config;
 

@@ -157,7 +157,7 @@ struct State {
     bool user_stream = false;
     double eps2 = 0, rcut2 = 0, G = 1;
     int precision = PGF_PRECISION_MIXED;
-    int variant = 0;  // mixed-precision kernel variant (pgf_set_kernel_variant)
+    int variant = PGF_DEFAULT_KERNEL_VARIANT;  // mixed-precision kernel variant (pgf_set_kernel_variant)
     int stages = 0;   // dispatch pipeline stages (pgf_set_dispatch_stages); 0 = by size
     bool walk_split = true;  // split the largest walks of small dispatches (pgf_set_walk_split)
     int mode = PGF_MODE_FORCE;

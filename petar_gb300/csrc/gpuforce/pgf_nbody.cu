@@ -887,15 +887,29 @@ __global__ __launch_bounds__(128) void group_reduce_kernel(TreeHdr* h, const TCe
     if (h->err) return;
     const int64_t ng = h->n_groups, nq = n_chunks(h);
     for (int64_t g = gtid(); g < ng; g += gstride()) {
+        // Counts are read kB chunks at a time before their offsets are
+        // written back: loads that follow a store to the same array would
+        // otherwise wait one memory latency per chunk.
+        constexpr int kB = 8;
         int64_t re = 0, rs = 0;
-#pragma unroll 8
-        for (int64_t q = 0; q < nq; ++q) {
-            const int64_t t = q * ng + g;
-            const int e = task_e[t], s = task_s[t];
-            task_e[t] = (int32_t)re;
-            task_s[t] = (int32_t)rs;
-            re += e;
-            rs += s;
+        for (int64_t q0 = 0; q0 < nq; q0 += kB) {
+            int e[kB], s[kB];
+#pragma unroll
+            for (int k = 0; k < kB; ++k) {
+                const int64_t t = (q0 + k) * ng + g;
+                e[k] = q0 + k < nq ? task_e[t] : 0;
+                s[k] = q0 + k < nq ? task_s[t] : 0;
+            }
+#pragma unroll
+            for (int k = 0; k < kB; ++k) {
+                if (q0 + k < nq) {
+                    const int64_t t = (q0 + k) * ng + g;
+                    task_e[t] = (int32_t)re;
+                    task_s[t] = (int32_t)rs;
+                }
+                re += e[k];
+                rs += s[k];
+            }
         }
         const int ne = (int)re, ns = (int)rs;
         const TCell& gc = cells[groups[g]];
@@ -1583,7 +1597,7 @@ int pgf_nbody_create(const pgf_nbody_config* cfg, int64_t n, const double* pos, 
     if (!(cfg->r_out > 0.0)) return nb_fail(PGF_ERR_ARG, "r_out must be positive");
     if (cfg->precision != PGF_PRECISION_MIXED && cfg->precision != PGF_PRECISION_FP64)
         return nb_fail(PGF_ERR_ARG, "unknown precision %d", cfg->precision);
-    const int variant = cfg->kernel_variant < 0 ? PGF_NUM_KERNEL_VARIANTS - 1 : cfg->kernel_variant;
+    const int variant = cfg->kernel_variant < 0 ? PGF_DEFAULT_KERNEL_VARIANT : cfg->kernel_variant;
     if (!valid_variant(variant)) return nb_fail(PGF_ERR_ARG, "kernel variant %d is not available here", variant);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return nb_fail(PGF_ERR_NO_DEVICE, "no CUDA device");

@@ -27,6 +27,7 @@ PGF_OK = 0
 PGF_PRECISION_MIXED = 0
 PGF_PRECISION_FP64 = 1
 NUM_KERNEL_VARIANTS = 9  # PGF_NUM_KERNEL_VARIANTS
+DEFAULT_KERNEL_VARIANT = 7  # PGF_DEFAULT_KERNEL_VARIANT
 PGF_MODE_FORCE = 0
 PGF_MODE_NEIGHBOR_SEARCH = 1
 PGF_MODE_FORCE_CHANGEOVER = 2

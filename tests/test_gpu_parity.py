@@ -217,11 +217,12 @@ def test_recompute_reproduces():
     np.testing.assert_array_equal(a["acc"], b["acc"])
 
 
-@pytest.mark.parametrize("variant", list(range(1, gpuforce.NUM_KERNEL_VARIANTS)))
+@pytest.mark.parametrize("variant", [v for v in range(gpuforce.NUM_KERNEL_VARIANTS)
+                                     if v != gpuforce.DEFAULT_KERNEL_VARIANT])
 @pytest.mark.parametrize("case", ["kernel_test_rsvar", "plummer2048_walks", "ragged", "binaries"])
 def test_kernel_variants(case, variant):
     """Every mixed-precision kernel variant the autotuner may pick meets the
-    same parity bar (variant 0 is covered by the tests above)."""
+    same parity bar (the default variant is covered by the tests above)."""
     if case == "ragged":
         wb = _ragged_batch()
     elif case == "binaries":
@@ -232,7 +233,7 @@ def test_kernel_variants(case, variant):
     try:
         res = gpuforce.compute(wb, PGF_PRECISION_MIXED)
     finally:
-        gpuforce.set_kernel_variant(0)
+        gpuforce.set_kernel_variant(gpuforce.DEFAULT_KERNEL_VARIANT)
     check(wb, res, PGF_PRECISION_MIXED, label=f"{case} v{variant}")
 
 
@@ -249,10 +250,10 @@ def test_autotune_picks_a_variant_and_keeps_results():
     gpuforce.recompute(0)
     f = gpuforce.retrieve(rec, tag=0)
     check(wb, dict(acc=f["acc"], pot=f["pot"], nnb=f["n_ngb"]), PGF_PRECISION_MIXED, o=o, label="autotuned")
-    gpuforce.set_kernel_variant(0)
+    gpuforce.set_kernel_variant(gpuforce.DEFAULT_KERNEL_VARIANT)
 
 
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, gpuforce.DEFAULT_KERNEL_VARIANT])
 def test_pipelined_dispatch_matches_single_launch(variant):
     """A dispatch split into pipeline stages (overlapped packing, copies and
     kernels over contiguous walk ranges) gives bit-identical forces, counts
@@ -278,7 +279,7 @@ def test_pipelined_dispatch_matches_single_launch(variant):
         out["recompute"] = (gpuforce.retrieve(rec, tag=0).copy(), None)
     finally:
         gpuforce.set_dispatch_stages(0)
-        gpuforce.set_kernel_variant(0)
+        gpuforce.set_kernel_variant(gpuforce.DEFAULT_KERNEL_VARIANT)
         gpuforce.set_walk_split(True)
     f1, r1 = out[1]
     for key in (2, 3, 8, "recompute"):
