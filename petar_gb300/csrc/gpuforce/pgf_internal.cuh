@@ -233,6 +233,9 @@ cudaError_t launch_retest(const Params& p, cudaStream_t s, int num_sms);
 // pot_soft and acorr (optional) are the changeover and gradient modes' outputs.
 cudaError_t launch_combine_parts(const SplitRec* recs, int n_recs, Accp* accp, int32_t* nnb, double* pot_soft,
                                  Accp* acorr, cudaStream_t s);
+// Copies every split walk's EPI rows (and its changeover / gradient records,
+// when given) from row0 to the rows of parts 1 .. n_parts-1.
+cudaError_t launch_split_rows(const SplitRec* recs, int n_recs, EpiDev* epi, CoRec* co, Accp* acc, cudaStream_t s);
 // Builds the (hi, lo) FP32 copies of the EPJ / SPJ arrays.
 cudaError_t launch_split_j(const EpjMix* epj, int64_t n_epj, EpjF32* epj32, const SpjMix* spj, int64_t n_spj,
                            SpjF32* spj32, cudaStream_t s);

@@ -616,6 +616,25 @@ cudaError_t launch_combine_parts(const SplitRec* recs, int n_recs, Accp* accp, i
     return cudaGetLastError();
 }
 
+__global__ __launch_bounds__(256) void split_rows_kernel(const SplitRec* __restrict__ recs, EpiDev* epi, CoRec* co,
+                                                         Accp* acc) {
+    const SplitRec r = recs[blockIdx.x];
+    const int64_t total = (int64_t)(r.n_parts - 1) * r.n_i;
+    for (int64_t k = threadIdx.x; k < total; k += blockDim.x) {
+        const int64_t i = k % r.n_i;
+        const int64_t src = (int64_t)r.row0 + i, dst = (int64_t)r.rows1 + k;
+        epi[dst] = epi[src];
+        if (co) co[dst] = co[src];
+        if (acc) acc[dst] = acc[src];
+    }
+}
+
+cudaError_t launch_split_rows(const SplitRec* recs, int n_recs, EpiDev* epi, CoRec* co, Accp* acc, cudaStream_t s) {
+    if (n_recs <= 0) return cudaSuccess;
+    split_rows_kernel<<<n_recs, 256, 0, s>>>(recs, epi, co, acc);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_retest(const Params& p, cudaStream_t s, int num_sms) {
     retest_kernel<<<num_sms * 2, 256, 0, s>>>(p);
     return cudaGetLastError();
