@@ -738,17 +738,17 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     }
     t.n_split = 0;
     if (gr_mode) {
-        PGF_CUDA(t.h_epi_acc.ensure(ni_all));
+        PGF_CUDA(t.h_epi_acc.ensure(ni));
         PGF_CUDA(t.epi_acc.ensure(ni_all));
         PGF_CUDA(t.acorr.ensure(ni_all));
     }
     if (co_mode) {
-        PGF_CUDA(t.h_epi_co.ensure(ni_all));
+        PGF_CUDA(t.h_epi_co.ensure(ni));
         PGF_CUDA(t.epi_co.ensure(ni_all));
         PGF_CUDA(t.pot_soft.ensure(ni_all));
     }
 
-    PGF_CUDA(t.h_epi.ensure(ni_all));
+    PGF_CUDA(t.h_epi.ensure(ni));
     PGF_CUDA(t.h_id_epj.ensure(ne));
     PGF_CUDA(t.h_id_spj.ensure(ns));
     PGF_CUDA(t.h_walks.ensure(n_desc));
