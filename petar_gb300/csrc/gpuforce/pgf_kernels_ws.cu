@@ -38,8 +38,8 @@ namespace pgf {
 namespace {
 
 // Ring geometry is a template parameter of each variant: TE EPJ entries per
-// EP tile (TE / 32 per producer lane), TE / 2 SPJ entries per SP tile, NS ring
-// slots.
+// EP tile (TE / 32 per producer lane), TE SPJ entries per SP tile (TE / 2
+// with TMA staging), NS ring slots.
 constexpr int kFlush = 256;   // pairs per consumer thread between FP64 flushes
 constexpr int kKMax = 1 << 22;
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;
@@ -169,9 +169,11 @@ struct SlotEP {
     float4 fr[TE];  // far:  hi x, y, z, m
     int nidx[TE];   // near: entry index in the tile (for re-tests)
 };
+// SPJ tiles hold up to TE entries (TE / 2 with TMA staging): 48 bytes an
+// entry, within the EP tile's 52, so they cost no shared memory.
 template <int TE>
 struct SlotSP {
-    float4 sp[TE / 2][3];
+    float4 sp[TE][3];
 };
 // Packed tiles: far EPJ and SPJ as pairs of j, component-interleaved, so a
 // consumer reads (x0, x1), (y0, y1), ... as float2 operands of the FP32x2
@@ -185,7 +187,7 @@ struct SlotEPx2 {
 };
 template <int TE>
 struct SlotSPx2 {
-    float4 sp[TE / 4][6];  // x, y, z, m, -Qxx, -Qyy, -Qzz, -Qxy, -Qxz, -Qyz, -c (pairs), pad
+    float4 sp[TE / 2][6];  // x, y, z, m, -Qxx, -Qyy, -Qzz, -Qxy, -Qxz, -Qyz, -c (pairs), pad
 };
 template <bool PK, int TE>
 union Slot {
@@ -319,8 +321,8 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
     constexpr bool SR = MD == kModeSearch, CO = MD == kModeChangeover;
     static_assert(!TM || (MD == kModeForce && TE == 128), "TMA staging: force mode, 128-entry EP tiles");
     constexpr int kMaxPass = CW * 32 * KI;
-    constexpr int kTileEP = TE, kTileSP = TE / 2, kSlots = NS;
-    constexpr int QE = TE / 32, QS = TE / 64;  // EPJ and SPJ entries per lane and tile
+    constexpr int kTileEP = TE, kTileSP = TM ? TE / 2 : TE, kSlots = NS;
+    constexpr int QE = TE / 32, QS = kTileSP / 32;  // EPJ and SPJ entries per lane and tile
     constexpr int QB = QE < 4 ? QE : 4, QSB = QS < 2 ? QS : 2;  // ... converted at a time
     static_assert(QE % QB == 0 && QS % QSB == 0, "tiles of whole sub-batches");
     static_assert(QS >= 1 && TE % 64 == 0, "EP tiles of a multiple of 64 entries");
