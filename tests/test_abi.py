@@ -74,6 +74,9 @@ def test_variant_count_matches_header():
     text = (ROOT / "include" / "petar_gpuforce.h").read_text()
     n = int(re.search(r"#define PGF_NUM_KERNEL_VARIANTS (\d+)", text).group(1))
     assert n == gpuforce.NUM_KERNEL_VARIANTS
+    d = int(re.search(r"#define PGF_DEFAULT_KERNEL_VARIANT (\d+)", text).group(1))
+    assert d == gpuforce.DEFAULT_KERNEL_VARIANT
+    assert 0 <= d < n
 
 
 def test_nbody_entry_points_without_device():
