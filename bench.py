@@ -217,8 +217,8 @@ def fp32_peak_tflops() -> dict:
     """FP32 FMA throughput of this GPU, measured with scalar FMAs and with
     packed FP32x2 FMAs (TFLOP/s, best of three)."""
     import ctypes
-    from petar_gb300.build import build_probe
-    lib = ctypes.CDLL(str(build_probe()))
+    from bench_support import build_fp32_probe
+    lib = ctypes.CDLL(str(build_fp32_probe()))
     out = {}
     for key, fn in (("ffma", lib.pgf_probe_fp32_peak), ("ffma2", lib.pgf_probe_fp32x2_peak)):
         fn.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
@@ -243,6 +243,21 @@ def traffic_from_profiles() -> float | None:
             if m:
                 return float(m.group(1))
     return None
+
+
+def accuracy_violations(acc: dict) -> list[str]:
+    """Mixed-precision results against the plain FP64 kernel on every particle
+    of the workload: median <= 1e-6, 99.9th percentile <= 1e-5 and max <= 1e-3
+    relative error for force and potential, neighbour counts equal."""
+    bad = []
+    for q in ("force", "pot"):
+        for stat, bound in (("median", 1e-6), ("p999", 1e-5), ("max", 1e-3)):
+            v = acc[f"{q}_rel_err_{stat}"]
+            if not v <= bound:
+                bad.append(f"{q} {stat} {v:.3g} > {bound:g}")
+    if acc["n_ngb_mismatches"]:
+        bad.append(f"{acc['n_ngb_mismatches']} neighbour-count mismatches")
+    return bad
 
 
 def sample_walks(wb, target_interactions: float, seed: int = 7) -> np.ndarray:
@@ -422,6 +437,7 @@ def run_ours(args):
 
     # ---- plain FP64 kernel on the same lists ----
     fp64 = None
+    parity_violations: list[str] = []
     if not args.no_fp64:
         gpuforce.set_precision(PGF_PRECISION_FP64)
         gpuforce.recompute(0)
@@ -442,8 +458,12 @@ def run_ours(args):
         fp64 = {"value": v64, "unit": "Ginteractions/s", "ms_per_step": 1e3 * t64, "speedup_mixed_vs_fp64": value / v64,
                 "accuracy_mixed_vs_fp64": {
                     "force_rel_err_median": float(np.median(ea)), "force_rel_err_p999": float(np.quantile(ea, 0.999)),
+                    "force_rel_err_max": float(ea.max()),
                     "pot_rel_err_median": float(np.median(ep)), "pot_rel_err_p999": float(np.quantile(ep, 0.999)),
-                    "n_ngb_mismatches": int((f_mixed["n_ngb"] != f64["n_ngb"]).sum())}}
+                    "pot_rel_err_max": float(ep.max()),
+                    "n_ngb_mismatches": int((f_mixed["n_ngb"] != f64["n_ngb"]).sum()),
+                    "bounds": "median <= 1e-6, p99.9 <= 1e-5, max <= 1e-3, counts exact"}}
+        parity_violations += accuracy_violations(fp64["accuracy_mixed_vs_fp64"])
         gpuforce.set_precision(PGF_PRECISION_MIXED)
 
     # ---- end to end through the C ABI with host records ----
@@ -581,9 +601,15 @@ def run_ours(args):
         "retest_records_per_step": n_retest, "wall_s_timed_region": wall, "modes": modes,
         "kdk_graph": kdk, "configs": configs,
     }
+    if parity_violations:
+        out["parity_violations"] = parity_violations
     print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.barrier()
+    if parity_violations:
+        # A throughput whose results miss the parity bar is not a result.
+        log("parity violated: " + "; ".join(parity_violations))
+        sys.exit(3)
 
 
 def run_fdps_batches(wb, rec, n_int: int, batch: int = 200, reps: int = 3) -> dict:

@@ -273,10 +273,19 @@ const char *pgf_last_error(void);
  * array of about 2.6 MB that every GPU loading the library keeps until the
  * process exits, sized for at most PGF_NOALLOC_MAX_WALKS walks per call;
  * larger calls return PGF_ERR_CAPACITY.  The first call on each device looks
- * up that array's device address (with the device current); make that first
- * call before any stream capture.  All calls share the array: calls on one
- * stream are ordered and safe, calls whose work overlaps on the GPU (other
- * streams, other host threads) race and corrupt each other's results.
+ * up that array's device address (with the device current) and keeps it; make
+ * that first call before any stream capture, and do not reset the device
+ * (cudaDeviceReset) while the library is in use, since the kept address would
+ * then be stale.  All calls share the array: calls on one stream are ordered
+ * and safe, calls whose work overlaps on the GPU (other streams, other host
+ * threads) race and corrupt each other's results.
+ *
+ * Every call blocks the calling thread: walk rows and ids are checked on the
+ * device first, and the call copies the check's result to the host and waits
+ * on the stream for it (so it also waits for the work queued on the stream
+ * before it) before it launches the force kernels.  Those are then left
+ * running on the stream.  They contain no waits and report no device errors,
+ * so the check is the only device-side failure the call can report.
  *
  * walk_table: 6 int64 per walk: i_begin, n_i, epj_begin, n_epj, spj_begin,
  *   n_spj (rows of epi; offsets into id_epj / id_spj).
@@ -285,11 +294,11 @@ const char *pgf_last_error(void);
  * spj: pgf_spj_device records.
  * accp: 4 doubles per i-particle: acc x, y, z, pot (G applied); n_ngb: one
  *   int per i-particle.  Rows that no walk covers are left untouched.
- * epi, epj, spj and accp must be 32-byte aligned.  Walk rows and ids are
- * checked on the device before the force kernels start (the call waits for
- * that check); the force kernels themselves are left running on the stream
- * (a cudaStream_t passed as void*; NULL is the legacy default stream).
- * errbuf (optional, errbuf_len bytes) receives a message on failure. */
+ * epi, epj, spj and accp must be 32-byte aligned, walk_table and epj_r_search
+ * 8-byte aligned, id_epj, id_spj and n_ngb 4-byte aligned (PGF_ERR_ARG
+ * otherwise).  cuda_stream is a cudaStream_t passed as void* that belongs to
+ * the current device (PGF_ERR_ARG otherwise); NULL is the legacy default
+ * stream.  errbuf (optional, errbuf_len bytes) receives a message on failure. */
 #define PGF_NOALLOC_MAX_WALKS 16384
 
 typedef struct pgf_epj_device { /* 32 bytes */

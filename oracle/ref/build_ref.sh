@@ -14,10 +14,14 @@
 # The SIMD kernels are x86 only; on other hosts only the NoSimd library is
 # built.  The NoSimd build uses -ffp-contract=off so its FP64 results are
 # defined by source order alone.
-# Usage: oracle/ref/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/ref/build_ref.sh REFERENCE_ROOT   (or PETAR_REFERENCE_ROOT in the environment)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${PETAR_REFERENCE_ROOT:-}}"
+if [ -z "$REF" ]; then
+    echo "usage: $0 REFERENCE_ROOT (the PeTar checkout whose src/ holds soft_force.hpp)" >&2
+    exit 2
+fi
 SRC="$REF/src"
 OUT="$HERE/../_ref"
 if [ ! -f "$SRC/soft_force.hpp" ]; then

@@ -116,23 +116,9 @@ def build_harness(force: bool = False) -> Path:
     return out
 
 
-def build_probe(force: bool = False) -> Path:
-    """Compiles the FP32 FMA throughput probe into ``lib/libpgf_probe.so``."""
-    LIB.mkdir(exist_ok=True)
-    out = LIB / "libpgf_probe.so"
-    src = CSRC / "probe" / "fp32_peak.cu"
-    if not force and _newer(out, [src]):
-        return out
-    tmp = out.with_suffix(".so.tmp")
-    _run([_nvcc(), *ARCH_FLAGS, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", str(src), "-o", str(tmp)])
-    os.replace(tmp, out)
-    return out
-
-
 def build_all(force: bool = False, verbose: bool = False) -> None:
-    with ThreadPoolExecutor(max_workers=3) as ex:
-        futs = [ex.submit(build_gpuforce, force, verbose), ex.submit(build_harness, force),
-                ex.submit(build_probe, force)]
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        futs = [ex.submit(build_gpuforce, force, verbose), ex.submit(build_harness, force)]
         for f in futs:
             f.result()
 

@@ -77,9 +77,11 @@ __global__ __launch_bounds__(128) void walk_prep_kernel(int n_walk, const int64_
     __syncthreads();
     const int64_t* row = table + 6 * (int64_t)w;
     const int64_t i0 = row[0], ni = row[1], e0 = row[2], ne = row[3], s0 = row[4], ns = row[5];
-    const bool ok = i0 >= 0 && ni >= 0 && ni <= 0x7fffffff && i0 + ni <= n_epi && e0 >= 0 && ne >= 0 &&
-                    ne <= 0x7fffffff && e0 + ne <= n_id_epj && s0 >= 0 && ns >= 0 && ns <= 0x7fffffff &&
-                    s0 + ns <= n_id_spj;
+    // Each range is tested as offset <= size - count with both terms
+    // non-negative, so no sum can overflow whatever the table holds.
+    const bool ok = ni >= 0 && ni <= 0x7fffffff && ni <= n_epi && i0 >= 0 && i0 <= n_epi - ni && ne >= 0 &&
+                    ne <= 0x7fffffff && ne <= n_id_epj && e0 >= 0 && e0 <= n_id_epj - ne && ns >= 0 &&
+                    ns <= 0x7fffffff && ns <= n_id_spj && s0 >= 0 && s0 <= n_id_spj - ns;
     if (!ok) {
         if (t == 0) atomicOr(err, kBadWalk);
         return;
@@ -165,10 +167,26 @@ extern "C" int pgf_force_device_noalloc(int n_walk, const int64_t* walk_table, c
     if ((reinterpret_cast<uintptr_t>(accp) | reinterpret_cast<uintptr_t>(epj) | reinterpret_cast<uintptr_t>(spj) |
          reinterpret_cast<uintptr_t>(epi)) & 31)
         return fail(errbuf, errbuf_len, PGF_ERR_ARG, "pgf_force_device_noalloc: epi, epj, spj and accp must be 32-byte aligned");
+    if ((reinterpret_cast<uintptr_t>(walk_table) | reinterpret_cast<uintptr_t>(epj_r_search)) & 7)
+        return fail(errbuf, errbuf_len, PGF_ERR_ARG, "pgf_force_device_noalloc: walk_table and epj_r_search must be 8-byte aligned");
+    if ((reinterpret_cast<uintptr_t>(id_epj) | reinterpret_cast<uintptr_t>(id_spj) | reinterpret_cast<uintptr_t>(n_ngb)) & 3)
+        return fail(errbuf, errbuf_len, PGF_ERR_ARG, "pgf_force_device_noalloc: id_epj, id_spj and n_ngb must be 4-byte aligned");
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail(errbuf, errbuf_len, PGF_ERR_NO_DEVICE, "pgf_force_device_noalloc: %s", cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return fail(errbuf, errbuf_len, PGF_ERR_NO_DEVICE, "pgf_force_device_noalloc: device %d", dev);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(cuda_stream);
+    if (s) {
+        // The scratch address below belongs to the current device; work
+        // queued on another device's stream would use that device's array
+        // through the wrong address.
+        int sdev = -1;
+        e = cudaStreamGetDevice(s, &sdev);
+        if (e != cudaSuccess) return fail(errbuf, errbuf_len, PGF_ERR_ARG, "pgf_force_device_noalloc: stream: %s", cudaGetErrorString(e));
+        if (sdev != dev)
+            return fail(errbuf, errbuf_len, PGF_ERR_ARG,
+                        "pgf_force_device_noalloc: the stream belongs to device %d, the current device is %d", sdev, dev);
+    }
     if (!g_scratch_addr[dev]) {
         unsigned char* ptr = nullptr;
         e = cudaGetSymbolAddress(reinterpret_cast<void**>(&ptr), g_noalloc_scratch);
@@ -185,7 +203,6 @@ extern "C" int pgf_force_device_noalloc(int n_walk, const int64_t* walk_table, c
     WalkDesc* desc = reinterpret_cast<WalkDesc*>(base + kDescOff);
     int32_t* order = reinterpret_cast<int32_t*>(base + kOrderOff);
     Retest* retest = reinterpret_cast<Retest*>(base + kRetestOff);
-    cudaStream_t s = reinterpret_cast<cudaStream_t>(cuda_stream);
 
     e = cudaMemsetAsync(flags, 0, 3 * sizeof(int32_t), s);
     if (e != cudaSuccess) return fail(errbuf, errbuf_len, PGF_ERR_CUDA, "pgf_force_device_noalloc: %s", cudaGetErrorString(e));

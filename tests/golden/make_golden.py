@@ -47,6 +47,7 @@ Usage: python tests/golden/make_golden.py [fixture names]   (default: all)
 from __future__ import annotations
 
 import ctypes
+import os
 import subprocess
 import sys
 from pathlib import Path
@@ -217,7 +218,9 @@ def run_ref_gradient(case: dict) -> dict:
 
 def main() -> None:
     if not (REF_LIBS / "libref_nosimd.so").exists() or not (REF_LIBS / "libref_changeover.so").exists():
-        subprocess.run([str(ROOT / "oracle" / "ref" / "build_ref.sh")], check=True)
+        # The reference checkout: PETAR_REFERENCE_ROOT, else the one this project was built against.
+        ref = os.environ.get("PETAR_REFERENCE_ROOT", "/root/reference")
+        subprocess.run([str(ROOT / "oracle" / "ref" / "build_ref.sh"), ref], check=True)
     sys.path.insert(0, str(ROOT))
     only = set(sys.argv[1:])
     if not only or "changeover_w" in only:

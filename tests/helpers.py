@@ -51,3 +51,19 @@ def rows_batch(wb: WalkBatch, rows: np.ndarray) -> WalkBatch:
         eps2=wb.eps2, rcut2=wb.rcut2, G=wb.G,
         walk_rcut2=None if wb.walk_rcut2 is None else wb.walk_rcut2[w],
         epi_index=None if wb.epi_index is None else wb.epi_index[rows])
+
+
+# Mixed-precision parity bar of every GPU test: relative force and potential
+# error median <= 1e-6, 99.9th percentile <= 1e-5 and max <= 1e-3 against the
+# FP64 oracle, neighbour counts bit-exact.
+MIXED_MEDIAN = 1e-6
+MIXED_P999 = 1e-5
+MIXED_MAX = 1e-3
+
+
+def assert_mixed_parity(acc: np.ndarray, pot: np.ndarray, nnb: np.ndarray, o: dict, label: str = "") -> tuple:
+    np.testing.assert_array_equal(nnb, o["nnb"], err_msg=f"{label} neighbour counts")
+    sa, sp = stats(rel_err_vec(acc, o["acc"])), stats(rel_err(pot, o["pot"]))
+    for name, s in (("force", sa), ("pot", sp)):
+        assert s["median"] <= MIXED_MEDIAN and s["p999"] <= MIXED_P999 and s["max"] <= MIXED_MAX, (label, name, s)
+    return sa, sp

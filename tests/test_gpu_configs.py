@@ -1,6 +1,9 @@
-"""Per-configuration parity on the GPU for the named benchmark configurations
-that are not the bench line itself:
+"""Per-configuration parity on the GPU for the named benchmark configurations:
 
+* Plummer 1,048,576 centres of mass with 50% binaries (theta 0.3,
+  r_out 0.003), the bench workload: the default mixed-precision kernel and
+  the plain FP64 kernel over all walks, checked against the FP64 oracle on
+  the 20 most expensive walks, the 20 cheapest and 300 random ones.
 * Plummer 65,536 (theta 0.3, r_out 0.008): the mixed kernel against the FP64
   oracle on all walks, and its error against FP64 direct N^2 summation, which
   must equal the tree's own error (the kernel adds nothing visible to it).
@@ -17,7 +20,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import rel_err, rel_err_vec, stats
+from helpers import MIXED_MAX, assert_mixed_parity, rel_err, rel_err_vec, stats
 from petar_gb300 import gpuforce, ics, walks
 from petar_gb300.gpuforce import PGF_PRECISION_FP64, PGF_PRECISION_MIXED
 
@@ -33,6 +36,34 @@ def _errors(res, o, rows=None):
         acc, pot, nnb = acc[rows], pot[rows], nnb[rows]
     np.testing.assert_array_equal(nnb, o["nnb"])
     return stats(rel_err_vec(acc, o["acc"])), stats(rel_err(pot, o["pot"]))
+
+
+def test_plummer1m_bin50_headline_config():
+    """The bench workload itself (1,572,864 particles, 10,882 walks): the
+    default mixed-precision kernel at the full parity bar, the plain FP64
+    kernel to 1e-12, counts exact for both."""
+    cl = ics.make_plummer_cluster(3, 1048576, 0.003, binary_fraction=0.5, theta=0.3)
+    wb = walks.build_walks(cl)
+    assert cl.n == 1572864
+    cost = wb.n_epi.astype(np.int64) * (wb.n_epj + 2 * wb.n_spj)
+    by_cost = np.argsort(cost, kind="stable")
+    by_cost = by_cost[wb.n_epi[by_cost] > 0]
+    rng = np.random.default_rng(13)
+    sw = np.unique(np.concatenate([by_cost[-20:], by_cost[:20], rng.choice(wb.n_walk, 300, replace=False)]))
+    rows = np.concatenate([np.arange(wb.epi_disp[w], wb.epi_disp[w + 1]) for w in sw])
+    o = oracle.force(wb.subset(sw))
+    assert gpuforce.get_kernel_variant() == gpuforce.DEFAULT_KERNEL_VARIANT
+    res = gpuforce.compute(wb, PGF_PRECISION_MIXED)
+    assert_mixed_parity(res["acc"][rows], res["pot"][rows], res["nnb"][rows], o, label="C3 mixed")
+    f64 = gpuforce.compute(wb, PGF_PRECISION_FP64)
+    np.testing.assert_array_equal(f64["nnb"][rows], o["nnb"])
+    assert rel_err_vec(f64["acc"][rows], o["acc"]).max() <= 1e-12
+    assert rel_err(f64["pot"][rows], o["pot"]).max() <= 1e-12
+    # Every particle: mixed against the FP64 kernel (the comparison bench.py gates on).
+    np.testing.assert_array_equal(res["nnb"], f64["nnb"])
+    for e in (rel_err_vec(res["acc"], f64["acc"]), rel_err(res["pot"], f64["pot"])):
+        s = stats(e)
+        assert s["median"] <= MIXED_MEDIAN and s["p999"] <= MIXED_P999 and s["max"] <= MIXED_MAX, s
 
 
 def test_plummer65k_against_oracle_and_direct_sum():

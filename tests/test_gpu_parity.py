@@ -179,8 +179,8 @@ def test_reference_call_sequence_and_tags():
           rec.n_spj[ws], None, 0, None, 0, False)
     for tag, ws in enumerate(halves):
         gpuforce.RetrieveForceCUDA(tag + 2, ws.size, rec.n_epi[ws], rec.p_force[ws])
-    np.testing.assert_array_equal(rec.force["n_ngb"], o["nnb"])
-    assert rel_err_vec(rec.force["acc"], o["acc"]).max() < MIXED_MAX
+    check(wb, dict(acc=rec.force["acc"], pot=rec.force["pot"], nnb=rec.force["n_ngb"]), PGF_PRECISION_MIXED, o=o,
+          label="FDPS call sequence")
 
 
 def test_retrieve_errors():
