@@ -260,13 +260,16 @@ def accuracy_violations(acc: dict) -> list[str]:
     return bad
 
 
-def sample_walks(wb, target_interactions: float, seed: int = 7) -> np.ndarray:
-    rng = np.random.default_rng(seed)
-    order = rng.permutation(wb.n_walk)
-    per = wb.n_epi.astype(np.int64) * (wb.n_epj + wb.n_spj)
-    cum = np.cumsum(per[order])
-    k = int(np.searchsorted(cum, target_interactions)) + 1
-    return np.sort(order[:max(1, min(k, wb.n_walk))])
+CPU_SAMPLE_FRACTION = 0.5  # of the walks, seeded: the same sample in both legs
+CPU_SAMPLE_SEED = 7
+
+
+def sample_walks(wb, fraction: float = CPU_SAMPLE_FRACTION, seed: int = CPU_SAMPLE_SEED) -> np.ndarray:
+    """The CPU legs' sample: a seeded random fraction of the walks (the same
+    walks in the GPU arm's cpu_baseline and in --impl reference)."""
+    order = np.random.default_rng(seed).permutation(wb.n_walk)
+    k = max(1, int(round(fraction * wb.n_walk)))
+    return np.sort(order[:k])
 
 
 def cpu_reference_runner():
@@ -316,26 +319,31 @@ def cpu_reference_runner():
     return "reference", run
 
 
-def time_cpu(wb, seconds: float) -> tuple[str, dict, callable]:
-    """Chooses a sample of walks worth about `seconds` of CPU work."""
+def time_cpu(wb) -> tuple[str, dict, callable]:
+    """The CPU legs' runner and their fixed seeded sample of the walks."""
     kind, run = cpu_reference_runner()
-    calib = wb.subset(sample_walks(wb, 2e8, seed=11))
-    t = time.time()
-    run(calib)
-    rate = sum(calib.interactions()) / max(time.time() - t, 1e-3)
-    sub = wb.subset(sample_walks(wb, rate * seconds))
+    sub = wb.subset(sample_walks(wb))
     n_int = sum(sub.interactions())
-    desc = (f"{sub.n_walk} of {wb.n_walk} walks chosen at random (seed 7), {n_int:.3e} of "
+    desc = (f"{sub.n_walk} of {wb.n_walk} walks chosen at random (seed {CPU_SAMPLE_SEED}), {n_int:.3e} of "
             f"{sum(wb.interactions()):.3e} interactions")
     return kind, dict(batch=sub, n_int=n_int, desc=desc), run
+
+
+def workload_config(name: str, cl, wb) -> dict:
+    """The `config` of both arms' JSON lines."""
+    n_epep, n_epsp = wb.interactions()
+    return {"workload": name, "n_particles": int(cl.n), "n_walk": int(wb.n_walk),
+            "interactions_epep": int(n_epep), "interactions_epsp": int(n_epsp),
+            "theta": WORKLOADS[name]["theta"], "r_out": WORKLOADS[name]["r_out"],
+            "l2": "flushed between steps (256 MB write)", "replica_per_rank": True}
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    _, wb = make_workload(args.workload, 0)
-    kind, s, run = time_cpu(wb, args.cpu_seconds)
+    cl, wb = make_workload(args.workload, 0)
+    kind, s, run = time_cpu(wb)
     for _ in range(args.warmup):
         run(s["batch"])
     ts = []
@@ -348,7 +356,7 @@ def run_reference(args):
            "unit": "Ginteractions/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1e3 * statistics.mean(ts), "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": args.workload, "sample": s["desc"]},
+           "config": workload_config(args.workload, cl, wb), "sample": s["desc"],
            "cpu_baseline": {"value": v, "unit": "Ginteractions/s", "cores": os.cpu_count(), "kind": kind,
                             "sample": s["desc"]},
            "e2e": {"value": v, "unit": "Ginteractions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -437,6 +445,7 @@ def run_ours(args):
 
     # ---- plain FP64 kernel on the same lists ----
     fp64 = None
+    f64 = None
     parity_violations: list[str] = []
     if not args.no_fp64:
         gpuforce.set_precision(PGF_PRECISION_FP64)
@@ -466,6 +475,11 @@ def run_ours(args):
         parity_violations += accuracy_violations(fp64["accuracy_mixed_vs_fp64"])
         gpuforce.set_precision(PGF_PRECISION_MIXED)
 
+    # ---- the reference's own CUDA kernels on the same lists ----
+    ref_gpu = None
+    if not args.no_fp64 and rank == 0:
+        ref_gpu = reference_gpu_kernel(wb, n_int, f64)
+
     # ---- end to end through the C ABI with host records ----
     ni, ne, ns = wb.epi_rs.size, wb.id_epj.size, wb.id_spj.size
     # EPJ: EpjMix 32 B + FP64 mass and r_search 16 B; SPJ: SpjMix 64 B + SpjQ64 64 B;
@@ -473,6 +487,9 @@ def run_ours(args):
     # 32 B + count 4 B per i, and the 16-byte status words.
     h2d = (wb.epj_mass.size * 48 + wb.spj_mass.size * 128 + ni * 32 + (ne + ns) * 4 + wb.n_walk * 100)
     d2h = ni * (32 + 4) + 16
+    # The library's dispatch autotuner: pipeline stages and split unit on
+    # this workload's host records (kept for the e2e steps below).
+    tuned_dispatch = gpuforce.autotune_dispatch(rec, tag=0, repeats=2)
     e2e_t = []
     for k in range(args.warmup + args.steps):
         barrier()
@@ -488,7 +505,8 @@ def run_ours(args):
     e2e = {"value": world * n_int * args.steps / e2e_total / 1e9, "unit": "Ginteractions/s",
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
            "ms_per_step": 1e3 * e2e_total / args.steps,
-           "breakdown_ms_per_step": {k: 1e3 * bd[k] / args.steps for k in ("copy", "send", "calc", "recv")}}
+           "breakdown_ms_per_step": {k: 1e3 * bd[k] / args.steps for k in ("copy", "send", "calc", "recv")},
+           "host_direct": gpuforce.host_direct_active(), "tuned_dispatch": tuned_dispatch}
 
     # ---- the other modes on the same lists ----
     modes = None
@@ -579,7 +597,7 @@ def run_ours(args):
 
     cpu = None
     if world == 1 and not args.no_cpu:
-        kind, s, run = time_cpu(wb, args.cpu_seconds)
+        kind, s, run = time_cpu(wb)
         t = time.time()
         run(s["batch"])
         dt = time.time() - t
@@ -591,15 +609,13 @@ def run_ours(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic",
-        "config": {"workload": args.workload, "n_particles": int(cl.n), "n_walk": int(wb.n_walk),
-                   "interactions_epep": n_epep, "interactions_epsp": n_epsp, "theta": WORKLOADS[args.workload]["theta"],
-                   "r_out": WORKLOADS[args.workload]["r_out"], "l2": "flushed between steps (256 MB write)",
-                   "replica_per_rank": True},
+        "config": workload_config(args.workload, cl, wb),
         "gpu_launches": 2 * args.steps,
         "kernel_variant": best_variant, "variant_main_ms": variant_ms,
         "fp64_plain": fp64, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
         "retest_records_per_step": n_retest, "wall_s_timed_region": wall, "modes": modes,
-        "kdk_graph": kdk, "configs": configs,
+        "kdk_graph": kdk, "configs": configs, "reference_gpu_kernel": ref_gpu,
+        "cpu_reference_x86": cpu_reference_x86(),
     }
     if parity_violations:
         out["parity_violations"] = parity_violations
@@ -610,6 +626,40 @@ def run_ours(args):
         # A throughput whose results miss the parity bar is not a result.
         log("parity violated: " + "; ".join(parity_violations))
         sys.exit(3)
+
+
+def reference_gpu_kernel(wb, n_int: int, f64) -> dict:
+    """The reference's force_kernel_ep_ep + force_kernel_ep_sp (compiled from
+    its sources into a cubin, launched as its functor launches them) on the
+    same lists: kernel time and accuracy against the plain FP64 kernel."""
+    import oracle
+    try:
+        r = oracle.ref_gpu(wb, repeats=3)
+    except oracle.ReferenceKernelUnavailable as e:
+        return {"unavailable": str(e)}
+    out = {"ms_per_step": r["ms"], "value": n_int / r["ms"] / 1e6, "unit": "Ginteractions/s",
+           "kernels": "force_kernel_ep_ep + force_kernel_ep_sp (src/force_gpu_cuda.cu), one launch each, all walks"}
+    if f64 is not None:
+        ea = np.linalg.norm(r["acc"] - f64["acc"], axis=1) / np.linalg.norm(f64["acc"], axis=1)
+        ep = np.abs(r["pot"] - f64["pot"]) / np.abs(f64["pot"])
+        out["accuracy_vs_fp64"] = {
+            "force_rel_err_median": float(np.median(ea)), "force_rel_err_p999": float(np.quantile(ea, 0.999)),
+            "force_rel_err_max": float(ea.max()), "pot_rel_err_median": float(np.median(ep)),
+            "pot_rel_err_p999": float(np.quantile(ep, 0.999)), "pot_rel_err_max": float(ep.max()),
+            "n_ngb_mismatches": int((r["nnb"] != f64["n_ngb"]).sum())}
+    return out
+
+
+def cpu_reference_x86() -> dict | None:
+    """The reference's AVX-512 CPU kernels (PhantomGrapeQuad FP32 and 64-bit)
+    and FP64 NoSimd functors on the same seeded sample of this workload,
+    measured on an x86 host by oracle/ref/time_cpu_reference.py (the GPU hosts
+    are aarch64): a side record read from its committed summary."""
+    p = ROOT / "profiles" / "cpu_reference_x86_plummer1m_bin50.md"
+    if not p.exists():
+        return None
+    m = re.search(r"^record: (\{.*\})$", p.read_text(), flags=re.M)
+    return json.loads(m.group(1)) if m else None
 
 
 def run_fdps_batches(wb, rec, n_int: int, batch: int = 200, reps: int = 3) -> dict:
@@ -633,6 +683,11 @@ def run_fdps_batches(wb, rec, n_int: int, batch: int = 200, reps: int = 3) -> di
                                        force_dtype=rec.force.dtype)
 
     out = {"walks_per_call": batch, "calls_per_evaluation": (nw + batch - 1) // batch, "unit": "Ginteractions/s"}
+    # The dispatch autotuner on one 200-walk call from the middle of the
+    # evaluation (the split unit matters for calls this small).
+    mid = nw // 2 // batch * batch
+    sub = walks_subset_records(rec, mid, min(nw, mid + batch))
+    out["tuned_dispatch"] = gpuforce.autotune_dispatch(sub, tag=0, repeats=3)
     try:
         for split in (True, False):
             gpuforce.set_walk_split(split)
@@ -647,6 +702,17 @@ def run_fdps_batches(wb, rec, n_int: int, batch: int = 200, reps: int = 3) -> di
     finally:
         gpuforce.set_walk_split(True)
     return out
+
+
+def walks_subset_records(rec, w0: int, w1: int):
+    """A Records view of walks [w0, w1): the same j arrays and pointer tables."""
+    import copy
+    sub = copy.copy(rec)
+    sub.n_walk = w1 - w0
+    for k in ("n_epi", "n_epj", "n_spj", "p_epi", "p_force", "p_id_epj", "p_id_spj"):
+        setattr(sub, k, np.ascontiguousarray(getattr(rec, k)[w0:w1]))
+    sub.walk_rcut2 = None if rec.walk_rcut2 is None else rec.walk_rcut2[w0:w1]
+    return sub
 
 
 def _time_tag(tag: int, stream, flush, reps: int = 3) -> float:
@@ -734,6 +800,9 @@ def run_kdk_graph(n: int = 4194304, steps: int = 100, dt: float = 1.0 / 1024) ->
     rng = np.random.default_rng(11)
     sample = np.sort(rng.choice(n, 4096, replace=False))
     with nbody.DeviceNBody(clk) as h:
+        # n_group_limit autotuner (tree + lists + force per evaluation), then
+        # the kernel variant for the chosen lists.
+        groups = h.autotune_groups((256, 512, 1024, 2048), repeats=2)
         variant, _ = h.autotune(2)
         # Accuracy run: every step records a random 4096-particle sample, mixed
         # precision against an FP64 evaluation over the same lists.
@@ -759,7 +828,8 @@ def run_kdk_graph(n: int = 4194304, steps: int = 100, dt: float = 1.0 / 1024) ->
                          float(np.quantile(ep, 0.999)), int((r["n_ngb"] != r["n_ngb64"]).sum())))
     ps = np.array(per_step)
     return {"config": {"model": "King W0=7", "n": n, "theta": 0.4, "r_out": 0.0015, "dt": dt,
-                       "n_leaf_limit": clk.n_leaf_limit, "n_group_limit": clk.n_group_limit},
+                       "n_leaf_limit": clk.n_leaf_limit, "n_group_limit": groups["best_n_group_limit"]},
+            "group_limit_autotune": groups,
             "steps_per_graph": steps, "ms_per_step": ms / steps, "value": inter / (ms * 1e-3) / 1e9,
             "unit": "Ginteractions/s over whole steps (tree, lists, force, kicks, drifts)",
             "tree_ms": st0["last_tree_ms"], "force_ms": st0["last_force_ms"],
@@ -783,7 +853,6 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="plummer1m_bin50")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-modes", action="store_true", help="skip the search and changeover mode timings")

@@ -202,11 +202,44 @@ int pgf_set_dispatch_stages(int stages);
  * All modes; no counterpart in the reference. */
 int pgf_set_walk_split(int enable);
 
+/* Host-direct data movement (1, the default, or 0 = off).  On GB300 the GPU
+ * reads ordinary (pageable) host memory coherently through the host page
+ * tables over NVLink-C2C.  When the device reports that
+ * (cudaDevAttrPageableMemoryAccess), the send phase and single-launch walk
+ * dispatches read the caller's records and id lists in place with a gather
+ * kernel, and retrieve writes results into the caller's Force records with a
+ * scatter kernel, instead of packing on the host into pinned staging and
+ * copying.  The device arrays, and so the results, are bit-identical either
+ * way; ids are still checked before any force kernel runs.  The caller's
+ * arrays must stay valid and unchanged for the duration of each call, as the
+ * reference requires.  No counterpart in the reference, whose host code
+ * packs on the CPU (src/force_gpu_cuda.cu:577-699, 866-875). */
+int pgf_set_host_direct(int enable);
+/* *active = 1 when later calls move data host-direct (enabled and supported). */
+int pgf_get_host_direct(int *active);
+
 /* Autotuner: times every kernel variant `repeats` times on the data of the
  * tag's last index dispatch (already on the device), keeps the fastest for
  * later dispatches and reports it and its mean main-kernel time.  The results
  * of the tag are those of the last variant run; retrieve after a recompute. */
 int pgf_autotune(int tag, int repeats, int *best_variant, double *best_ms);
+
+/* Autotuner for the dispatch itself: runs the caller's walk dispatch and
+ * retrieve (the arguments of pgf_dispatch_index's walk phase and of
+ * pgf_retrieve; the j arrays must have been sent) for each candidate, best of
+ * `repeats` timed runs after a warm-up, and keeps the fastest for later
+ * dispatches.  Candidates: pipeline stage counts 1, 2, 4 and 8 (how many
+ * launches a dispatch is cut into, each overlapping the next stage's packing
+ * and copies), and for single launches the walk-split unit (an eighth of one
+ * SM's even share by default; 4, 16 and 32 also tried).  The force records
+ * hold the last run's results.  The reference fixes its walks per launch at
+ * compile time (N_WALK_LIMIT, src/force_gpu_cuda.cu:12-17) and PeTar its
+ * n_walk_limit (src/petar.hpp:888). */
+int pgf_autotune_dispatch(int tag, int n_walk, const void *const *epi, const int *n_epi,
+                          const pgf_epi_layout *epi_layout, const int *const *id_epj, const int *n_epj,
+                          const int *const *id_spj, const int *n_spj, void *const *force,
+                          const pgf_force_layout *force_layout, int repeats, int *best_stages, int *best_split,
+                          double *best_ms);
 
 /* Launch on the caller's CUDA stream (a cudaStream_t passed as void*);
  * NULL restores the library's own stream. */
@@ -399,6 +432,21 @@ int pgf_nbody_export_lists(pgf_nbody *h, int64_t *order, int64_t *group_begin, i
                            double *cell_pos, double *cell_quad, int32_t *cell_level);
 /* Times every available variant on the resident lists and keeps the fastest. */
 int pgf_nbody_autotune(pgf_nbody *h, int repeats, int *best_variant, double *best_ms);
+/* Changes n_group_limit (the largest i-group) and rebuilds the tree and lists
+ * at the current positions, then evaluates the forces.  Larger groups share
+ * one interaction list among more i-particles (fewer, longer walks and more
+ * interactions per particle), as FDPS's n_group_limit does; PeTar picks it per
+ * instruction set (1024 with AVX-512, 512 with AVX2, src/petar.hpp:155-159).
+ * The lists, and so the result, depend on it. */
+int pgf_nbody_set_group_limit(pgf_nbody *h, int n_group_limit);
+/* Autotuner over n_group_limit: for each candidate (NULL / 0 candidates:
+ * 256, 512, 1024, 2048) it rebuilds the lists, picks the kernel variant
+ * (mixed precision), and times tree + lists + force of one evaluation
+ * (`repeats` timed runs); step_ms[c] and interactions[c] (optional, n_limits
+ * each) receive the time and the EP-EP + EP-SP interactions per evaluation.
+ * Keeps the fastest candidate and its variant, and reports them. */
+int pgf_nbody_autotune_groups(pgf_nbody *h, const int *limits, int n_limits, int repeats, double *step_ms,
+                              int64_t *interactions, int *best_limit, int *best_variant, double *best_ms);
 /* Per-step sample: after every force evaluation (pgf_nbody_force and each
  * step of pgf_nbody_run, graphs included) the n_sample given particles get a
  * record with the mixed-precision result and an FP64 evaluation over the same

@@ -33,6 +33,76 @@ def build(force: bool = False) -> Path:
     return out
 
 
+REF_DIR = HERE / "_ref"
+
+
+def build_ref_gpu_driver(force: bool = False) -> Path | None:
+    """Compiles ref/ref_gpu_driver.cu (this project's host driver for the
+    reference's own CUDA kernels) into _ref/libref_gpu_driver.so; None without
+    nvcc."""
+    import shutil
+    nvcc = os.environ.get("NVCC") or shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(nvcc).exists():
+        return None
+    REF_DIR.mkdir(exist_ok=True)
+    out = REF_DIR / "libref_gpu_driver.so"
+    src = HERE / "ref" / "ref_gpu_driver.cu"
+    if force or not out.exists() or out.stat().st_mtime < src.stat().st_mtime:
+        tmp = out.with_suffix(".so.tmp")
+        subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "-Xcompiler",
+                        "-fPIC", "-shared", str(src), "-o", str(tmp), "-lcuda"], check=True)
+        os.replace(tmp, out)
+    return out
+
+
+_REF_GPU = None
+
+
+class ReferenceKernelUnavailable(RuntimeError):
+    pass
+
+
+def ref_gpu(batch, repeats: int = 0) -> dict:
+    """The reference's own CUDA kernels (force_kernel_ep_ep + force_kernel_ep_sp
+    of src/force_gpu_cuda.cu, from _ref/ref_force_gpu.cubin) on a WalkBatch:
+    acc, pot and nnb as its retrieve writes them (FP32 widened to FP64), and
+    ms, the mean time of `repeats` re-runs of the two kernels."""
+    global _REF_GPU
+    cubin = REF_DIR / "ref_force_gpu.cubin"
+    if not cubin.exists():
+        raise ReferenceKernelUnavailable("the reference's kernels were not compiled (no reference sources here)")
+    if _REF_GPU is None:
+        lib = ctypes.CDLL(str(build_ref_gpu_driver()))
+        vp = ctypes.c_void_p
+        lib.ref_gpu_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t]
+        lib.ref_gpu_load.restype = ctypes.c_int
+        lib.ref_gpu_force.argtypes = ([ctypes.c_int] + [vp] * 7 + [ctypes.c_int64] + [vp] * 3 + [ctypes.c_int64]
+                                      + [vp] * 3 + [ctypes.c_double] * 3 + [ctypes.c_int] + [vp] * 4
+                                      + [ctypes.c_char_p, ctypes.c_size_t])
+        lib.ref_gpu_force.restype = ctypes.c_int
+        msg = ctypes.create_string_buffer(256)
+        if lib.ref_gpu_load(str(cubin).encode(), msg, len(msg)) != 0:
+            raise ReferenceKernelUnavailable(msg.value.decode())
+        _REF_GPU = lib
+    a = [_c(batch.epi_disp, np.int64), _c(batch.epi_pos, np.float64), _c(batch.epi_rs, np.float64),
+         _c(batch.epj_disp, np.int64), _c(batch.id_epj, np.int32), _c(batch.spj_disp, np.int64),
+         _c(batch.id_spj, np.int32)]
+    j = [_c(batch.epj_pos, np.float64), _c(batch.epj_mass, np.float64), _c(batch.epj_rs, np.float64)]
+    sp = [_c(batch.spj_pos, np.float64), _c(batch.spj_mass, np.float64), _c(batch.spj_quad, np.float64)]
+    ni = batch.epi_rs.size
+    out = dict(acc=np.zeros((ni, 3)), pot=np.zeros(ni), nnb=np.zeros(ni, np.int64))
+    ms = ctypes.c_double(0.0)
+    msg = ctypes.create_string_buffer(256)
+    rc = _REF_GPU.ref_gpu_force(batch.n_walk, *[_p(x) for x in a], batch.epj_mass.size, *[_p(x) for x in j],
+                                batch.spj_mass.size, *[_p(x) for x in sp], float(batch.eps2), float(batch.rcut2),
+                                float(batch.G), int(repeats), _p(out["acc"]), _p(out["pot"]), _p(out["nnb"]),
+                                ctypes.byref(ms), msg, len(msg))
+    if rc != 0:
+        raise RuntimeError(f"reference kernels: {msg.value.decode()} ({rc})")
+    out["ms"] = ms.value
+    return out
+
+
 def _lib():
     global _LIB
     if _LIB is None:

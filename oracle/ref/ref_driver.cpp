@@ -7,6 +7,8 @@
 //                over PhantomGrapeQuad (FP32) or, with CALC_EP_64bit /
 //                CALC_SP_64bit, PhantomGrapeQuad64Bit.
 // Each call evaluates one i-set against one j-set, as one FDPS walk would.
+#include <vector>
+
 #include "ref_shim.hpp"
 #include "soft_force.hpp"
 
@@ -163,5 +165,66 @@ void ref_correct(int ni, const double* xi, const double* ai, int nj, const doubl
     delete[] f;
 }
 #endif
+
+// Every walk of a multi-walk batch, OpenMP over walks with a dynamic schedule
+// and buffers per thread, the way PeTar's tree walk calls its CPU functors
+// (src/soft_force.hpp:365-373): the walk's EPJ and SPJ gathered from the
+// shared arrays by its id lists (FDPS's interaction list), then EP-EP and
+// EP-SP into one cleared Force per i.  For timing the reference CPU path over
+// the same lists as the GPU kernels.
+void ref_force_walks(int n_walk, const long long* epi_disp, const double* epi_pos, const double* epi_rs,
+                     const long long* epj_disp, const int* id_epj, const long long* spj_disp, const int* id_spj,
+                     const double* epj_pos, const double* epj_mass, const double* epj_rs, const double* spj_pos,
+                     const double* spj_mass, const double* spj_quad, double* acc, double* pot, long long* nnb) {
+#pragma omp parallel
+    {
+        std::vector<EPISoft> epi;
+        std::vector<EPJSoft> epj;
+        std::vector<SPJSoft> spj;
+        std::vector<ForceSoft> f;
+#pragma omp for schedule(dynamic, 1)
+        for (int w = 0; w < n_walk; ++w) {
+            const long long i0 = epi_disp[w], ni = epi_disp[w + 1] - i0;
+            const long long e0 = epj_disp[w], ne = epj_disp[w + 1] - e0;
+            const long long s0 = spj_disp[w], ns = spj_disp[w + 1] - s0;
+            epi.resize(ni > 0 ? ni : 1);
+            epj.resize(ne > 0 ? ne : 1);
+            spj.resize(ns > 0 ? ns : 1);
+            f.resize(ni > 0 ? ni : 1);
+            load_i((int)ni, epi_pos + 3 * i0, epi_rs + i0, epi.data());
+            for (long long j = 0; j < ne; ++j) {
+                const int k = id_epj[e0 + j];
+                epj[j].id = k;
+                epj[j].mass = epj_mass[k];
+                epj[j].pos = PS::F64vec(epj_pos[3 * k], epj_pos[3 * k + 1], epj_pos[3 * k + 2]);
+                epj[j].r_search = epj_rs[k];
+            }
+            for (long long j = 0; j < ns; ++j) {
+                const int k = id_spj[s0 + j];
+                spj[j].mass = spj_mass[k];
+                spj[j].pos = PS::F64vec(spj_pos[3 * k], spj_pos[3 * k + 1], spj_pos[3 * k + 2]);
+                const double* q = spj_quad + 6 * k;
+                spj[j].quad.xx = q[0];
+                spj[j].quad.yy = q[1];
+                spj[j].quad.zz = q[2];
+                spj[j].quad.xy = q[3];
+                spj[j].quad.xz = q[4];
+                spj[j].quad.yz = q[5];
+            }
+            for (long long i = 0; i < ni; ++i) f[i].clear();
+            if (ni > 0) {
+                EpEp()(epi.data(), (int)ni, epj.data(), (int)ne, f.data());
+                if (ns > 0) EpSp()(epi.data(), (int)ni, spj.data(), (int)ns, f.data());
+            }
+            for (long long i = 0; i < ni; ++i) {
+                acc[3 * (i0 + i)] = f[i].acc.x;
+                acc[3 * (i0 + i) + 1] = f[i].acc.y;
+                acc[3 * (i0 + i) + 2] = f[i].acc.z;
+                pot[i0 + i] = f[i].pot;
+                nnb[i0 + i] = f[i].n_ngb;
+            }
+        }
+    }
+}
 
 }  // extern "C"

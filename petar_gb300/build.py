@@ -59,6 +59,7 @@ GPU_SOURCES = [
     "gpuforce/pgf_kernels_mixed.cu",
     "gpuforce/pgf_kernels_ws.cu",
     "gpuforce/pgf_noalloc.cu",
+    "gpuforce/pgf_hostdirect.cu",
     "gpuforce/pgf_kernels_gradient.cu",
     "gpuforce/pgf_nbody.cu",
 ]
@@ -83,8 +84,11 @@ def build_gpuforce(force: bool = False, verbose: bool = False) -> Path:
     nvcc = _nvcc()
     objdir = LIB / "obj"
     objdir.mkdir(exist_ok=True)
+    # Host code without FP contraction: the host packing and the host-direct
+    # gather kernels must round every FP64 operation the same way.
     common = [nvcc, *ARCH_FLAGS, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-fopenmp", "-I", str(INCLUDE), "-I", str(CSRC / "gpuforce")]
+              "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off", "-I", str(INCLUDE),
+              "-I", str(CSRC / "gpuforce")]
     if verbose:
         common += ["-Xptxas", "-v"]
 

@@ -143,6 +143,13 @@ struct TagState {
     int n_split = 0;
     DevBuf<SplitRec> splits;
     HostBuf<SplitRec> h_splits;
+    // Host-direct tables: where the gather kernel reads each walk, and where
+    // the scatter kernel writes its results.
+    HostBuf<WalkSrc> h_src;
+    DevBuf<WalkSrc> src;
+    HostBuf<ForceDst> h_dst;
+    DevBuf<ForceDst> dst;
+    HostBuf<int32_t> h_hd_err;
 };
 
 struct State {
@@ -160,6 +167,12 @@ struct State {
     int variant = PGF_DEFAULT_KERNEL_VARIANT;  // mixed-precision kernel variant (pgf_set_kernel_variant)
     int stages = 0;   // dispatch pipeline stages (pgf_set_dispatch_stages); 0 = by size
     bool walk_split = true;  // split the largest walks of small dispatches (pgf_set_walk_split)
+    int split_div = 8;       // split unit: 1/split_div of one SM's even share (pgf_autotune_dispatch)
+    // Host-direct data movement (pgf_set_host_direct): the device reads the
+    // caller's records in place and writes results into them; used when the
+    // device can access pageable host memory.
+    bool hd_supported = false;
+    bool hd_enabled = true;
     int mode = PGF_MODE_FORCE;
     // shared j data
     DevBuf<EpjMix> epj;
@@ -209,6 +222,9 @@ int ensure_init() {
     return PGF_OK;
 }
 
+// Whether this call moves data host-direct (supported and not turned off).
+bool use_hd() { return g.hd_supported && g.hd_enabled; }
+
 int setup_device(int rank) {
     int ngpu = 0;
     cudaError_t e = cudaGetDeviceCount(&ngpu);
@@ -220,6 +236,9 @@ int setup_device(int rank) {
     g.device = (rank < 0 ? -rank : rank) % ngpu;
     PGF_CUDA(cudaSetDevice(g.device));
     PGF_CUDA(cudaDeviceGetAttribute(&g.num_sms, cudaDevAttrMultiProcessorCount, g.device));
+    int pageable = 0;
+    PGF_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, g.device));
+    g.hd_supported = pageable != 0;
     PGF_CUDA(cudaStreamCreateWithFlags(&g.own_stream, cudaStreamNonBlocking));
     PGF_CUDA(cudaStreamCreateWithFlags(&g.copy_stream, cudaStreamNonBlocking));
     for (auto& st : g.stage_stream) PGF_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
@@ -322,6 +341,77 @@ void harvest_send(bool wait = false) {
     g.send_pending = false;
 }
 
+// The send phase host-direct: one kernel reads the caller's EPJ / SPJ records
+// in place and writes every device form of them (the host packing's
+// arithmetic), then the call waits for it, since the caller's arrays are only
+// valid during the call.
+int send_j_host_direct(const void* epj, int64_t n_epj, const pgf_epj_layout* el, const void* spj, int64_t n_spj,
+                       const pgf_spj_layout* sl) {
+    PGF_CUDA(g.epj.ensure(n_epj));
+    PGF_CUDA(g.epj_m64.ensure(n_epj));
+    PGF_CUDA(g.epj_rs64.ensure(n_epj));
+    PGF_CUDA(g.spj.ensure(n_spj));
+    PGF_CUDA(g.spj_q64.ensure(n_spj));
+    PGF_CUDA(g.epj32.ensure(n_epj));
+    PGF_CUDA(g.spj32.ensure(n_spj));
+    const bool co = g.co_set && n_epj > 0, gr = g.gr_set && n_epj > 0;
+    if (co) PGF_CUDA(g.epj_co.ensure(n_epj));
+    if (gr) PGF_CUDA(g.epj_acc32.ensure(n_epj));
+    HdSendArgs a{};
+    a.epj = static_cast<const char*>(epj);
+    a.n_epj = n_epj;
+    if (n_epj > 0) {
+        a.epj_size = el->size;
+        a.epj_off_mass = el->off_mass;
+        a.epj_off_pos = el->off_pos;
+        a.epj_off_rs = el->off_r_search;
+    }
+    a.spj = static_cast<const char*>(spj);
+    a.n_spj = n_spj;
+    if (n_spj > 0) {
+        a.spj_size = sl->size;
+        a.spj_off_mass = sl->off_mass;
+        a.spj_off_pos = sl->off_pos;
+        a.spj_off_quad = sl->off_quad;
+        a.spj_has_quad = sl->has_quad;
+    }
+    if (co) {
+        a.co_epj_off_id = g.co.epj_off_id;
+        a.co_epj_off_r_in = g.co.epj_off_r_in;
+        a.co_epj_off_r_out = g.co.epj_off_r_out;
+        a.co_epj_off_mass_backup = g.co.epj_off_mass_backup;
+        a.co_epj_off_status = g.co.epj_off_status;
+        a.out_epj_co = g.epj_co.d;
+    }
+    if (gr) {
+        a.gr_epj_off_acc = g.gr.epj_off_acc;
+        a.out_epj_acc32 = g.epj_acc32.d;
+    }
+    a.out_epj = g.epj.d;
+    a.out_epj_m64 = g.epj_m64.d;
+    a.out_epj_rs64 = g.epj_rs64.d;
+    a.out_epj32 = g.epj32.d;
+    a.out_spj = g.spj.d;
+    a.out_spj_q64 = g.spj_q64.d;
+    a.out_spj32 = g.spj32.d;
+    PGF_CUDA(cudaEventRecord(g.ev_send0, g.stream));
+    {
+        const cudaError_t e = launch_gather_j(a, g.num_sms, g.stream);
+        if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "j gather kernel failed: %s", cudaGetErrorString(e));
+    }
+    PGF_CUDA(cudaEventRecord(g.ev_send1, g.stream));
+    g.j_co_sent = co;
+    g.j_gr_sent = gr;
+    if (int r = encode_tensor_maps(n_epj, n_spj)) return r;
+    PGF_CUDA(cudaEventSynchronize(g.ev_send1));
+    g.send_pending = true;
+    harvest_send();
+    g.n_epj_tot = n_epj;
+    g.n_spj_tot = n_spj;
+    g.j_sent = true;
+    return PGF_OK;
+}
+
 // Packs the shared EPJ / SPJ arrays (the send_flag phase,
 // src/force_gpu_cuda.cu:577-619).
 int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, const void* spj,
@@ -334,6 +424,7 @@ int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, co
     // either is reused or reallocated.
     PGF_CUDA(cudaStreamSynchronize(g.stream));
     harvest_send();
+    if (use_hd()) return send_j_host_direct(epj, n_epj, el, spj, n_spj, sl);
     const double t0 = now_s();
     PGF_CUDA(g.h_epj.ensure(n_epj));
     PGF_CUDA(g.h_epj_m64.ensure(n_epj));
@@ -640,6 +731,128 @@ bool pack_walk(TagState& t, int k, int w, const Slot3& o, const void* const* epi
     return bad == 0;
 }
 
+// A walk of a single-launch dispatch that runs as several parts.
+struct SplitPlan {
+    int k, parts;
+    int64_t rows1;  // first EPI row of part 1
+    int desc1;      // layout position of part 1's descriptor
+};
+
+// Cost of list slice j of `parts` of a walk (the work-queue order of walks
+// and parts): n_i (n_epj + 2 n_spj) of the slice.
+inline double part_cost(int n_i, int n_epj, int n_spj, int j, int parts) {
+    const int e = (int)((int64_t)n_epj * (j + 1) / parts) - (int)((int64_t)n_epj * j / parts);
+    const int s = (int)((int64_t)n_spj * (j + 1) / parts) - (int)((int64_t)n_spj * j / parts);
+    return (double)n_i * ((double)e + 2.0 * (double)s);
+}
+
+// The walk phase of a single-launch index dispatch, host-direct: the host
+// writes one table entry per walk (where its EPI records and id lists lie,
+// where they go, how it splits), and a gather kernel reads the caller's
+// arrays in place, builds the EPI rows, the walk descriptors and the id
+// lists, and checks every id against the sent arrays.  The call waits for
+// the gather (the caller's arrays are only valid during the call) and reports
+// an out-of-range id before any force kernel is launched.
+int dispatch_host_direct(TagState& t, int n_walk, const std::vector<int32_t>& ord, const std::vector<Slot3>& off,
+                         const std::vector<SplitPlan>& plan, int n_desc, const void* const* epi, const int* n_epi,
+                         const pgf_epi_layout* il, const int* const* id_epj, const int* n_epj,
+                         const int* const* id_spj, const int* n_spj, bool co_mode, bool gr_mode, double t0) {
+    PGF_CUDA(t.h_src.ensure(n_walk));
+    PGF_CUDA(t.src.ensure(n_walk));
+    PGF_CUDA(t.h_hd_err.ensure(2));
+    std::vector<int> plan_of(n_walk, -1);
+    for (size_t q = 0; q < plan.size(); ++q) plan_of[plan[q].k] = (int)q;
+    std::vector<std::pair<double, int>> cq(n_desc);
+    for (int k = 0; k < n_walk; ++k) {
+        const int w = ord[k];
+        WalkSrc ws;
+        ws.epi = static_cast<const char*>(epi[w]);
+        ws.id_epj = n_epj[w] ? id_epj[w] : nullptr;
+        ws.id_spj = n_spj[w] ? id_spj[w] : nullptr;
+        ws.i_off = off[k].i;
+        ws.e_off = off[k].e;
+        ws.s_off = off[k].s;
+        ws.rcut2 = g.walk_rcut2.empty() ? g.rcut2 : g.walk_rcut2[w];
+        ws.n_i = n_epi[w];
+        ws.n_epj = n_epj[w];
+        ws.n_spj = n_spj[w];
+        ws.walk = w;
+        ws.parts = 1;
+        ws.desc1 = 0;
+        ws.rows1 = 0;
+        if (plan_of[k] >= 0) {
+            const SplitPlan& sp = plan[plan_of[k]];
+            ws.parts = sp.parts;
+            ws.desc1 = sp.desc1;
+            ws.rows1 = sp.rows1;
+            for (int j = 1; j < sp.parts; ++j)
+                cq[sp.desc1 + j - 1] = {part_cost(n_epi[w], n_epj[w], n_spj[w], j, sp.parts), sp.desc1 + j - 1};
+        }
+        cq[k] = {part_cost(n_epi[w], n_epj[w], n_spj[w], 0, ws.parts), k};
+        t.h_src.h[k] = ws;
+    }
+    if (plan.empty()) {
+        for (int k = 0; k < n_desc; ++k) t.h_order.h[k] = k;
+    } else {
+        std::stable_sort(cq.begin(), cq.end(), [](const std::pair<double, int>& a, const std::pair<double, int>& b) {
+            return a.first > b.first;
+        });
+        for (int k = 0; k < n_desc; ++k) t.h_order.h[k] = cq[k].second;
+        PGF_CUDA(t.h_splits.ensure(plan.size()));
+        PGF_CUDA(t.splits.ensure(plan.size()));
+        for (size_t q = 0; q < plan.size(); ++q) {
+            const SplitPlan& sp = plan[q];
+            t.h_splits.h[q] = SplitRec{(int32_t)off[sp.k].i, (int32_t)sp.rows1, n_epi[ord[sp.k]], sp.parts};
+        }
+    }
+    HdWalkArgs a{};
+    a.src = t.src.d;
+    a.n_walk = n_walk;
+    a.epi_size = il->size;
+    a.epi_off_pos = il->off_pos;
+    a.epi_off_rs = il->off_r_search;
+    if (gr_mode) {
+        a.gr_epi_off_acc = g.gr.epi_off_acc;
+        a.out_epi_acc = t.epi_acc.d;
+    }
+    if (co_mode) {
+        a.co_epi_off_id = g.co.epi_off_id;
+        a.co_epi_off_r_in = g.co.epi_off_r_in;
+        a.co_epi_off_r_out = g.co.epi_off_r_out;
+        a.co_epi_off_self_mass = g.co.epi_off_self_mass;
+        a.out_epi_co = t.epi_co.d;
+    }
+    a.n_epj_tot = g.n_epj_tot;
+    a.n_spj_tot = g.n_spj_tot;
+    a.out_epi = t.epi.d;
+    a.out_id_epj = t.id_epj.d;
+    a.out_id_spj = t.id_spj.d;
+    a.out_walks = t.walks.d;
+    a.err = g.scratch.d + 4;
+    g.prof.copy += now_s() - t0;
+    PGF_CUDA(cudaEventRecord(t.ev[0], g.stream));
+    PGF_CUDA(cudaMemsetAsync(a.err, 0, 2 * sizeof(int32_t), g.stream));
+    PGF_CUDA(cudaMemcpyAsync(t.src.d, t.h_src.h, n_walk * sizeof(WalkSrc), cudaMemcpyHostToDevice, g.stream));
+    {
+        const cudaError_t e = launch_gather_walks(a, g.num_sms, g.stream);
+        if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "walk gather kernel failed: %s", cudaGetErrorString(e));
+    }
+    PGF_CUDA(cudaMemcpyAsync(t.h_hd_err.h, a.err, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, g.stream));
+    PGF_CUDA(cudaStreamSynchronize(g.stream));
+    if (t.h_hd_err.h[0] != 0)
+        return fail(PGF_ERR_ARG, "walk %d has an EPJ/SPJ id outside the sent arrays", t.h_hd_err.h[1]);
+    PGF_CUDA(cudaMemcpyAsync(t.order.d, t.h_order.h, n_desc * sizeof(int32_t), cudaMemcpyHostToDevice, g.stream));
+    if (!plan.empty()) {
+        PGF_CUDA(cudaMemcpyAsync(t.splits.d, t.h_splits.h, plan.size() * sizeof(SplitRec), cudaMemcpyHostToDevice,
+                                 g.stream));
+        const cudaError_t e = launch_split_rows(t.splits.d, (int)plan.size(), t.epi.d, co_mode ? t.epi_co.d : nullptr,
+                                                gr_mode ? t.epi_acc.d : nullptr, g.stream);
+        if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "split rows kernel failed: %s", cudaGetErrorString(e));
+        t.n_split = (int)plan.size();
+    }
+    return launch_tag(t);
+}
+
 // Packs the walks of one index dispatch (src/force_gpu_cuda.cu:621-699) and
 // launches the kernels.  Walks are laid out in descending cost (EP-SP pairs
 // weighted by their larger instruction count), so the work queue is the
@@ -707,18 +920,13 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     // On 200-walk batches of the 1M binary Plummer workload an eighth runs
     // the kernels 24% faster than parts of a quarter share split only above
     // two units.
-    struct SplitPlan {
-        int k, parts;
-        int64_t rows1;  // first EPI row of part 1
-        int desc1;      // layout position of part 1's descriptor
-    };
     std::vector<SplitPlan> plan;
     int64_t ni_all = ni;
     int n_desc = n_walk;
     if (n_chunks == 1 && g.walk_split && n_walk > 0) {
         double total = 0.0;
         for (int k = 0; k < n_walk; ++k) total += cost(ord[k]);
-        const double target = total / (8.0 * (double)g.num_sms);
+        const double target = total / ((double)g.split_div * (double)g.num_sms);
         for (int k = 0; k < n_walk; ++k) {
             const int w = ord[k];
             const double c = cost(w);
@@ -738,20 +946,23 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     }
     t.n_split = 0;
     if (gr_mode) {
-        PGF_CUDA(t.h_epi_acc.ensure(ni));
+        if (!(n_chunks == 1 && use_hd())) PGF_CUDA(t.h_epi_acc.ensure(ni));
         PGF_CUDA(t.epi_acc.ensure(ni_all));
         PGF_CUDA(t.acorr.ensure(ni_all));
     }
     if (co_mode) {
-        PGF_CUDA(t.h_epi_co.ensure(ni));
+        if (!(n_chunks == 1 && use_hd())) PGF_CUDA(t.h_epi_co.ensure(ni));
         PGF_CUDA(t.epi_co.ensure(ni_all));
         PGF_CUDA(t.pot_soft.ensure(ni_all));
     }
 
-    PGF_CUDA(t.h_epi.ensure(ni));
-    PGF_CUDA(t.h_id_epj.ensure(ne));
-    PGF_CUDA(t.h_id_spj.ensure(ns));
-    PGF_CUDA(t.h_walks.ensure(n_desc));
+    const bool hd_single = n_chunks == 1 && use_hd();
+    if (!hd_single) {  // pinned staging of the host packing
+        PGF_CUDA(t.h_epi.ensure(ni));
+        PGF_CUDA(t.h_id_epj.ensure(ne));
+        PGF_CUDA(t.h_id_spj.ensure(ns));
+        PGF_CUDA(t.h_walks.ensure(n_desc));
+    }
     PGF_CUDA(t.h_order.ensure(n_desc));
     PGF_CUDA(t.epi.ensure(ni_all));
     PGF_CUDA(t.id_epj.ensure(ne));
@@ -848,7 +1059,13 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
         return PGF_OK;
     };
 
+    if (n_chunks == 1 && use_hd()) {
+        t.ord = ord;
+        return dispatch_host_direct(t, n_walk, ord, off, plan, n_desc, epi, n_epi, il, id_epj, n_epj, id_spj, n_spj,
+                                    co_mode, gr_mode, t0);
+    }
     if (n_chunks == 1) {
+        t.ord = ord;
         const int bad_walk = pack_range(0, n_walk);
         if (bad_walk >= 0) {
             g.prof.copy += now_s() - t0;
@@ -1127,6 +1344,17 @@ int pgf_set_changeover_layout(const pgf_changeover_layout* layout) {
     return PGF_OK;
 }
 
+int pgf_set_host_direct(int enable) {
+    g.hd_enabled = enable != 0;
+    return PGF_OK;
+}
+
+int pgf_get_host_direct(int* active) {
+    if (!active) return fail(PGF_ERR_ARG, "NULL argument");
+    *active = use_hd() ? 1 : 0;
+    return PGF_OK;
+}
+
 int pgf_set_walk_split(int enable) {
     g.walk_split = enable != 0;
     return PGF_OK;
@@ -1180,6 +1408,52 @@ int pgf_autotune(int tag, int repeats, int* best_variant, double* best_ms) {
     return PGF_OK;
 }
 
+int pgf_autotune_dispatch(int tag, int n_walk, const void* const* epi, const int* n_epi,
+                          const pgf_epi_layout* epi_layout, const int* const* id_epj, const int* n_epj,
+                          const int* const* id_spj, const int* n_spj, void* const* force,
+                          const pgf_force_layout* force_layout, int repeats, int* best_stages, int* best_split,
+                          double* best_ms) {
+    if (int r = ensure_init()) return r;
+    if (!valid_tag(tag)) return fail(PGF_ERR_ARG, "tag %d outside [0, %d)", tag, kMaxTags);
+    if (repeats < 1) repeats = 1;
+    const int saved_stages = g.stages, saved_div = g.split_div;
+    struct Cand {
+        int stages, div;
+    };
+    std::vector<Cand> cands;
+    for (int st : {1, 2, 4, 8}) cands.push_back({st, g.split_div});
+    for (int dv : {4, 16, 32}) cands.push_back({1, dv});
+    double best_t = HUGE_VAL;
+    Cand best{saved_stages, saved_div};
+    for (const Cand& c : cands) {
+        g.stages = c.stages;
+        g.split_div = c.div;
+        double t_min = HUGE_VAL;
+        for (int k = 0; k <= repeats; ++k) {  // the first run warms up
+            const double t0 = now_s();
+            int r = pgf_dispatch_index(tag, n_walk, epi, n_epi, epi_layout, id_epj, n_epj, id_spj, n_spj, nullptr, 0,
+                                       nullptr, nullptr, 0, nullptr, 0);
+            if (r == PGF_OK) r = pgf_retrieve(tag, n_walk, n_epi, force, force_layout);
+            if (r != PGF_OK) {
+                g.stages = saved_stages;
+                g.split_div = saved_div;
+                return r;
+            }
+            if (k > 0) t_min = std::min(t_min, now_s() - t0);
+        }
+        if (t_min < best_t) {
+            best_t = t_min;
+            best = c;
+        }
+    }
+    g.stages = best.stages;
+    g.split_div = best.div;
+    if (best_stages) *best_stages = best.stages;
+    if (best_split) *best_split = best.div;
+    if (best_ms) *best_ms = 1e3 * best_t;
+    return PGF_OK;
+}
+
 // Writes the results of walk w into the caller's records.
 void unpack_walk(const TagState& t, int w, const int* ni, void* const* force, const pgf_force_layout* fl) {
     char* base = reinterpret_cast<char*>(force[w]);
@@ -1224,6 +1498,70 @@ int copy_back(TagState& t, int64_t r0, int64_t r1, cudaStream_t s) {
     return PGF_OK;
 }
 
+// Retrieve host-direct: a scatter kernel writes each walk's results into the
+// caller's Force records (in walk layout order, stage by stage for a
+// pipelined dispatch), so nothing is copied back or unpacked on the host.
+int retrieve_host_direct(TagState& t, int n_walk, const int* ni, void* const* force, const pgf_force_layout* fl) {
+    PGF_CUDA(t.h_dst.ensure(n_walk));
+    PGF_CUDA(t.dst.ensure(n_walk));
+    for (int k = 0; k < n_walk; ++k) {
+        const int w = t.ord[k];
+        t.h_dst.h[k] = ForceDst{static_cast<char*>(force[w]), t.epi_disp[w], ni[w], 0};
+    }
+    HdScatterArgs a{};
+    a.counts_only = t.mode == PGF_MODE_NEIGHBOR_SEARCH;
+    a.size = fl->size;
+    a.off_acc = fl->off_acc;
+    a.off_pot = fl->off_pot;
+    a.off_nnb = fl->off_n_ngb;
+    a.nnb_bytes = fl->n_ngb_bytes;
+    a.accp = t.accp.d;
+    a.nnb = t.nnb.d;
+    if (t.mode == PGF_MODE_FORCE_CHANGEOVER) {
+        a.pot_soft = t.pot_soft.d;
+        a.off_pot_soft = g.co.force_off_pot_soft;
+    }
+    if (t.mode == PGF_MODE_GRADIENT) {
+        a.acorr = t.acorr.d;
+        a.off_acorr = g.gr.force_off_acorr;
+    }
+    auto scatter = [&](int k0, int k1, cudaStream_t st) -> int {
+        HdScatterArgs b = a;
+        b.dst = t.dst.d + k0;
+        b.n_walk = k1 - k0;
+        const cudaError_t e = launch_scatter_results(b, g.num_sms, st);
+        if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "result scatter kernel failed: %s", cudaGetErrorString(e));
+        return PGF_OK;
+    };
+    cudaStream_t st = t.n_chunks > 0 ? g.d2h_stream : g.stream;
+    PGF_CUDA(cudaMemcpyAsync(t.dst.d, t.h_dst.h, n_walk * sizeof(ForceDst), cudaMemcpyHostToDevice, st));
+    if (t.n_chunks > 0) {
+        for (int c = 0; c < t.n_chunks; ++c) {
+            PGF_CUDA(cudaStreamWaitEvent(st, t.evc[c][4], 0));
+            if (c == 0) PGF_CUDA(cudaEventRecord(t.ev[4], st));
+            if (int r = scatter(t.stage_k[c], t.stage_k[c + 1], st)) return r;
+        }
+        PGF_CUDA(cudaStreamWaitEvent(st, t.ev[3], 0));
+    } else {
+        PGF_CUDA(cudaEventRecord(t.ev[4], st));
+        if (int r = scatter(0, n_walk, st)) return r;
+    }
+    PGF_CUDA(cudaMemcpyAsync(t.h_flags.h, g.scratch.d, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    PGF_CUDA(cudaMemsetAsync(g.scratch.d + 2, 0, 2 * sizeof(int32_t), st));
+    PGF_CUDA(cudaEventRecord(t.ev[5], st));
+    if (t.n_chunks > 0) PGF_CUDA(cudaStreamWaitEvent(g.stream, t.ev[5], 0));  // later work follows the memset
+    PGF_CUDA(cudaEventSynchronize(t.ev[5]));
+    t.dispatched = false;
+    harvest_times(t);
+    harvest_send();
+    float ms_recv = 0;
+    cudaEventElapsedTime(&ms_recv, t.ev[4], t.ev[5]);
+    g.prof.recv += 1e-3 * ms_recv;
+    g.prof.n_retest += t.h_flags.h[3];
+    if (t.h_flags.h[2] != 0) return fail(PGF_ERR_DEVICE, "device error word %d", t.h_flags.h[2]);
+    return PGF_OK;
+}
+
 int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const pgf_force_layout* fl) {
     if (int r = ensure_init()) return r;
     if (!valid_tag(tag)) return fail(PGF_ERR_ARG, "tag %d outside [0, %d)", tag, kMaxTags);
@@ -1238,9 +1576,10 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
     }
     PGF_CUDA(cudaSetDevice(g.device));
     const int64_t n = t.ni_tot;
+    PGF_CUDA(t.h_flags.ensure(4));
+    if (use_hd()) return retrieve_host_direct(t, n_walk, ni, force, fl);
     PGF_CUDA(t.h_accp.ensure(n));
     PGF_CUDA(t.h_nnb.ensure(n));
-    PGF_CUDA(t.h_flags.ensure(4));
     if (t.mode == PGF_MODE_GRADIENT) PGF_CUDA(t.h_acorr.ensure(n));
     if (t.mode == PGF_MODE_FORCE_CHANGEOVER) PGF_CUDA(t.h_pot_soft.ensure(n));
     if (t.n_chunks > 0) {

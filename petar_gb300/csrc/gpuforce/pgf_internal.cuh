@@ -224,6 +224,91 @@ struct SplitRec {
     int32_t row0, rows1, n_i, n_parts;
 };
 
+// ---- Host-direct data movement (pgf_hostdirect.cu) ----
+// The GPU reads the caller's records in host memory through the host page
+// tables and writes results into them; these tables and arguments describe
+// where.
+
+// One walk of a host-direct dispatch, in layout order.
+struct WalkSrc {
+    const char* epi;        // the caller's EPI records of the walk
+    const int32_t* id_epj;  // the caller's id lists of the walk
+    const int32_t* id_spj;
+    int64_t i_off, e_off, s_off;  // first EPI row and list entries in the device arrays
+    int64_t rows1;          // split walks: first EPI row of part 1's copy
+    double rcut2;           // r_out^2 of the walk
+    int32_t n_i, n_epj, n_spj;
+    int32_t walk;           // the caller's walk index (error reports)
+    int32_t parts;          // 1, or the parts of a split walk
+    int32_t desc1;          // split walks: descriptor index of part 1
+};
+
+// Where retrieve writes walk k's results.
+struct ForceDst {
+    char* base;   // the caller's Force records of the walk
+    int64_t row;  // first result row of the walk
+    int32_t n;
+    int32_t pad;
+};
+
+struct HdSendArgs {
+    const char* epj;
+    int64_t n_epj;
+    size_t epj_size, epj_off_mass, epj_off_pos, epj_off_rs;
+    const char* spj;
+    int64_t n_spj;
+    size_t spj_size, spj_off_mass, spj_off_pos, spj_off_quad;
+    int spj_has_quad;
+    // fused changeover mode (out_epj_co non-null)
+    size_t co_epj_off_id, co_epj_off_r_in, co_epj_off_r_out, co_epj_off_mass_backup, co_epj_off_status;
+    // gradient mode (out_epj_acc32 non-null)
+    size_t gr_epj_off_acc;
+    EpjMix* out_epj;
+    double* out_epj_m64;
+    double* out_epj_rs64;
+    EpjF32* out_epj32;
+    CoRec* out_epj_co;
+    AccF32* out_epj_acc32;
+    SpjMix* out_spj;
+    SpjQ64* out_spj_q64;
+    SpjF32* out_spj32;
+};
+
+struct HdWalkArgs {
+    const WalkSrc* src;
+    int n_walk;
+    int pad;
+    size_t epi_size, epi_off_pos, epi_off_rs;
+    size_t gr_epi_off_acc;  // gradient mode (out_epi_acc non-null)
+    size_t co_epi_off_id, co_epi_off_r_in, co_epi_off_r_out, co_epi_off_self_mass;  // changeover (out_epi_co)
+    int64_t n_epj_tot, n_spj_tot;
+    EpiDev* out_epi;
+    Accp* out_epi_acc;
+    CoRec* out_epi_co;
+    int32_t* out_id_epj;
+    int32_t* out_id_spj;
+    WalkDesc* out_walks;
+    int32_t* err;  // [0] set when an id is out of range, [1] the largest such caller walk index
+};
+
+struct HdScatterArgs {
+    const ForceDst* dst;
+    int n_walk;
+    int counts_only;  // neighbour search: n_ngb only
+    size_t size, off_acc, off_pot, off_nnb;
+    int nnb_bytes;
+    int pad;
+    size_t off_pot_soft, off_acorr;
+    const Accp* accp;
+    const int32_t* nnb;
+    const double* pot_soft;  // changeover mode, else null
+    const Accp* acorr;       // gradient mode, else null
+};
+
+cudaError_t launch_gather_j(const HdSendArgs& a, int num_sms, cudaStream_t s);
+cudaError_t launch_gather_walks(const HdWalkArgs& a, int num_sms, cudaStream_t s);
+cudaError_t launch_scatter_results(const HdScatterArgs& a, int num_sms, cudaStream_t s);
+
 // Launchers (stream-ordered, asynchronous).
 cudaError_t launch_fp64(const Params& p, cudaStream_t s, int num_sms);
 cudaError_t launch_mixed(const Params& p, cudaStream_t s, int num_sms);

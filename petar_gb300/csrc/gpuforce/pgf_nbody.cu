@@ -1898,6 +1898,66 @@ int pgf_nbody_autotune(pgf_nbody* h, int repeats, int* best_variant, double* bes
     return check_errors(h);
 }
 
+int pgf_nbody_set_group_limit(pgf_nbody* h, int n_group_limit) {
+    if (!h) return nb_fail(PGF_ERR_ARG, "NULL handle");
+    if (n_group_limit < 1) return nb_fail(PGF_ERR_ARG, "n_group_limit must be >= 1");
+    NB_CUDA(cudaStreamSynchronize(h->stream));
+    h->cfg.n_group_limit = n_group_limit;
+    h->front_limit = (int)std::max<int64_t>(n_group_limit, h->n / 1024);
+    drop_graph(h);  // the captured steps build other lists now
+    if (int r = build_fit(h)) return r;
+    return pgf_nbody_force(h);
+}
+
+int pgf_nbody_autotune_groups(pgf_nbody* h, const int* limits, int n_limits, int repeats, double* step_ms,
+                              int64_t* interactions, int* best_limit, int* best_variant, double* best_ms) {
+    if (!h) return nb_fail(PGF_ERR_ARG, "NULL handle");
+    if (n_limits < 0 || (n_limits > 0 && !limits)) return nb_fail(PGF_ERR_ARG, "bad candidate list");
+    static const int kDefault[4] = {256, 512, 1024, 2048};
+    if (n_limits == 0) {
+        limits = kDefault;
+        n_limits = 4;
+    }
+    if (repeats < 1) repeats = 1;
+    int best = h->cfg.n_group_limit, best_v = h->variant;
+    double best_t = 1e300;
+    for (int c = 0; c < n_limits; ++c) {
+        if (int r = pgf_nbody_set_group_limit(h, limits[c])) return r;
+        if (h->cfg.precision == PGF_PRECISION_MIXED) {
+            if (int r = pgf_nbody_autotune(h, repeats, nullptr, nullptr)) return r;
+        }
+        // Tree, lists and force of one evaluation at the current positions.
+        NB_CUDA(enqueue_build(h));
+        NB_CUDA(enqueue_force(h));
+        NB_CUDA(cudaEventRecord(h->ev[0], h->stream));
+        for (int r = 0; r < repeats; ++r) {
+            NB_CUDA(enqueue_build(h));
+            NB_CUDA(enqueue_force(h));
+        }
+        NB_CUDA(cudaEventRecord(h->ev[1], h->stream));
+        NB_CUDA(cudaStreamSynchronize(h->stream));
+        if (int r = check_errors(h)) return r;
+        float t = 0;
+        cudaEventElapsedTime(&t, h->ev[0], h->ev[1]);
+        const double ms = t / repeats;
+        TreeHdr th;
+        if (int r = read_hdr(h, &th)) return r;
+        if (step_ms) step_ms[c] = ms;
+        if (interactions) interactions[c] = (int64_t)th.n_epep + (int64_t)th.n_epsp;
+        if (ms < best_t) {
+            best_t = ms;
+            best = limits[c];
+            best_v = h->variant;
+        }
+    }
+    if (int r = pgf_nbody_set_group_limit(h, best)) return r;
+    h->variant = best_v;
+    if (best_limit) *best_limit = best;
+    if (best_variant) *best_variant = best_v;
+    if (best_ms) *best_ms = best_t;
+    return pgf_nbody_force(h);
+}
+
 int pgf_nbody_set_sample(pgf_nbody* h, int n_sample, const int64_t* particles, int max_records) {
     if (!h) return nb_fail(PGF_ERR_ARG, "NULL handle");
     if (n_sample < 0 || max_records < 0 || (n_sample > 0 && (!particles || max_records == 0)))

@@ -157,11 +157,14 @@ def load(build: bool = True) -> ctypes.CDLL:
         "pgf_set_kernel_variant": [ci],
         "pgf_set_dispatch_stages": [ci],
         "pgf_set_walk_split": [ci],
+        "pgf_set_host_direct": [ci],
+        "pgf_get_host_direct": [vp],
         "pgf_set_mode": [ci],
         "pgf_set_changeover_layout": [vp],
         "pgf_set_gradient_layout": [vp],
         "pgf_get_kernel_variant": [vp],
         "pgf_autotune": [ci, ci, vp, vp],
+        "pgf_autotune_dispatch": [ci, ci, vp, vp, vp, vp, vp, vp, vp, vp, vp, ci, vp, vp, vp],
         "pgf_wait": [ci],
         "pgf_get_profile": [vp],
         "pgf_clear_profile": [],
@@ -236,6 +239,18 @@ def set_walk_split(enable: bool) -> None:
     """Split the most expensive walks of small single-launch dispatches over
     several CTAs (default on)."""
     _check(load().pgf_set_walk_split(1 if enable else 0))
+
+
+def set_host_direct(enable: bool) -> None:
+    """Move data host-direct where the device supports it (default on): the
+    GPU reads the caller's records in place and writes results into them."""
+    _check(load().pgf_set_host_direct(1 if enable else 0))
+
+
+def host_direct_active() -> bool:
+    v = ctypes.c_int(0)
+    _check(load().pgf_get_host_direct(ctypes.byref(v)))
+    return bool(v.value)
 
 
 def get_kernel_variant() -> int:
@@ -412,6 +427,23 @@ class Records:
                          + np.asarray(batch.spj_disp[:-1], np.uint64) * np.uint64(4)).astype(np.uint64)
         self.walk_rcut2 = batch.walk_rcut2
         self.eps2, self.rcut2, self.G = batch.eps2, batch.rcut2, batch.G
+
+
+def autotune_dispatch(rec: Records, tag: int = 0, repeats: int = 2) -> dict:
+    """Tunes the dispatch pipeline's stage count and the walk-split unit on
+    the caller's records (send first), through pgf_autotune_dispatch."""
+    send_j(rec, tag)
+    el, _, _, fl = _layouts(epi_dt=rec.epi.dtype, force_dt=rec.force.dtype)
+    st, sp, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+    set_walk_rcut2(rec.walk_rcut2)
+    try:
+        _check(load().pgf_autotune_dispatch(tag, rec.n_walk, _ptr(rec.p_epi), _ptr(rec.n_epi), ctypes.byref(el),
+                                            _ptr(rec.p_id_epj), _ptr(rec.n_epj), _ptr(rec.p_id_spj),
+                                            _ptr(rec.n_spj), _ptr(rec.p_force), ctypes.byref(fl), int(repeats),
+                                            ctypes.byref(st), ctypes.byref(sp), ctypes.byref(ms)))
+    finally:
+        set_walk_rcut2(None)
+    return {"stages": st.value, "split_unit": sp.value, "ms": ms.value}
 
 
 def send_j(rec: Records, tag: int = 0) -> None:

@@ -62,6 +62,8 @@ def _lib() -> ctypes.CDLL:
             "pgf_nbody_get_stats": [vp, vp],
             "pgf_nbody_export_lists": [vp] + [vp] * 10,
             "pgf_nbody_autotune": [vp, ci, vp, vp],
+            "pgf_nbody_set_group_limit": [vp, ci],
+            "pgf_nbody_autotune_groups": [vp, vp, ci, ci, vp, vp, vp, vp, vp],
             "pgf_nbody_set_sample": [vp, ci, vp, ci],
             "pgf_nbody_get_sample": [vp, vp, vp],
             "pgf_nbody_destroy": [vp],
@@ -157,6 +159,24 @@ class DeviceNBody:
         v, ms = ctypes.c_int(), ctypes.c_double()
         _check(_lib().pgf_nbody_autotune(self._h, repeats, ctypes.byref(v), ctypes.byref(ms)))
         return v.value, ms.value
+
+    def set_group_limit(self, n_group_limit: int) -> None:
+        """Rebuilds the tree and lists with this n_group_limit (and evaluates)."""
+        _check(_lib().pgf_nbody_set_group_limit(self._h, int(n_group_limit)))
+
+    def autotune_groups(self, limits=(256, 512, 1024, 2048), repeats: int = 2) -> dict:
+        """Times tree + lists + force per evaluation for each n_group_limit
+        candidate (kernel variant tuned per candidate) and keeps the fastest."""
+        lim = np.ascontiguousarray(limits, dtype=np.int32)
+        ms = np.zeros(lim.size)
+        inter = np.zeros(lim.size, np.int64)
+        best, var, bms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _check(_lib().pgf_nbody_autotune_groups(self._h, _p(lim), lim.size, int(repeats), _p(ms), _p(inter),
+                                                ctypes.byref(best), ctypes.byref(var), ctypes.byref(bms)))
+        return {"best_n_group_limit": best.value, "kernel_variant": var.value, "best_ms": bms.value,
+                "candidates": [{"n_group_limit": int(g), "ms_per_evaluation": float(t), "interactions": int(i),
+                                "value": float(i) / (t * 1e-3) / 1e9 if t > 0 else None}
+                               for g, t, i in zip(lim, ms, inter)]}
 
     def set_sample(self, particles: np.ndarray, max_records: int) -> None:
         """Record, after every force evaluation, the mixed-precision result of
