@@ -202,6 +202,18 @@ int pgf_set_dispatch_stages(int stages);
  * All modes; no counterpart in the reference. */
 int pgf_set_walk_split(int enable);
 
+/* Limit of every bounded wait inside the warp-specialised kernels, in
+ * nanoseconds of the GPU's global timer (0 restores the default, 1 s).  A
+ * wait that runs out sets the device error word and its warp returns, so the
+ * kernel ends and the next retrieve reports PGF_ERR_DEVICE instead of the
+ * launch hanging.  No counterpart in the reference, whose kernels do not wait. */
+int pgf_set_wait_limit_ns(uint64_t limit_ns);
+/* Test hook for the path above: with items > 0 the producer warp of the
+ * warp-specialised kernels stops publishing ring items after that many, so
+ * that the consumers' waits run out (no fault, no trap; every warp returns).
+ * 0 (the default) turns it off.  For failure-detection tests only. */
+int pgf_test_stall_producer(int items);
+
 /* Host-direct data movement (1, the default, or 0 = off).  On GB300 the GPU
  * reads ordinary (pageable) host memory coherently through the host page
  * tables over NVLink-C2C.  When the device reports that

@@ -150,6 +150,7 @@ struct TagState {
     HostBuf<ForceDst> h_dst;
     DevBuf<ForceDst> dst;
     HostBuf<int32_t> h_hd_err;
+    cudaEvent_t ev_in = nullptr;  // host-direct dispatch: the gather has read the caller's arrays
 };
 
 struct State {
@@ -168,6 +169,8 @@ struct State {
     int stages = 0;   // dispatch pipeline stages (pgf_set_dispatch_stages); 0 = by size
     bool walk_split = true;  // split the largest walks of small dispatches (pgf_set_walk_split)
     int split_div = 8;       // split unit: 1/split_div of one SM's even share (pgf_autotune_dispatch)
+    uint64_t wait_limit_ns = 0;  // bounded waits of the kernels (pgf_set_wait_limit_ns; 0: 1 s)
+    int stall_after_items = 0;   // test hook (pgf_test_stall_producer)
     // Host-direct data movement (pgf_set_host_direct): the device reads the
     // caller's records in place and writes results into them; used when the
     // device can access pageable host memory.
@@ -204,6 +207,7 @@ struct State {
     DevBuf<int32_t> scratch;
     DevBuf<Retest> retest;
     int retest_cap = 0;
+    DevBuf<int32_t> hd_err;  // per tag: id check of its last host-direct dispatch (2 words)
     std::vector<double> walk_rcut2;
     TagState tags[kMaxTags];
     pgf_profile prof{};
@@ -247,6 +251,7 @@ int setup_device(int rank) {
     PGF_CUDA(cudaEventCreate(&g.ev_send0));
     PGF_CUDA(cudaEventCreate(&g.ev_send1));
     for (auto& t : g.tags) {
+        PGF_CUDA(cudaEventCreate(&t.ev_in));
         for (auto& ev : t.ev) PGF_CUDA(cudaEventCreate(&ev));
         for (auto& c : t.evc)
             for (auto& ev : c) PGF_CUDA(cudaEventCreate(&ev));
@@ -255,6 +260,8 @@ int setup_device(int rank) {
     g.retest_cap = 1 << 20;
     PGF_CUDA(g.retest.ensure((size_t)g.retest_cap));
     PGF_CUDA(cudaMemset(g.scratch.d, 0, kScratchInts * sizeof(int32_t)));
+    PGF_CUDA(g.hd_err.ensure(2 * kMaxTags));
+    PGF_CUDA(cudaMemset(g.hd_err.d, 0, 2 * kMaxTags * sizeof(int32_t)));
     g.init = true;
     return PGF_OK;
 }
@@ -557,6 +564,8 @@ int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, co
 // n_stages: its own queue cursor, re-test counter and slice of the re-test
 // records, so that the launches of different stages may overlap.
 void bind_scratch(Params& p, int stage = -1, int n_stages = 1) {
+    p.wait_limit_ns = g.wait_limit_ns;
+    p.stall_after_items = g.stall_after_items;
     p.err = g.scratch.d + 2;
     p.retest_total = g.scratch.d + 3;
     if (stage < 0) {
@@ -828,7 +837,8 @@ int dispatch_host_direct(TagState& t, int n_walk, const std::vector<int32_t>& or
     a.out_id_epj = t.id_epj.d;
     a.out_id_spj = t.id_spj.d;
     a.out_walks = t.walks.d;
-    a.err = g.scratch.d + 4;
+    const int tag = (int)(&t - g.tags);
+    a.err = g.hd_err.d + 2 * tag;
     g.prof.copy += now_s() - t0;
     PGF_CUDA(cudaEventRecord(t.ev[0], g.stream));
     PGF_CUDA(cudaMemsetAsync(a.err, 0, 2 * sizeof(int32_t), g.stream));
@@ -838,9 +848,11 @@ int dispatch_host_direct(TagState& t, int n_walk, const std::vector<int32_t>& or
         if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "walk gather kernel failed: %s", cudaGetErrorString(e));
     }
     PGF_CUDA(cudaMemcpyAsync(t.h_hd_err.h, a.err, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, g.stream));
-    PGF_CUDA(cudaStreamSynchronize(g.stream));
-    if (t.h_hd_err.h[0] != 0)
-        return fail(PGF_ERR_ARG, "walk %d has an EPJ/SPJ id outside the sent arrays", t.h_hd_err.h[1]);
+    PGF_CUDA(cudaEventRecord(t.ev_in, g.stream));
+    // The force kernels are queued right behind the gather, with no host
+    // round trip between: they read the check's result themselves and run
+    // nothing when an id was out of range.
+    t.params.input_err = a.err;
     PGF_CUDA(cudaMemcpyAsync(t.order.d, t.h_order.h, n_desc * sizeof(int32_t), cudaMemcpyHostToDevice, g.stream));
     if (!plan.empty()) {
         PGF_CUDA(cudaMemcpyAsync(t.splits.d, t.h_splits.h, plan.size() * sizeof(SplitRec), cudaMemcpyHostToDevice,
@@ -850,7 +862,16 @@ int dispatch_host_direct(TagState& t, int n_walk, const std::vector<int32_t>& or
         if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "split rows kernel failed: %s", cudaGetErrorString(e));
         t.n_split = (int)plan.size();
     }
-    return launch_tag(t);
+    if (int r = launch_tag(t)) return r;
+    // The caller's arrays are only valid during the call: return once the
+    // gather has read them, with the check's verdict.
+    PGF_CUDA(cudaEventSynchronize(t.ev_in));
+    if (t.h_hd_err.h[0] != 0) {
+        t.dispatched = false;
+        t.has_data = false;
+        return fail(PGF_ERR_ARG, "walk %d has an EPJ/SPJ id outside the sent arrays", t.h_hd_err.h[1]);
+    }
+    return PGF_OK;
 }
 
 // Packs the walks of one index dispatch (src/force_gpu_cuda.cu:621-699) and
@@ -1344,6 +1365,17 @@ int pgf_set_changeover_layout(const pgf_changeover_layout* layout) {
     return PGF_OK;
 }
 
+int pgf_set_wait_limit_ns(uint64_t limit_ns) {
+    g.wait_limit_ns = limit_ns;
+    return PGF_OK;
+}
+
+int pgf_test_stall_producer(int items) {
+    if (items < 0) return fail(PGF_ERR_ARG, "items must be >= 0");
+    g.stall_after_items = items;
+    return PGF_OK;
+}
+
 int pgf_set_host_direct(int enable) {
     g.hd_enabled = enable != 0;
     return PGF_OK;
@@ -1699,6 +1731,8 @@ int pgf_finalize(void) {
         t.h_epi_acc.release();
         t.acorr.release();
         t.h_acorr.release();
+        if (t.ev_in) cudaEventDestroy(t.ev_in);
+        t.ev_in = nullptr;
         for (auto& ev : t.ev) {
             if (ev) cudaEventDestroy(ev);
             ev = nullptr;
@@ -1731,6 +1765,7 @@ int pgf_finalize(void) {
     g.h_spj_q64.release();
     g.scratch.release();
     g.retest.release();
+    g.hd_err.release();
     if (g.ev_send0) cudaEventDestroy(g.ev_send0);
     if (g.ev_send1) cudaEventDestroy(g.ev_send1);
     g.ev_send0 = g.ev_send1 = nullptr;

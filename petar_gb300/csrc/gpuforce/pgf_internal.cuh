@@ -166,6 +166,14 @@ struct Params {
     // list builder), or null: the kernels then run min(*n_walk_dev, n_walk)
     // walks, n_walk being the capacity of walks and order.
     const int32_t* n_walk_dev;
+    // Limit of every bounded wait in the warp-specialised kernels (0: 1 s).
+    uint64_t wait_limit_ns;
+    // Test hook: > 0 makes their producer stop after that many ring items.
+    int32_t stall_after_items;
+    int32_t pad2;
+    // Result of the device-side check of a host-direct dispatch's ids, or
+    // null: when it is non-zero the force kernels run nothing.
+    const int32_t* input_err;
 };
 
 // Number of walks of this launch.

@@ -15,6 +15,7 @@ namespace {
 constexpr int kT = 128;  // threads per block = i per chunk = j per tile
 
 __global__ __launch_bounds__(kT) void fp64_kernel(Params p) {
+    if (p.input_err && *p.input_err) return;  // the inputs failed their check: run nothing
     __shared__ double sx[kT], sy[kT], sz[kT], sm[kT], srs[kT];
     __shared__ double sq[6][kT];
     __shared__ int s_w;

@@ -68,6 +68,7 @@ struct SmemGP {
 
 template <int KU>
 __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
+    if (p.input_err && *p.input_err) return;  // the inputs failed their check: run nothing
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmemGP<KU>& s = *reinterpret_cast<SmemGP<KU>*>(smem_raw);
     const int tid = threadIdx.x;

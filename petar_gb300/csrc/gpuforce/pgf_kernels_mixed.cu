@@ -164,6 +164,7 @@ __device__ __forceinline__ double as_double(unsigned lo, unsigned hi) {
 }
 
 __global__ __launch_bounds__(kThreads, PGF_MINB) void mixed_kernel(Params p) {
+    if (p.input_err && *p.input_err) return;  // the inputs failed their check: run nothing
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem& s = *reinterpret_cast<Smem*>(smem_raw);
     const int tid = threadIdx.x;
@@ -521,6 +522,7 @@ __global__ __launch_bounds__(kThreads, PGF_MINB) void mixed_kernel(Params p) {
 // One warp per Retest record: exact FP64 recount of its pair range, added to
 // the neighbour count the interaction kernel wrote.
 __global__ __launch_bounds__(256) void retest_kernel(Params p) {
+    if (p.input_err && *p.input_err) return;  // the inputs failed their check: run nothing
     const int n_rec = min(*p.n_retest, p.retest_cap);
     if (p.retest_total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(p.retest_total, *p.n_retest);
     const int lane = threadIdx.x & 31;

@@ -104,8 +104,10 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
         : "memory");
 }
 
-// Waits for the phase of the given parity to complete; false after 1 s.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int32_t* err) {
+// Waits for the phase of the given parity to complete; false after `limit_ns`
+// of %globaltimer (1 s when 0), with the error word set.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int32_t* err, uint64_t limit_ns) {
+    const unsigned long long limit = limit_ns ? limit_ns : kWaitLimitNs;
     const uint32_t a = smem_addr(bar);
     unsigned done = 0;
     asm volatile(
@@ -128,7 +130,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int32_
             : "r"(a), "r"(parity), "r"(100000u)
             : "memory");
         if (done) return true;
-        if (globaltimer() - t0 > kWaitLimitNs) {
+        if (globaltimer() - t0 > limit) {
             atomicOr(err, kErrWaitTimeout);
             return false;
         }
@@ -336,13 +338,16 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
     auto bail = [&]() {
         if constexpr (TM) {
             for (int b = 0; b < 2; ++b)
-                if (tm_inflight & (1u << b)) (void)mbar_wait(&s.tm.bar[b], (tm_phase >> b) & 1u, p.err);
+                if (tm_inflight & (1u << b)) (void)mbar_wait(&s.tm.bar[b], (tm_phase >> b) & 1u, p.err, p.wait_limit_ns);
         }
     };
     auto acquire = [&](int& sl) -> bool {
+        // Test hook (pgf_test_stall_producer): stop publishing after the
+        // given number of items, so that the consumers' bounded waits expire.
+        if (p.stall_after_items > 0 && item >= (unsigned)p.stall_after_items) return false;
         sl = item % kSlots;
         const unsigned parity = ((item / kSlots) & 1u) ^ 1u;
-        return mbar_wait(&s.empty[sl], parity, p.err);
+        return mbar_wait(&s.empty[sl], parity, p.err, p.wait_limit_ns);
     };
     auto publish = [&](int sl) {
         __syncwarp();
@@ -407,7 +412,7 @@ __device__ void producer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
         auto tm_wait = [&](int u) -> bool {
             if constexpr (TM) {
                 const int b = u & 1;
-                const bool ok = mbar_wait(&s.tm.bar[b], (tm_phase >> b) & 1u, p.err);
+                const bool ok = mbar_wait(&s.tm.bar[b], (tm_phase >> b) & 1u, p.err, p.wait_limit_ns);
                 if (ok) {
                     tm_phase ^= 1u << b;
                     tm_inflight &= ~(1u << b);
@@ -1039,7 +1044,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
 
     for (;;) {
         const int sl = item % kSlots;
-        if (!mbar_wait(&s.full[sl], (item / kSlots) & 1u, p.err)) return;
+        if (!mbar_wait(&s.full[sl], (item / kSlots) & 1u, p.err, p.wait_limit_ns)) return;
         const Hdr h = s.hdr[sl];
         if (h.kind == kItemExit) return;
         if (h.kind == kItemBegin) {
@@ -1165,6 +1170,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
 template <int CW, int KI, int MINB, bool PK, int MD, int TE, int NS, bool TM>
 __global__ __launch_bounds__((CW + 1) * 32, MINB) void ws_kernel(Params p, const __grid_constant__ CUtensorMap tme,
                                                                  const __grid_constant__ CUtensorMap tms) {
+    if (p.input_err && *p.input_err) return;  // the inputs failed their check: run nothing
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Smem<CW, KI, PK, TE, NS, MD, TM>& s = *reinterpret_cast<Smem<CW, KI, PK, TE, NS, MD, TM>*>(smem_raw);
     const int tid = threadIdx.x;

@@ -158,6 +158,8 @@ def load(build: bool = True) -> ctypes.CDLL:
         "pgf_set_dispatch_stages": [ci],
         "pgf_set_walk_split": [ci],
         "pgf_set_host_direct": [ci],
+        "pgf_set_wait_limit_ns": [ctypes.c_uint64],
+        "pgf_test_stall_producer": [ci],
         "pgf_get_host_direct": [vp],
         "pgf_set_mode": [ci],
         "pgf_set_changeover_layout": [vp],
@@ -245,6 +247,16 @@ def set_host_direct(enable: bool) -> None:
     """Move data host-direct where the device supports it (default on): the
     GPU reads the caller's records in place and writes results into them."""
     _check(load().pgf_set_host_direct(1 if enable else 0))
+
+
+def set_wait_limit_ns(limit_ns: int) -> None:
+    """Limit of the kernels' bounded waits (0: the default, 1 s)."""
+    _check(load().pgf_set_wait_limit_ns(int(limit_ns)))
+
+
+def test_stall_producer(items: int) -> None:
+    """Failure-detection test hook: the producer stops after `items` ring items."""
+    _check(load().pgf_test_stall_producer(int(items)))
 
 
 def host_direct_active() -> bool:

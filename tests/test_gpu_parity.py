@@ -534,3 +534,23 @@ def test_walk_split_changeover_and_gradient_modes():
         for q in ("median", "p999"):
             assert e1[q] <= max(1.05 * e0[q], MIXED_MEDIAN if q == "median" else MIXED_P999), (k, q, e1, e0)
     assert (gr[True]["nnb"] == 0).all()
+
+
+def test_bounded_wait_runs_out_and_is_reported():
+    """Failure detection on the device, with no fault: the producer warp of
+    the warp-specialised kernel stops after its first ring item (a test hook)
+    and the wait limit is 1 ms, so every consumer's bounded wait runs out, its
+    warp sets the error word and returns, the kernel ends, and retrieve
+    reports PGF_ERR_DEVICE.  The next evaluation is correct again."""
+    wb, _ = load_golden("plummer2048_walks")
+    assert gpuforce.get_kernel_variant() != 0  # a warp-specialised variant
+    gpuforce.set_wait_limit_ns(1_000_000)
+    gpuforce.test_stall_producer(1)
+    try:
+        with pytest.raises(gpuforce.GpuForceError) as e:
+            gpuforce.compute(wb, PGF_PRECISION_MIXED)
+        assert e.value.code == 6  # PGF_ERR_DEVICE
+    finally:
+        gpuforce.test_stall_producer(0)
+        gpuforce.set_wait_limit_ns(0)
+    check(wb, gpuforce.compute(wb, PGF_PRECISION_MIXED), PGF_PRECISION_MIXED, label="after the timeout")
