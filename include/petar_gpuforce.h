@@ -219,9 +219,11 @@ int pgf_test_stall_producer(int items);
  * tables over NVLink-C2C.  When the device reports that
  * (cudaDevAttrPageableMemoryAccess), the send phase and single-launch walk
  * dispatches read the caller's records and id lists in place with a gather
- * kernel, and retrieve writes results into the caller's Force records with a
- * scatter kernel, instead of packing on the host into pinned staging and
- * copying.  The device arrays, and so the results, are bit-identical either
+ * kernel, and retrieve of a single-launch dispatch writes results into the
+ * caller's Force records with a scatter kernel, instead of packing on the
+ * host into pinned staging and copying.  Pipelined dispatches keep the host
+ * packing and unpacking of their walks, which overlap the kernels of other
+ * stages on the copy engines and host cores.  The device arrays, and so the results, are bit-identical either
  * way; ids are still checked before any force kernel runs.  The caller's
  * arrays must stay valid and unchanged for the duration of each call, as the
  * reference requires.  No counterpart in the reference, whose host code

@@ -1530,9 +1530,9 @@ int copy_back(TagState& t, int64_t r0, int64_t r1, cudaStream_t s) {
     return PGF_OK;
 }
 
-// Retrieve host-direct: a scatter kernel writes each walk's results into the
-// caller's Force records (in walk layout order, stage by stage for a
-// pipelined dispatch), so nothing is copied back or unpacked on the host.
+// Retrieve host-direct (single-launch dispatches): a scatter kernel writes
+// each walk's results into the caller's Force records, so nothing is copied
+// back or unpacked on the host.
 int retrieve_host_direct(TagState& t, int n_walk, const int* ni, void* const* force, const pgf_force_layout* fl) {
     PGF_CUDA(t.h_dst.ensure(n_walk));
     PGF_CUDA(t.dst.ensure(n_walk));
@@ -1565,23 +1565,13 @@ int retrieve_host_direct(TagState& t, int n_walk, const int* ni, void* const* fo
         if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "result scatter kernel failed: %s", cudaGetErrorString(e));
         return PGF_OK;
     };
-    cudaStream_t st = t.n_chunks > 0 ? g.d2h_stream : g.stream;
+    cudaStream_t st = g.stream;
     PGF_CUDA(cudaMemcpyAsync(t.dst.d, t.h_dst.h, n_walk * sizeof(ForceDst), cudaMemcpyHostToDevice, st));
-    if (t.n_chunks > 0) {
-        for (int c = 0; c < t.n_chunks; ++c) {
-            PGF_CUDA(cudaStreamWaitEvent(st, t.evc[c][4], 0));
-            if (c == 0) PGF_CUDA(cudaEventRecord(t.ev[4], st));
-            if (int r = scatter(t.stage_k[c], t.stage_k[c + 1], st)) return r;
-        }
-        PGF_CUDA(cudaStreamWaitEvent(st, t.ev[3], 0));
-    } else {
-        PGF_CUDA(cudaEventRecord(t.ev[4], st));
-        if (int r = scatter(0, n_walk, st)) return r;
-    }
+    PGF_CUDA(cudaEventRecord(t.ev[4], st));
+    if (int r = scatter(0, n_walk, st)) return r;
     PGF_CUDA(cudaMemcpyAsync(t.h_flags.h, g.scratch.d, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     PGF_CUDA(cudaMemsetAsync(g.scratch.d + 2, 0, 2 * sizeof(int32_t), st));
     PGF_CUDA(cudaEventRecord(t.ev[5], st));
-    if (t.n_chunks > 0) PGF_CUDA(cudaStreamWaitEvent(g.stream, t.ev[5], 0));  // later work follows the memset
     PGF_CUDA(cudaEventSynchronize(t.ev[5]));
     t.dispatched = false;
     harvest_times(t);
@@ -1609,7 +1599,10 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
     PGF_CUDA(cudaSetDevice(g.device));
     const int64_t n = t.ni_tot;
     PGF_CUDA(t.h_flags.ensure(4));
-    if (use_hd()) return retrieve_host_direct(t, n_walk, ni, force, fl);
+    // Host-direct results for single launches.  A pipelined dispatch keeps
+    // the copy-engine copies and host unpacking per stage: those overlap the
+    // later stages' kernels, where a scatter kernel would wait for their SMs.
+    if (use_hd() && t.n_chunks == 0) return retrieve_host_direct(t, n_walk, ni, force, fl);
     PGF_CUDA(t.h_accp.ensure(n));
     PGF_CUDA(t.h_nnb.ensure(n));
     if (t.mode == PGF_MODE_GRADIENT) PGF_CUDA(t.h_acorr.ensure(n));
