@@ -665,64 +665,6 @@ __device__ __forceinline__ float pass_cost(int nip, int ku, int ct_threads) {
     return (float)warps * ((float)ku + 0.15f) / (float)n_js;
 }
 
-// Pass layouts with a per-warp i count.  A pass of nip i-particles runs as
-// n_js j-slices; every slice holds all nip i.  Its i are split between two
-// classes of threads laid out class-major over the consumer threads: class A
-// (threads [0, n_js sA), KI i per thread, slot l of slice q at thread q sA + l,
-// holding i = l + k sA) and class B (starting at the next warp boundary after
-// class A, kuB < KI i per thread, holding i = KI sA + l + k sB).  Each warp
-// runs one i count, so no warp executes two loop bodies, and the threads a
-// layout leaves idle fill whole warps where possible: those sleep at the ring
-// barriers and leave their issue slots to the other CTAs on the SM.  Per j
-// entry, the layout costs sum over warps of (i count + 0.15) / n_js issue
-// slots (pass_cost's measure); the table keeps, per nip, the cheapest layout
-// whose pass takes no longer than the uniform layout pass_cost picks.  Packed
-// per entry: n_js | sA << 8 | kuB << 16 | sB << 24.
-constexpr int kMaxPassCfg = 384;
-__device__ uint32_t g_pass_cfg[2][kMaxPassCfg + 1];  // [KI - 2][nip]
-
-__global__ void pass_cfg_kernel(int ct_threads) {
-    const int ki = 2 + blockIdx.x;
-    const int nip = threadIdx.x + 1;
-    if (nip > ct_threads * ki || nip > kMaxPassCfg) return;
-    // The uniform layout (all slices KI or KI - 1 i per thread).
-    float best_cost = 3.0e38f, wall0 = 0.f;
-    uint32_t best = 0;
-    for (int ku = ki; ku >= ki - 1 && ku >= 1; --ku) {
-        const int S = (nip + ku - 1) / ku;
-        const int n = ct_threads / S;
-        if (n == 0) continue;
-        const float c = pass_cost(nip, ku, ct_threads);
-        if (c < best_cost) {
-            best_cost = c;
-            wall0 = (float)ku / (float)n;
-            best = ku == ki ? ((uint32_t)n | ((uint32_t)S << 8) | (1u << 16))
-                            : ((uint32_t)n | ((uint32_t)ku << 16) | ((uint32_t)S << 24));
-        }
-    }
-    for (int n = 1; n <= ct_threads; ++n) {
-        for (int sa = 0; sa * n <= ct_threads; ++sa) {
-            const int rem = nip > ki * sa ? nip - ki * sa : 0;
-            for (int kub = 1; kub < ki; ++kub) {
-                const int sb = (rem + kub - 1) / kub;
-                if (sa + sb == 0) continue;
-                const int ta = n * sa, taw = (ta + 31) & ~31, tb = n * sb;
-                if (taw + tb > ct_threads) continue;
-                const float wall = (float)(sa > 0 ? ki : kub) / (float)n;
-                if (wall > wall0 * 1.0001f) continue;
-                const float c = ((float)((ta + 31) >> 5) * ((float)ki + 0.15f) +
-                                 (float)((tb + 31) >> 5) * ((float)kub + 0.15f)) / (float)n;
-                if (c < best_cost * 0.9999f) {
-                    best_cost = c;
-                    best = (uint32_t)n | ((uint32_t)sa << 8) | ((uint32_t)kub << 16) | ((uint32_t)sb << 24);
-                }
-            }
-            if (ki * sa >= nip) break;
-        }
-    }
-    g_pass_cfg[ki - 2][nip] = best;
-}
-
 // Consumer registers hold only what the far and SP loops need: the i hi
 // coordinates and the pair accumulators.  The near-only data of each i (lo
 // coordinates, r_search^2, guard band) and the neighbour counts live in
@@ -738,13 +680,10 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
     const float eps2 = (float)p.eps2;
     unsigned item = 0;
 
-    // Pass state: this thread's class of the pass layout (g_pass_cfg): ku i
-    // per thread, its j-slice js of n_js, the row gbase of its first i and
-    // the row stride istride between its i, of which ivalid lie in the pass.
-    // cbase is the thread's class base and slot its place in its slice.  The
-    // tile bodies are instantiated for every i count up to KI.
+    // Pass state.  A pass runs ku (KA or KI) i-particles per thread, whichever
+    // leaves fewer lanes idle; the tile bodies are instantiated for both.
     float rcut2 = 0.f;
-    int nip = 0, istride = 1, n_js = 1, js = 0, slot = 0, ku = KI, gbase = 0, ivalid = 0, cbase = 0;
+    int nip = 0, S = 1, n_js = 1, js = 0, slot = 0, ku = KI, gbase = 0;
     bool active = false;
     // Scalar path: i coordinates and accumulators a[0..2] acceleration, a[3]
     // potential.  Packed path: (-x_i, -x_i) operands and pair accumulators
@@ -855,7 +794,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
         since = 0;
     };
     auto push_retest = [&](int k, int64_t jidx) -> int {
-        const int gi = gbase + k * istride;
+        const int gi = gbase + k * S;
         const int r = atomicAdd(p.n_retest, 1);
         if (r < p.retest_cap) {
             Retest rr;
@@ -902,7 +841,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
                 lo[k] = s.nlo[k][ct];
                 kb[k] = s.nkb[k][ct];
                 c[k] = 0;
-                vk[k] = k < ivalid;
+                vk[k] = slot + k * S < nip;
                 if constexpr (CO) ci[k] = s.co.coi[k][ct];
             }
             (void)ci;
@@ -1112,42 +1051,16 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
             const WalkDesc wd = p.walks[h.walk];
             rcut2 = (float)wd.rcut2;
             nip = min(kMaxPass, wd.n_i - h.ipass);
-            const uint32_t cfg = (KI >= 2 && KI <= 3 && nip <= kMaxPassCfg) ? g_pass_cfg[KI - 2][nip] : 0u;
-            int ioff = 0;
-            active = false;
-            if (cfg & 0xffu) {
-                n_js = (int)(cfg & 0xffu);
-                const int sa = (int)((cfg >> 8) & 0xffu), kub = (int)((cfg >> 16) & 0xffu),
-                          sb = (int)(cfg >> 24);
-                const int ta = n_js * sa, taw = (ta + 31) & ~31;
-                if (ct < ta) {
-                    ku = KI;
-                    istride = sa;
-                    cbase = 0;
-                    active = true;
-                } else if (ct >= taw && ct < taw + n_js * sb) {
-                    ku = kub;
-                    istride = sb;
-                    cbase = taw;
-                    ioff = KI * sa;
-                    active = true;
-                }
-            } else {
-                // Table not built on this device yet: the uniform layout.
-                ku = KI;
-                if constexpr (KA < KI) {
-                    if (pass_cost(nip, KA, CT) < pass_cost(nip, KI, CT)) ku = KA;
-                }
-                istride = (nip + ku - 1) / ku;
-                n_js = CT / istride;
-                cbase = 0;
-                active = ct < n_js * istride;
+            ku = KI;
+            if constexpr (KA < KI) {
+                if (pass_cost(nip, KA, CT) < pass_cost(nip, KI, CT)) ku = KA;
             }
-            js = active ? (ct - cbase) / istride : 0;
-            slot = active ? (ct - cbase) - js * istride : 0;
-            const int i0 = ioff + slot;
-            ivalid = (!active || i0 >= nip) ? 0 : min(ku, (nip - 1 - i0) / istride + 1);
-            gbase = wd.i_begin + h.ipass + i0;
+            S = (nip + ku - 1) / ku;
+            n_js = CT / S;
+            js = ct / S;
+            slot = ct - js * S;
+            active = js < n_js;
+            gbase = wd.i_begin + h.ipass + slot;
             if constexpr (CO) {
                 r_out_walk = sqrt(wd.rcut2);
                 rcut2d = wd.rcut2;
@@ -1156,12 +1069,12 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
             }
 #pragma unroll
             for (int k = 0; k < KI; ++k) {
-                const bool valid = k < ivalid;
+                const bool valid = active && k < ku && slot + k * S < nip;
                 float hx = 0.f, hy = 0.f, hz = 0.f;
                 float4 lo = make_float4(0.f, 0.f, 0.f, 0.f);
                 int kb = 0;
                 if (valid) {
-                    const EpiDev e = p.epi[gbase + k * istride];
+                    const EpiDev e = p.epi[gbase + k * S];
                     const double dx = e.x - wd.cx, dy = e.y - wd.cy, dz = e.z - wd.cz;
                     hx = (float)dx;
                     hy = (float)dy;
@@ -1184,7 +1097,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
                 if constexpr (CO) {
                     CoRec cr{};
                     cr.id = -1;
-                    if (valid) cr = p.epi_co[gbase + k * istride];
+                    if (valid) cr = p.epi_co[gbase + k * S];
                     s.co.coi[k][ct] = cr;
                     s.co.dtot[k][ct] = make_float2(0.f, 0.f);
                     s.co.dsoft[k][ct] = make_float2(0.f, 0.f);
@@ -1199,24 +1112,16 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
             if (active) {
                 if (ku == KI)
                     ep_tile(IntC<KI>{}, h, sl);
-                else if constexpr (KA < KI) {
-                    if (ku == KA)
-                        ep_tile(IntC<KA>{}, h, sl);
-                    else if constexpr (KA > 1)
-                        ep_tile(IntC<1>{}, h, sl);
-                }
+                else if constexpr (KA < KI)
+                    ep_tile(IntC<KA>{}, h, sl);
                 if (since >= kFlush) flush();
             }
         } else if (h.kind == kItemSP) {
             if (active) {
                 if (ku == KI)
                     sp_tile(IntC<KI>{}, h, sl);
-                else if constexpr (KA < KI) {
-                    if (ku == KA)
-                        sp_tile(IntC<KA>{}, h, sl);
-                    else if constexpr (KA > 1)
-                        sp_tile(IntC<1>{}, h, sl);
-                }
+                else if constexpr (KA < KI)
+                    sp_tile(IntC<KA>{}, h, sl);
                 if (since >= kFlush) flush();
             }
         } else {  // kItemEnd: reduce the j-slices of the pass and write
@@ -1226,11 +1131,11 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
                 const double G = p.G;
 #pragma unroll
                 for (int k = 0; k < KI; ++k) {
-                    if (k >= ivalid) continue;
+                    if (!(k < ku && slot + k * S < nip)) continue;
                     double r[4] = {0.0, 0.0, 0.0, 0.0}, rt = 0.0, rs = 0.0;
                     int n = 0;
                     for (int q = 0; q < n_js; ++q) {
-                        const int src = cbase + q * istride + slot;
+                        const int src = q * S + slot;
 #pragma unroll
                         for (int c = 0; c < 4; ++c) {
                             const float2 v = s.acc[k][c][src];
@@ -1243,10 +1148,10 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
                         }
                         n += s.cnt[k][src];
                     }
-                    const int gi = gbase + k * istride;
+                    const int gi = gbase + k * S;
                     if constexpr (CO) {
                         // self-potential G m / r_out removed (src/hard.hpp:1663-1674)
-                        const double self = self_scale * (double)s.co.coi[k][ct].mass / r_out_walk;
+                        const double self = self_scale * (double)s.co.coi[k][slot].mass / r_out_walk;
                         p.out_accp[gi] = Accp{G * r[0], G * r[1], G * r[2], G * ((r[3] + rt) + self)};
                         p.out_pot_soft[gi] = G * ((r[3] + rs) + self);
                     } else if constexpr (!SR) {
@@ -1288,25 +1193,9 @@ __global__ __launch_bounds__((CW + 1) * 32, MINB) void ws_kernel(Params p, const
         consumer<CW, KI, PK, MD, TE, NS, TM>(p, s, tid);
 }
 
-// Builds the pass-layout table on the current device before its first
-// warp-specialised launch (stream-ordered; once per device).
-cudaError_t ensure_pass_cfg(cudaStream_t st, int ct_threads) {
-    static bool built[64] = {};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev >= 0 && dev < 64 && built[dev]) return cudaSuccess;
-    pass_cfg_kernel<<<2, kMaxPassCfg, 0, st>>>(ct_threads);
-    e = cudaGetLastError();
-    if (e == cudaSuccess && dev >= 0 && dev < 64) built[dev] = true;
-    return e;
-}
-
 template <int CW, int KI, int MINB, bool PK, int MD = kModeForce, int TE = 128, int NS = 4, bool TM = false>
 cudaError_t launch_ws_t(const Params& p, cudaStream_t st, int num_sms, const TensorMaps* tm = nullptr) {
-    static_assert(CW * 32 == 128 && KI >= 2 && KI <= 3, "pass-layout table: 128 consumer threads, 2 or 3 i each");
-    cudaError_t e = ensure_pass_cfg(st, CW * 32);
-    if (e == cudaSuccess) e = cudaMemsetAsync(p.queue_head, 0, sizeof(int32_t), st);
+    cudaError_t e = cudaMemsetAsync(p.queue_head, 0, sizeof(int32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), st);
     if (e != cudaSuccess) return e;
     if (p.n_walk <= 0) return cudaSuccess;
