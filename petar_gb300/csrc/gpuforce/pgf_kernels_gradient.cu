@@ -41,6 +41,21 @@ __device__ __forceinline__ void two_sum_g(float a, float b, float& s, float& e) 
     e = (a - (s - bb)) + (b - bb);
 }
 
+// Double-float helpers: a value is an FP32 pair (h, l) with h + l exact to
+// about 2^-48 relative.  two_prod_g is exact with one FMA.
+__device__ __forceinline__ void two_prod_g(float a, float b, float& p, float& e) {
+    p = a * b;
+    e = fmaf(a, b, -p);
+}
+
+// (x_j - x_i) as a double-float from both operands' (hi, lo) halves; the i
+// halves are passed negated.
+__device__ __forceinline__ void df_diff(float jh, float jl, float nih, float nil, float& h, float& l) {
+    float s, e;
+    two_sum_g(jh, nih, s, e);
+    two_sum_g(s, e + (jl + nil), h, l);
+}
+
 __device__ __forceinline__ void flush_into(float2& v, float x) {
     float e;
     two_sum_g(v.x, x, v.x, e);
@@ -62,6 +77,11 @@ struct SmemGP {
     float4 P[kTileEPG / 2][4];
     float4 A[kTileEPG / 2][3];
     float4 S[kTileSPG / 2][6];
+    // Near entries of the EP tile at their own index: (xh, yh, zh, m),
+    // (xl, yl, zl, -), (axh, ayh, azh, -), (axl, ayl, azl, -); which entries
+    // are near: one bit each.
+    float4 N[kTileEPG][4];
+    unsigned nmask[kTileEPG / 32];
     float2 acc[KU][7][kThreadsG];
     int w;
 };
@@ -85,6 +105,17 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
         const float clx = (float)(wd.cx - (double)chx), cly = (float)(wd.cy - (double)chy),
                     clz = (float)(wd.cz - (double)chz);
         const float rcut2 = (float)wd.rcut2;
+        // Near entries (possibly within r_out of an i of the walk's box):
+        // their pairs run in the near loop below.  Inside r_out the distance
+        // is clamped to r_out, and da - 3 (dr.da) / r_out^2 dr cancels for
+        // pairs at r_out / sqrt(3) with da along dr (close binary companions);
+        // those pairs are evaluated in double-float arithmetic with
+        // kdf = 3 / r_out^2 and r3c = r_out^-3 formed in FP64 here.
+        const float rc = sqrtf(rcut2);
+        const float hmax = fmaxf(wd.hx, fmaxf(wd.hy, wd.hz));
+        const double kd = 3.0 / wd.rcut2;
+        const float kdh = (float)kd, kdl = (float)(kd - (double)kdh);
+        const float r3c = (float)(1.0 / (wd.rcut2 * sqrt(wd.rcut2)));
         for (int ipass = 0; ipass < wd.n_i; ipass += kThreadsG * KU) {
             const int nip = min(kThreadsG * KU, wd.n_i - ipass);
             const int S = (nip + KU - 1) / KU;
@@ -152,6 +183,7 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
             for (int t = 0; t < wd.n_epj; t += kTileEPG) {
                 const int nt = min(kTileEPG, wd.n_epj - t);
                 __syncthreads();
+                bool near = false;
                 if (tid < nt) {
                     const int id = p.id_epj[wd.epj_begin + t + tid];
                     const EpjF32 r = p.epj32[id];
@@ -163,11 +195,25 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
                     two_sum_g(s_, e_ + (r.yl - cly), hy, ly);
                     two_sum_g(r.zh, -chz, s_, e_);
                     two_sum_g(s_, e_ + (r.zl - clz), hz, lz);
+                    // Conservative box test (0.2% and absolute margins over r_out).
+                    const float ex = fmaxf(fabsf(hx) - wd.hx, 0.f);
+                    const float ey = fmaxf(fabsf(hy) - wd.hy, 0.f);
+                    const float ez = fmaxf(fabsf(hz) - wd.hz, 0.f);
+                    const float dist2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+                    const float dmax = fmaxf(fabsf(hx), fmaxf(fabsf(hy), fabsf(hz)));
+                    const float Rm = rc * 1.002f + 1e-6f * (dmax + hmax);
+                    near = !(dist2 > Rm * Rm);
+                    if (near) {
+                        s.N[tid][0] = make_float4(hx, hy, hz, r.m);
+                        s.N[tid][1] = make_float4(lx, ly, lz, 0.f);
+                        s.N[tid][2] = make_float4(a.xh, a.yh, a.zh, 0.f);
+                        s.N[tid][3] = make_float4(a.xl, a.yl, a.zl, 0.f);
+                    }
                     float* P = reinterpret_cast<float*>(&s.P[tid >> 1][0]) + (tid & 1);
                     P[0] = hx;
                     P[2] = hy;
                     P[4] = hz;
-                    P[6] = r.m;
+                    P[6] = near ? 0.f : r.m;  // near pairs run in the near loop
                     P[8] = lx;
                     P[10] = ly;
                     P[12] = lz;
@@ -185,6 +231,10 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
                     float* A = reinterpret_cast<float*>(&s.A[tid >> 1][0]) + 1;
                     for (int u = 0; u < 16; u += 2) P[u] = 0.f;
                     for (int u = 0; u < 12; u += 2) A[u] = 0.f;
+                }
+                {
+                    const unsigned bn = __ballot_sync(0xffffffffu, near);
+                    if ((tid & 31) == 0 && tid < kTileEPG) s.nmask[tid >> 5] = bn;
                 }
                 __syncthreads();
                 if (active) {
@@ -213,8 +263,12 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
                             float2 r2 = __ffma2_rn(dx, dx, e2);
                             r2 = __ffma2_rn(dy, dy, r2);
                             r2 = __ffma2_rn(dz, dz, r2);
-                            const float2 ri = make_float2(rsqrt_approx_g(fmaxf(r2.x, rcut2)),
-                                                          rsqrt_approx_g(fmaxf(r2.y, rcut2)));
+                            const float2 r2c = make_float2(fmaxf(r2.x, rcut2), fmaxf(r2.y, rcut2));
+                            float2 ri = make_float2(rsqrt_approx_g(r2c.x), rsqrt_approx_g(r2c.y));
+                            // one Newton step: the sum over j cancels, so each
+                            // term's 1/r^3 is kept to about an ulp
+                            const float2 hh = __fmul2_rn(__fmul2_rn(r2c, ri), ri);
+                            ri = __fmul2_rn(ri, __ffma2_rn(hh, make_float2(-0.5f, -0.5f), make_float2(1.5f, 1.5f)));
                             const float2 ri2 = __fmul2_rn(ri, ri);
                             const float2 mr3 = __fmul2_rn(__fmul2_rn(M, ri), ri2);
                             const float2 drda = __ffma2_rn(dx, dax, __ffma2_rn(dy, day, __fmul2_rn(dz, daz)));
@@ -226,6 +280,67 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
                         }
                     }
                     since += 2 * (j1 - j0);
+                    // Near entries, each handled by slice (index mod n_js).
+                    for (int wv = 0; wv < kTileEPG / 32; ++wv) {
+                        unsigned m = s.nmask[wv];
+                        while (m) {
+                            const int e = wv * 32 + __ffs(m) - 1;
+                            m &= m - 1;
+                            if (e % n_js != js) continue;
+                            const float4 q0 = s.N[e][0], q1 = s.N[e][1], q2 = s.N[e][2], q3 = s.N[e][3];
+#pragma unroll
+                            for (int k = 0; k < KU; ++k) {
+                                if (li + k * S >= nip) continue;
+                                float dh[3], dl[3], ah[3], al[3];
+                                df_diff(q0.x, q1.x, nxh[k].x, nxl[k].x, dh[0], dl[0]);
+                                df_diff(q0.y, q1.y, nyh[k].x, nyl[k].x, dh[1], dl[1]);
+                                df_diff(q0.z, q1.z, nzh[k].x, nzl[k].x, dh[2], dl[2]);
+                                df_diff(q2.x, q3.x, nah[k][0].x, nal[k][0].x, ah[0], al[0]);
+                                df_diff(q2.y, q3.y, nah[k][1].x, nal[k][1].x, ah[1], al[1]);
+                                df_diff(q2.z, q3.z, nah[k][2].x, nal[k][2].x, ah[2], al[2]);
+                                const float r2 = fmaf(dh[0], dh[0], fmaf(dh[1], dh[1], fmaf(dh[2], dh[2], eps2)));
+                                float v[3], mr3;
+                                if (r2 < rcut2) {
+                                    // clamped: v = da - (3 / r_out^2)(dr.da) dr in double-float
+                                    float sh = 0.f, sl = 0.f;
+#pragma unroll
+                                    for (int c = 0; c < 3; ++c) {
+                                        float pp, pe, t1, t2;
+                                        two_prod_g(dh[c], ah[c], pp, pe);
+                                        pe = fmaf(dh[c], al[c], fmaf(dl[c], ah[c], pe));
+                                        two_sum_g(sh, pp, t1, t2);
+                                        sh = t1;
+                                        sl += t2 + pe;
+                                    }
+                                    float alh, ale;
+                                    two_prod_g(kdh, sh, alh, ale);
+                                    ale = fmaf(kdh, sl, fmaf(kdl, sh, ale));
+#pragma unroll
+                                    for (int c = 0; c < 3; ++c) {
+                                        float qh, qe, vh, ve;
+                                        two_prod_g(alh, dh[c], qh, qe);
+                                        qe = fmaf(alh, dl[c], fmaf(ale, dh[c], qe));
+                                        two_sum_g(ah[c], -qh, vh, ve);
+                                        v[c] = vh + (ve + (al[c] - qe));
+                                    }
+                                    mr3 = q0.w * r3c;
+                                } else {
+                                    float ri = rsqrt_approx_g(r2);
+                                    ri = ri * fmaf(-0.5f, (r2 * ri) * ri, 1.5f);
+                                    const float ri2 = ri * ri;
+                                    mr3 = (q0.w * ri) * ri2;
+                                    const float drda = fmaf(dh[0], ah[0], fmaf(dh[1], ah[1], dh[2] * ah[2]));
+                                    const float nl3 = -3.f * (drda * ri2);
+#pragma unroll
+                                    for (int c = 0; c < 3; ++c) v[c] = fmaf(nl3, dh[c], ah[c]);
+                                }
+                                g[k][0].x = fmaf(mr3, v[0], g[k][0].x);
+                                g[k][1].x = fmaf(mr3, v[1], g[k][1].x);
+                                g[k][2].x = fmaf(mr3, v[2], g[k][2].x);
+                            }
+                            ++since;
+                        }
+                    }
                     if (since >= kFlushG) flush();
                 }
             }
