@@ -682,7 +682,8 @@ def run_fdps_batches(wb, rec, n_int: int, batch: int = 200, reps: int = 3) -> di
             gpuforce.RetrieveForceCUDA(0, w1 - w0, rec.n_epi[w0:w1], rec.p_force[w0:w1],
                                        force_dtype=rec.force.dtype)
 
-    out = {"walks_per_call": batch, "calls_per_evaluation": (nw + batch - 1) // batch, "unit": "Ginteractions/s"}
+    out = {"walks_per_call": batch, "calls_per_evaluation": (nw + batch - 1) // batch, "unit": "Ginteractions/s",
+           "caller": "the Python functors (ctypes)"}
     # The dispatch autotuner on one 200-walk call from the middle of the
     # evaluation (the split unit matters for calls this small).
     mid = nw // 2 // batch * batch
@@ -701,7 +702,45 @@ def run_fdps_batches(wb, rec, n_int: int, batch: int = 200, reps: int = 3) -> di
             out[key] = {"ms_per_evaluation": 1e3 * min(ts), "value": n_int / min(ts) / 1e9}
     finally:
         gpuforce.set_walk_split(True)
+    out["cpp_functors"] = fdps_batches_cpp(wb, n_int, batch)
     return out
+
+
+def fdps_batches_cpp(wb, n_int: int, batch: int = 200, reps: int = 3) -> dict:
+    """The same call pattern from C++ (bench_support/fdps_batches.cpp): the
+    header functors with PeTar-layout records, as PeTar itself calls them,
+    with no Python between the calls; checked against the single-dispatch
+    result of the same lists."""
+    import ctypes
+    from bench_support import build_fdps_driver
+    from petar_gb300 import gpuforce
+    lib = ctypes.CDLL(str(build_fdps_driver()))
+    vp = ctypes.c_void_p
+    lib.fdps_batches_run.argtypes = ([ctypes.c_int64, vp, vp, vp, vp, vp, ctypes.c_int64, vp, vp, vp,
+                                      ctypes.c_int64, vp, vp, vp, vp, vp] + [ctypes.c_double] * 3
+                                     + [ctypes.c_int, ctypes.c_int, vp, vp, vp, vp])
+    lib.fdps_batches_run.restype = ctypes.c_int
+    c = lambda a, t: np.ascontiguousarray(a, dtype=t)
+    arrs = [c(wb.n_epi, np.int32), c(wb.n_epj, np.int32), c(wb.n_spj, np.int32), c(wb.epi_pos, np.float64),
+            c(wb.epi_rs, np.float64)]
+    je = [c(wb.epj_mass, np.float64), c(wb.epj_pos, np.float64), c(wb.epj_rs, np.float64)]
+    js = [c(wb.spj_mass, np.float64), c(wb.spj_pos, np.float64), c(wb.spj_quad, np.float64)]
+    ids = [c(wb.id_epj, np.int32), c(wb.id_spj, np.int32)]
+    ni = wb.epi_rs.size
+    acc, pot, nnb = np.zeros((ni, 3)), np.zeros(ni), np.zeros(ni, np.int64)
+    ms = ctypes.c_double()
+    rc = lib.fdps_batches_run(wb.n_walk, *[a.ctypes.data for a in arrs], wb.epj_mass.size,
+                              *[a.ctypes.data for a in je], wb.spj_mass.size, *[a.ctypes.data for a in js],
+                              *[a.ctypes.data for a in ids], wb.eps2, wb.rcut2, wb.G, batch, reps,
+                              ctypes.byref(ms), acc.ctypes.data, pot.ctypes.data, nnb.ctypes.data)
+    if rc != 0:
+        return {"error": f"driver returned {rc}"}
+    ref = gpuforce.compute(wb, gpuforce.PGF_PRECISION_MIXED)
+    ea = np.linalg.norm(acc - ref["acc"], axis=1) / np.linalg.norm(ref["acc"], axis=1)
+    return {"ms_per_evaluation": ms.value, "value": n_int / ms.value / 1e6, "unit": "Ginteractions/s",
+            "caller": "C++ (bench_support/fdps_batches.cpp, include/petar_gpuforce.hpp)",
+            "vs_single_dispatch": {"force_rel_err_p999": float(np.quantile(ea, 0.999)),
+                                   "n_ngb_mismatches": int((nnb != ref["nnb"]).sum())}}
 
 
 def walks_subset_records(rec, w0: int, w1: int):

@@ -263,12 +263,8 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
                             float2 r2 = __ffma2_rn(dx, dx, e2);
                             r2 = __ffma2_rn(dy, dy, r2);
                             r2 = __ffma2_rn(dz, dz, r2);
-                            const float2 r2c = make_float2(fmaxf(r2.x, rcut2), fmaxf(r2.y, rcut2));
-                            float2 ri = make_float2(rsqrt_approx_g(r2c.x), rsqrt_approx_g(r2c.y));
-                            // one Newton step: the sum over j cancels, so each
-                            // term's 1/r^3 is kept to about an ulp
-                            const float2 hh = __fmul2_rn(__fmul2_rn(r2c, ri), ri);
-                            ri = __fmul2_rn(ri, __ffma2_rn(hh, make_float2(-0.5f, -0.5f), make_float2(1.5f, 1.5f)));
+                            const float2 ri = make_float2(rsqrt_approx_g(fmaxf(r2.x, rcut2)),
+                                                          rsqrt_approx_g(fmaxf(r2.y, rcut2)));
                             const float2 ri2 = __fmul2_rn(ri, ri);
                             const float2 mr3 = __fmul2_rn(__fmul2_rn(M, ri), ri2);
                             const float2 drda = __ffma2_rn(dx, dax, __ffma2_rn(dy, day, __fmul2_rn(dz, daz)));
@@ -291,17 +287,21 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
 #pragma unroll
                             for (int k = 0; k < KU; ++k) {
                                 if (li + k * S >= nip) continue;
-                                float dh[3], dl[3], ah[3], al[3];
-                                df_diff(q0.x, q1.x, nxh[k].x, nxl[k].x, dh[0], dl[0]);
-                                df_diff(q0.y, q1.y, nyh[k].x, nyl[k].x, dh[1], dl[1]);
-                                df_diff(q0.z, q1.z, nzh[k].x, nzl[k].x, dh[2], dl[2]);
-                                df_diff(q2.x, q3.x, nah[k][0].x, nal[k][0].x, ah[0], al[0]);
-                                df_diff(q2.y, q3.y, nah[k][1].x, nal[k][1].x, ah[1], al[1]);
-                                df_diff(q2.z, q3.z, nah[k][2].x, nal[k][2].x, ah[2], al[2]);
-                                const float r2 = fmaf(dh[0], dh[0], fmaf(dh[1], dh[1], fmaf(dh[2], dh[2], eps2)));
+                                // dr and da from both halves, as the packed loop forms them
+                                const float d0 = (q0.x + nxh[k].x) + (q1.x + nxl[k].x);
+                                const float d1 = (q0.y + nyh[k].x) + (q1.y + nyl[k].x);
+                                const float d2 = (q0.z + nzh[k].x) + (q1.z + nzl[k].x);
+                                const float r2 = fmaf(d0, d0, fmaf(d1, d1, fmaf(d2, d2, eps2)));
                                 float v[3], mr3;
                                 if (r2 < rcut2) {
                                     // clamped: v = da - (3 / r_out^2)(dr.da) dr in double-float
+                                    float dh[3], dl[3], ah[3], al[3];
+                                    df_diff(q0.x, q1.x, nxh[k].x, nxl[k].x, dh[0], dl[0]);
+                                    df_diff(q0.y, q1.y, nyh[k].x, nyl[k].x, dh[1], dl[1]);
+                                    df_diff(q0.z, q1.z, nzh[k].x, nzl[k].x, dh[2], dl[2]);
+                                    df_diff(q2.x, q3.x, nah[k][0].x, nal[k][0].x, ah[0], al[0]);
+                                    df_diff(q2.y, q3.y, nah[k][1].x, nal[k][1].x, ah[1], al[1]);
+                                    df_diff(q2.z, q3.z, nah[k][2].x, nal[k][2].x, ah[2], al[2]);
                                     float sh = 0.f, sl = 0.f;
 #pragma unroll
                                     for (int c = 0; c < 3; ++c) {
@@ -325,14 +325,16 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
                                     }
                                     mr3 = q0.w * r3c;
                                 } else {
-                                    float ri = rsqrt_approx_g(r2);
-                                    ri = ri * fmaf(-0.5f, (r2 * ri) * ri, 1.5f);
+                                    const float e0 = (q2.x + nah[k][0].x) + (q3.x + nal[k][0].x);
+                                    const float e1 = (q2.y + nah[k][1].x) + (q3.y + nal[k][1].x);
+                                    const float e2_ = (q2.z + nah[k][2].x) + (q3.z + nal[k][2].x);
+                                    const float ri = rsqrt_approx_g(r2);
                                     const float ri2 = ri * ri;
                                     mr3 = (q0.w * ri) * ri2;
-                                    const float drda = fmaf(dh[0], ah[0], fmaf(dh[1], ah[1], dh[2] * ah[2]));
-                                    const float nl3 = -3.f * (drda * ri2);
-#pragma unroll
-                                    for (int c = 0; c < 3; ++c) v[c] = fmaf(nl3, dh[c], ah[c]);
+                                    const float nl3 = -3.f * (fmaf(d0, e0, fmaf(d1, e1, d2 * e2_)) * ri2);
+                                    v[0] = fmaf(nl3, d0, e0);
+                                    v[1] = fmaf(nl3, d1, e1);
+                                    v[2] = fmaf(nl3, d2, e2_);
                                 }
                                 g[k][0].x = fmaf(mr3, v[0], g[k][0].x);
                                 g[k][1].x = fmaf(mr3, v[1], g[k][1].x);

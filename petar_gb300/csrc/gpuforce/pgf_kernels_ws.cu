@@ -53,12 +53,19 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
     return y;
 }
 
-// See kband_near in pgf_kernels_mixed.cu for the derivation.
-__device__ __forceinline__ int kband_near(double D, double rs, double eps2) {
-    const double r2ref = rs * rs - eps2;
-    if (!(r2ref > 0.0)) return kKMax;
-    const double k = 48.0 + 1e-5 * D / sqrt(r2ref);
-    return k >= double(kKMax) ? kKMax : int(k) + 1;
+// Guard band in ulps of rs2 for the near-pair neighbour test of one i at
+// distance D (max norm) from the walk centre; see kband_near in
+// pgf_kernels_mixed.cu for the derivation: the FP32 test is off by less than
+// 8 + 1.3e-6 D / r_ref ulps, r_ref = sqrt(rs^2 - eps2), and the band is
+// 48 + 1e-5 D / r_ref.  Evaluated here in FP32 (GB300's FP64 pipe runs at
+// 1/64 of the FP32 rate and this runs for every i of every pass); the few
+// ulps of rounding of the FP32 form are far inside the factor of six between
+// the band and the bound, and a larger band only adds FP64 re-tests.
+__device__ __forceinline__ int kband_near(float D, float rs2, float eps2) {
+    const float r2ref = rs2 - eps2;
+    if (!(r2ref > 0.f)) return kKMax;
+    const float k = 48.f + 1e-5f * D * rsqrt_approx(r2ref) * 1.001f;
+    return k >= float(kKMax) ? kKMax : int(k) + 1;
 }
 
 // L2 policy for data read once per launch (the id lists): evicted before
@@ -676,7 +683,6 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
     constexpr int CT = CW * 32;
     constexpr int kMaxPass = CT * KI;
     constexpr int KA = KI > 1 ? KI - 1 : 1;  // the other i-per-thread count a pass may use
-    const double eps2d = p.eps2;
     const float eps2 = (float)p.eps2;
     unsigned item = 0;
 
@@ -1081,7 +1087,7 @@ __device__ void consumer(const Params& p, Smem<CW, KI, PK, TE, NS, MD, TM>& s, i
                     hz = (float)dz;
                     lo = make_float4((float)(dx - (double)hx), (float)(dy - (double)hy), (float)(dz - (double)hz),
                                      (float)(e.rs * e.rs));
-                    kb = kband_near(fmax(fabs(dx), fmax(fabs(dy), fabs(dz))), e.rs, eps2d);
+                    kb = kband_near(fmaxf(fabsf(hx), fmaxf(fabsf(hy), fabsf(hz))), lo.w, eps2);
                 }
                 if constexpr (PK) {
                     nx2[k] = make_float2(-hx, -hx);
