@@ -202,6 +202,11 @@ int pgf_set_dispatch_stages(int stages);
  * All modes; no counterpart in the reference. */
 int pgf_set_walk_split(int enable);
 
+/* Split unit of walk splitting: a walk is split when it costs more than
+ * 1/div of one SM's even share of the dispatch (default 8; 1..256).
+ * pgf_autotune_dispatch sets it too.  Results are as for pgf_set_walk_split. */
+int pgf_set_walk_split_unit(int div);
+
 /* Limit of every bounded wait inside the warp-specialised kernels, in
  * nanoseconds of the GPU's global timer (0 restores the default, 1 s).  A
  * wait that runs out sets the device error word and its warp returns, so the

@@ -1392,6 +1392,12 @@ int pgf_set_walk_split(int enable) {
     return PGF_OK;
 }
 
+int pgf_set_walk_split_unit(int div) {
+    if (div < 1 || div > 256) return fail(PGF_ERR_ARG, "split unit divisor %d outside [1, 256]", div);
+    g.split_div = div;
+    return PGF_OK;
+}
+
 int pgf_set_dispatch_stages(int stages) {
     if (stages < 0 || stages > kMaxChunks)
         return fail(PGF_ERR_ARG, "dispatch stages %d outside [0, %d]", stages, kMaxChunks);

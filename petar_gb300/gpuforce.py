@@ -157,6 +157,7 @@ def load(build: bool = True) -> ctypes.CDLL:
         "pgf_set_kernel_variant": [ci],
         "pgf_set_dispatch_stages": [ci],
         "pgf_set_walk_split": [ci],
+        "pgf_set_walk_split_unit": [ci],
         "pgf_set_host_direct": [ci],
         "pgf_set_wait_limit_ns": [ctypes.c_uint64],
         "pgf_test_stall_producer": [ci],
@@ -241,6 +242,11 @@ def set_walk_split(enable: bool) -> None:
     """Split the most expensive walks of small single-launch dispatches over
     several CTAs (default on)."""
     _check(load().pgf_set_walk_split(1 if enable else 0))
+
+
+def set_walk_split_unit(div: int) -> None:
+    """Split walks costing more than 1/div of one SM's even share (default 8)."""
+    _check(load().pgf_set_walk_split_unit(div))
 
 
 def set_host_direct(enable: bool) -> None:
