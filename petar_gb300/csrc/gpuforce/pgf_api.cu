@@ -34,6 +34,7 @@ constexpr int kMaxTags = 16;
 constexpr int kMaxChunks = 8;                       // pipeline stages of a large dispatch
 constexpr int64_t kChunkIdEntries = 12 << 20;       // about 48 MB of id lists per stage
 constexpr int kScratchInts = 8 + 2 * kMaxChunks;
+constexpr int kHdErrWords = 4;  // HdWalkArgs::err
 static_assert(PGF_NUM_KERNEL_VARIANTS == 1 + kNumWsVariants, "variant 0 plus the warp-specialised variants");
 constexpr int64_t kMaxRows = 0x7fffffff;
 
@@ -143,12 +144,11 @@ struct TagState {
     int n_split = 0;
     DevBuf<SplitRec> splits;
     HostBuf<SplitRec> h_splits;
-    // Host-direct tables: where the gather kernel reads each walk, and where
-    // the scatter kernel writes its results.
+    // Host-direct tables, read by the kernels in place: where the gather
+    // kernel reads each walk, and where the scatter kernel writes its
+    // results; h_hd_err receives the gather's id-check verdict.
     HostBuf<WalkSrc> h_src;
-    DevBuf<WalkSrc> src;
     HostBuf<ForceDst> h_dst;
-    DevBuf<ForceDst> dst;
     HostBuf<int32_t> h_hd_err;
     cudaEvent_t ev_in = nullptr;  // host-direct dispatch: the gather has read the caller's arrays
 };
@@ -207,7 +207,7 @@ struct State {
     DevBuf<int32_t> scratch;
     DevBuf<Retest> retest;
     int retest_cap = 0;
-    DevBuf<int32_t> hd_err;  // per tag: id check of its last host-direct dispatch (2 words)
+    DevBuf<int32_t> hd_err;  // per tag: id check of its last host-direct dispatch (HdWalkArgs::err)
     std::vector<double> walk_rcut2;
     TagState tags[kMaxTags];
     pgf_profile prof{};
@@ -228,6 +228,57 @@ int ensure_init() {
 
 // Whether this call moves data host-direct (supported and not turned off).
 bool use_hd() { return g.hd_supported && g.hd_enabled; }
+
+// The host-direct kernels load and store the records' FP64 and integer
+// fields in place, so they take only naturally aligned records: 8-byte
+// aligned arrays whose record size and field offsets are multiples of 8 (and
+// at most 4 KB per EPI record, the gather's staging).  Anything else takes
+// the host packing path.
+inline bool al8(size_t v) { return (v & 7) == 0; }
+inline bool al8p(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 7) == 0; }
+
+bool hd_send_ok(const void* epj, int64_t n_epj, const pgf_epj_layout* el, const void* spj, int64_t n_spj,
+                const pgf_spj_layout* sl) {
+    if (n_epj > 0) {
+        if (!al8p(epj) || !al8(el->size) || !al8(el->off_mass) || !al8(el->off_pos) || !al8(el->off_r_search))
+            return false;
+        if (g.co_set && !(al8(g.co.epj_off_id) && al8(g.co.epj_off_r_in) && al8(g.co.epj_off_r_out) &&
+                          al8(g.co.epj_off_mass_backup) && al8(g.co.epj_off_status)))
+            return false;
+        if (g.gr_set && !al8(g.gr.epj_off_acc)) return false;
+    }
+    if (n_spj > 0 && (!al8p(spj) || !al8(sl->size) || !al8(sl->off_mass) || !al8(sl->off_pos) ||
+                      (sl->has_quad && !al8(sl->off_quad))))
+        return false;
+    return true;
+}
+
+bool hd_walks_ok(int n_walk, const void* const* epi, const int* n_epi, const pgf_epi_layout* il,
+                 const int* const* id_epj, const int* n_epj, const int* const* id_spj, const int* n_spj, int mode) {
+    if (n_walk <= 0) return true;
+    if (!al8(il->size) || il->size > 4096 || !al8(il->off_pos) || !al8(il->off_r_search)) return false;
+    if (mode == PGF_MODE_GRADIENT && !al8(g.gr.epi_off_acc)) return false;
+    if (mode == PGF_MODE_FORCE_CHANGEOVER && !(al8(g.co.epi_off_id) && al8(g.co.epi_off_r_in) &&
+                                               al8(g.co.epi_off_r_out) && al8(g.co.epi_off_self_mass)))
+        return false;
+    for (int w = 0; w < n_walk; ++w) {
+        if (n_epi[w] > 0 && !al8p(epi[w])) return false;
+        if (n_epj[w] > 0 && (reinterpret_cast<uintptr_t>(id_epj[w]) & 3)) return false;
+        if (n_spj[w] > 0 && (reinterpret_cast<uintptr_t>(id_spj[w]) & 3)) return false;
+    }
+    return true;
+}
+
+bool hd_force_ok(int n_walk, const int* ni, void* const* force, const pgf_force_layout* fl, int mode) {
+    if (n_walk <= 0) return true;
+    if (!al8(fl->size) || !al8(fl->off_acc) || !al8(fl->off_pot) || fl->off_n_ngb % (size_t)fl->n_ngb_bytes)
+        return false;
+    if (mode == PGF_MODE_GRADIENT && !al8(g.gr.force_off_acorr)) return false;
+    if (mode == PGF_MODE_FORCE_CHANGEOVER && !al8(g.co.force_off_pot_soft)) return false;
+    for (int w = 0; w < n_walk; ++w)
+        if (ni[w] > 0 && !al8p(force[w])) return false;
+    return true;
+}
 
 int setup_device(int rank) {
     int ngpu = 0;
@@ -260,8 +311,8 @@ int setup_device(int rank) {
     g.retest_cap = 1 << 20;
     PGF_CUDA(g.retest.ensure((size_t)g.retest_cap));
     PGF_CUDA(cudaMemset(g.scratch.d, 0, kScratchInts * sizeof(int32_t)));
-    PGF_CUDA(g.hd_err.ensure(2 * kMaxTags));
-    PGF_CUDA(cudaMemset(g.hd_err.d, 0, 2 * kMaxTags * sizeof(int32_t)));
+    PGF_CUDA(g.hd_err.ensure(kHdErrWords * kMaxTags));
+    PGF_CUDA(cudaMemset(g.hd_err.d, 0, kHdErrWords * kMaxTags * sizeof(int32_t)));
     g.init = true;
     return PGF_OK;
 }
@@ -431,7 +482,8 @@ int pack_and_send_j(const void* epj, int64_t n_epj, const pgf_epj_layout* el, co
     // either is reused or reallocated.
     PGF_CUDA(cudaStreamSynchronize(g.stream));
     harvest_send();
-    if (use_hd()) return send_j_host_direct(epj, n_epj, el, spj, n_spj, sl);
+    if (use_hd() && hd_send_ok(epj, n_epj, el, spj, n_spj, sl))
+        return send_j_host_direct(epj, n_epj, el, spj, n_spj, sl);
     const double t0 = now_s();
     PGF_CUDA(g.h_epj.ensure(n_epj));
     PGF_CUDA(g.h_epj_m64.ensure(n_epj));
@@ -755,6 +807,28 @@ inline double part_cost(int n_i, int n_epj, int n_spj, int j, int parts) {
     return (double)n_i * ((double)e + 2.0 * (double)s);
 }
 
+// Work-queue order of a dispatch's walks and parts, most expensive first, in
+// linear time: costs are bucketed in eighths of an octave below the largest
+// (the 3 leading mantissa bits and the exponent of the double), and equal
+// buckets keep their layout order.  The order only decides which CTA runs
+// which descriptor, never a result.
+void queue_order(const std::vector<std::pair<double, int>>& cq, int32_t* out) {
+    constexpr int kBuckets = 256;
+    auto key = [](double c) -> int64_t {
+        if (!(c > 0.0)) return 0;
+        int64_t bits;
+        std::memcpy(&bits, &c, sizeof(bits));
+        return bits >> 49;  // exponent and 3 mantissa bits: monotonic in c > 0
+    };
+    int64_t kmax = 0;
+    for (const auto& e : cq) kmax = std::max(kmax, key(e.first));
+    int count[kBuckets + 1] = {};
+    auto bucket = [&](double c) { return (int)std::min<int64_t>(kBuckets - 1, kmax - key(c)); };
+    for (const auto& e : cq) ++count[bucket(e.first) + 1];
+    for (int b = 0; b < kBuckets; ++b) count[b + 1] += count[b];
+    for (const auto& e : cq) out[count[bucket(e.first)]++] = e.second;
+}
+
 // The walk phase of a single-launch index dispatch, host-direct: the host
 // writes one table entry per walk (where its EPI records and id lists lie,
 // where they go, how it splits), and a gather kernel reads the caller's
@@ -767,7 +841,6 @@ int dispatch_host_direct(TagState& t, int n_walk, const std::vector<int32_t>& or
                          const pgf_epi_layout* il, const int* const* id_epj, const int* n_epj,
                          const int* const* id_spj, const int* n_spj, bool co_mode, bool gr_mode, double t0) {
     PGF_CUDA(t.h_src.ensure(n_walk));
-    PGF_CUDA(t.src.ensure(n_walk));
     PGF_CUDA(t.h_hd_err.ensure(2));
     std::vector<int> plan_of(n_walk, -1);
     for (size_t q = 0; q < plan.size(); ++q) plan_of[plan[q].k] = (int)q;
@@ -789,11 +862,14 @@ int dispatch_host_direct(TagState& t, int n_walk, const std::vector<int32_t>& or
         ws.parts = 1;
         ws.desc1 = 0;
         ws.rows1 = 0;
+        ws.split = -1;
+        ws.pad = 0;
         if (plan_of[k] >= 0) {
             const SplitPlan& sp = plan[plan_of[k]];
             ws.parts = sp.parts;
             ws.desc1 = sp.desc1;
             ws.rows1 = sp.rows1;
+            ws.split = plan_of[k];
             for (int j = 1; j < sp.parts; ++j)
                 cq[sp.desc1 + j - 1] = {part_cost(n_epi[w], n_epj[w], n_spj[w], j, sp.parts), sp.desc1 + j - 1};
         }
@@ -803,20 +879,18 @@ int dispatch_host_direct(TagState& t, int n_walk, const std::vector<int32_t>& or
     if (plan.empty()) {
         for (int k = 0; k < n_desc; ++k) t.h_order.h[k] = k;
     } else {
-        std::stable_sort(cq.begin(), cq.end(), [](const std::pair<double, int>& a, const std::pair<double, int>& b) {
-            return a.first > b.first;
-        });
-        for (int k = 0; k < n_desc; ++k) t.h_order.h[k] = cq[k].second;
-        PGF_CUDA(t.h_splits.ensure(plan.size()));
+        queue_order(cq, t.h_order.h);
         PGF_CUDA(t.splits.ensure(plan.size()));
-        for (size_t q = 0; q < plan.size(); ++q) {
-            const SplitPlan& sp = plan[q];
-            t.h_splits.h[q] = SplitRec{(int32_t)off[sp.k].i, (int32_t)sp.rows1, n_epi[ord[sp.k]], sp.parts};
-        }
     }
+    // The gather reads the walk table and the order from pinned host memory
+    // in place and writes the split records itself.
     HdWalkArgs a{};
-    a.src = t.src.d;
+    a.src = t.h_src.h;
     a.n_walk = n_walk;
+    a.n_desc = n_desc;
+    a.order_src = t.h_order.h;
+    a.order_dst = t.order.d;
+    a.out_splits = plan.empty() ? nullptr : t.splits.d;
     a.epi_size = il->size;
     a.epi_off_pos = il->off_pos;
     a.epi_off_rs = il->off_r_search;
@@ -838,30 +912,20 @@ int dispatch_host_direct(TagState& t, int n_walk, const std::vector<int32_t>& or
     a.out_id_spj = t.id_spj.d;
     a.out_walks = t.walks.d;
     const int tag = (int)(&t - g.tags);
-    a.err = g.hd_err.d + 2 * tag;
+    a.err = g.hd_err.d + kHdErrWords * tag;
+    a.err_host = t.h_hd_err.h;
     g.prof.copy += now_s() - t0;
     PGF_CUDA(cudaEventRecord(t.ev[0], g.stream));
-    PGF_CUDA(cudaMemsetAsync(a.err, 0, 2 * sizeof(int32_t), g.stream));
-    PGF_CUDA(cudaMemcpyAsync(t.src.d, t.h_src.h, n_walk * sizeof(WalkSrc), cudaMemcpyHostToDevice, g.stream));
     {
         const cudaError_t e = launch_gather_walks(a, g.num_sms, g.stream);
         if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "walk gather kernel failed: %s", cudaGetErrorString(e));
     }
-    PGF_CUDA(cudaMemcpyAsync(t.h_hd_err.h, a.err, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, g.stream));
     PGF_CUDA(cudaEventRecord(t.ev_in, g.stream));
     // The force kernels are queued right behind the gather, with no host
-    // round trip between: they read the check's result themselves and run
+    // round trip between: they read the check's verdict themselves and run
     // nothing when an id was out of range.
-    t.params.input_err = a.err;
-    PGF_CUDA(cudaMemcpyAsync(t.order.d, t.h_order.h, n_desc * sizeof(int32_t), cudaMemcpyHostToDevice, g.stream));
-    if (!plan.empty()) {
-        PGF_CUDA(cudaMemcpyAsync(t.splits.d, t.h_splits.h, plan.size() * sizeof(SplitRec), cudaMemcpyHostToDevice,
-                                 g.stream));
-        const cudaError_t e = launch_split_rows(t.splits.d, (int)plan.size(), t.epi.d, co_mode ? t.epi_co.d : nullptr,
-                                                gr_mode ? t.epi_acc.d : nullptr, g.stream);
-        if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "split rows kernel failed: %s", cudaGetErrorString(e));
-        t.n_split = (int)plan.size();
-    }
+    t.params.input_err = a.err + 3;
+    t.n_split = (int)plan.size();
     if (int r = launch_tag(t)) return r;
     // The caller's arrays are only valid during the call: return once the
     // gather has read them, with the check's verdict.
@@ -929,6 +993,8 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     // share the remainder equally.
     int n_chunks = g.stages > 0 ? g.stages : (int)std::min<int64_t>(kMaxChunks, (ne + ns) / kChunkIdEntries + 1);
     if (n_walk < 8 * n_chunks) n_chunks = 1;
+    const bool hd_single =
+        n_chunks == 1 && use_hd() && hd_walks_ok(n_walk, epi, n_epi, il, id_epj, n_epj, id_spj, n_spj, t.mode);
 
     // Split plan.  In a single launch the most expensive walks bound the
     // launch time when there are few walks per CTA.  The unit is an eighth
@@ -967,17 +1033,16 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     }
     t.n_split = 0;
     if (gr_mode) {
-        if (!(n_chunks == 1 && use_hd())) PGF_CUDA(t.h_epi_acc.ensure(ni));
+        if (!hd_single) PGF_CUDA(t.h_epi_acc.ensure(ni));
         PGF_CUDA(t.epi_acc.ensure(ni_all));
         PGF_CUDA(t.acorr.ensure(ni_all));
     }
     if (co_mode) {
-        if (!(n_chunks == 1 && use_hd())) PGF_CUDA(t.h_epi_co.ensure(ni));
+        if (!hd_single) PGF_CUDA(t.h_epi_co.ensure(ni));
         PGF_CUDA(t.epi_co.ensure(ni_all));
         PGF_CUDA(t.pot_soft.ensure(ni_all));
     }
 
-    const bool hd_single = n_chunks == 1 && use_hd();
     if (!hd_single) {  // pinned staging of the host packing
         PGF_CUDA(t.h_epi.ensure(ni));
         PGF_CUDA(t.h_id_epj.ensure(ne));
@@ -1080,7 +1145,7 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
         return PGF_OK;
     };
 
-    if (n_chunks == 1 && use_hd()) {
+    if (hd_single) {
         t.ord = ord;
         return dispatch_host_direct(t, n_walk, ord, off, plan, n_desc, epi, n_epi, il, id_epj, n_epj, id_spj, n_spj,
                                     co_mode, gr_mode, t0);
@@ -1126,10 +1191,7 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
                 const WalkDesc& d = t.h_walks.h[k];
                 cq[k] = {(double)d.n_i * ((double)d.n_epj + 2.0 * (double)d.n_spj), k};
             }
-            std::stable_sort(cq.begin(), cq.end(), [](const std::pair<double, int>& a, const std::pair<double, int>& b) {
-                return a.first > b.first;
-            });
-            for (int k = 0; k < n_desc; ++k) t.h_order.h[k] = cq[k].second;
+            queue_order(cq, t.h_order.h);
         }
         g.prof.copy += now_s() - t0;
         PGF_CUDA(cudaEventRecord(t.ev[0], g.stream));
@@ -1541,7 +1603,6 @@ int copy_back(TagState& t, int64_t r0, int64_t r1, cudaStream_t s) {
 // back or unpacked on the host.
 int retrieve_host_direct(TagState& t, int n_walk, const int* ni, void* const* force, const pgf_force_layout* fl) {
     PGF_CUDA(t.h_dst.ensure(n_walk));
-    PGF_CUDA(t.dst.ensure(n_walk));
     for (int k = 0; k < n_walk; ++k) {
         const int w = t.ord[k];
         t.h_dst.h[k] = ForceDst{static_cast<char*>(force[w]), t.epi_disp[w], ni[w], 0};
@@ -1563,20 +1624,18 @@ int retrieve_host_direct(TagState& t, int n_walk, const int* ni, void* const* fo
         a.acorr = t.acorr.d;
         a.off_acorr = g.gr.force_off_acorr;
     }
-    auto scatter = [&](int k0, int k1, cudaStream_t st) -> int {
-        HdScatterArgs b = a;
-        b.dst = t.dst.d + k0;
-        b.n_walk = k1 - k0;
-        const cudaError_t e = launch_scatter_results(b, g.num_sms, st);
-        if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "result scatter kernel failed: %s", cudaGetErrorString(e));
-        return PGF_OK;
-    };
+    // The scatter reads the destination table from pinned host memory in
+    // place and moves the status words into t.h_flags itself.
+    a.dst = t.h_dst.h;
+    a.n_walk = n_walk;
+    a.flags_dev = g.scratch.d;
+    a.flags_host = t.h_flags.h;
     cudaStream_t st = g.stream;
-    PGF_CUDA(cudaMemcpyAsync(t.dst.d, t.h_dst.h, n_walk * sizeof(ForceDst), cudaMemcpyHostToDevice, st));
     PGF_CUDA(cudaEventRecord(t.ev[4], st));
-    if (int r = scatter(0, n_walk, st)) return r;
-    PGF_CUDA(cudaMemcpyAsync(t.h_flags.h, g.scratch.d, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    PGF_CUDA(cudaMemsetAsync(g.scratch.d + 2, 0, 2 * sizeof(int32_t), st));
+    {
+        const cudaError_t e = launch_scatter_results(a, g.num_sms, st);
+        if (e != cudaSuccess) return fail(PGF_ERR_CUDA, "result scatter kernel failed: %s", cudaGetErrorString(e));
+    }
     PGF_CUDA(cudaEventRecord(t.ev[5], st));
     PGF_CUDA(cudaEventSynchronize(t.ev[5]));
     t.dispatched = false;
@@ -1608,7 +1667,8 @@ int pgf_retrieve(int tag, int n_walk, const int* ni, void* const* force, const p
     // Host-direct results for single launches.  A pipelined dispatch keeps
     // the copy-engine copies and host unpacking per stage: those overlap the
     // later stages' kernels, where a scatter kernel would wait for their SMs.
-    if (use_hd() && t.n_chunks == 0) return retrieve_host_direct(t, n_walk, ni, force, fl);
+    if (use_hd() && t.n_chunks == 0 && hd_force_ok(n_walk, ni, force, fl, t.mode))
+        return retrieve_host_direct(t, n_walk, ni, force, fl);
     PGF_CUDA(t.h_accp.ensure(n));
     PGF_CUDA(t.h_nnb.ensure(n));
     if (t.mode == PGF_MODE_GRADIENT) PGF_CUDA(t.h_acorr.ensure(n));
@@ -1730,6 +1790,11 @@ int pgf_finalize(void) {
         t.h_epi_acc.release();
         t.acorr.release();
         t.h_acorr.release();
+        t.splits.release();
+        t.h_splits.release();
+        t.h_src.release();
+        t.h_dst.release();
+        t.h_hd_err.release();
         if (t.ev_in) cudaEventDestroy(t.ev_in);
         t.ev_in = nullptr;
         for (auto& ev : t.ev) {

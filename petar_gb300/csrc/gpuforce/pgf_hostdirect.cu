@@ -136,52 +136,138 @@ __global__ __launch_bounds__(256) void gather_j_kernel(HdSendArgs a) {
     }
 }
 
-// One CTA per walk (grid-stride over walks): EPI rows, the walk's box and
-// descriptor(s), and its id lists, checked against the sent arrays.
+// One CTA per walk (grid-stride over walks): EPI rows (with the copies that
+// the parts of a split walk read), the walk's box and descriptor(s), and its
+// id lists, checked against the sent arrays.  Host memory answers in
+// microseconds and serves whole lines best, so a CTA reads a walk's EPI
+// records as contiguous 8-byte words into shared memory (up to kEpiWords per
+// round) and its id lists as contiguous 4-byte words, and each thread issues
+// all its loads of a round before its first store.  The host sends only
+// 8-byte aligned records whose size and offsets are multiples of 8, at most
+// 4 KB each.  The CTAs also copy the work-queue order from the pinned host
+// table, and the last CTA to finish publishes the id check's verdict.
 constexpr int kGatherThreads = 256;
+constexpr int kIdBatch = 8;
+constexpr int kIdParts = 4;  // CTAs per walk for the id lists
+constexpr int kEpiWords = 3072;
+constexpr int kEpiPerThread = kEpiWords / kGatherThreads;
+
+__device__ __forceinline__ void write_rows(const HdWalkArgs& a, const WalkSrc& w, int i, const EpiDev& e,
+                                           const Accp& ac, const CoRec& co) {
+    for (int j = 0; j < w.parts; ++j) {
+        const int64_t row = j == 0 ? w.i_off + i : w.rows1 + (int64_t)(j - 1) * w.n_i + i;
+        a.out_epi[row] = e;
+        if (a.out_epi_acc) a.out_epi_acc[row] = ac;
+        if (a.out_epi_co) a.out_epi_co[row] = co;
+    }
+}
+
+// Loads the 8-byte words [0, n) of src, kEpiPerThread per thread.
+__device__ __forceinline__ void load_words(const uint64_t* src, int n, uint64_t (&v)[kEpiPerThread]) {
+#pragma unroll
+    for (int u = 0; u < kEpiPerThread; ++u) {
+        const int q = u * kGatherThreads + (int)threadIdx.x;
+        v[u] = q < n ? src[q] : 0ull;
+    }
+}
 
 __global__ __launch_bounds__(kGatherThreads) void gather_walks_kernel(HdWalkArgs a) {
     __shared__ double red[7][kGatherThreads];
+    __shared__ uint64_t ebuf[kEpiWords];
+    __shared__ uint64_t wsrc[sizeof(WalkSrc) / 8];
     __shared__ unsigned bad;
+    static_assert(sizeof(WalkSrc) % 8 == 0 && sizeof(WalkSrc) / 8 <= kGatherThreads, "walk table entry");
     const int t = threadIdx.x;
-    for (int k = blockIdx.x; k < a.n_walk; k += gridDim.x) {
-        const WalkSrc w = a.src[k];
+    for (int q = blockIdx.x * kGatherThreads + t; q < a.n_desc; q += gridDim.x * kGatherThreads)
+        a.order_dst[q] = a.order_src[q];
+    const int per_round = a.epi_size ? (int)((size_t)kEpiWords * 8 / a.epi_size) : 1;
+    // Unit c = (walk c / kIdParts, slice c % kIdParts of its id lists); the
+    // slice-0 unit also does the walk's EPI rows and descriptors.
+    const int64_t n_units = (int64_t)a.n_walk * kIdParts;
+    for (int64_t c = blockIdx.x; c < n_units; c += gridDim.x) {
+        const int k = (int)(c / kIdParts), part = (int)(c - (int64_t)k * kIdParts);
+        if (t < (int)(sizeof(WalkSrc) / 8)) wsrc[t] = reinterpret_cast<const uint64_t*>(a.src + k)[t];
         if (t == 0) bad = 0;
-        double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL}, rs_max = 0.0;
-        for (int i = t; i < w.n_i; i += kGatherThreads) {
-            const char* r = w.epi + (int64_t)i * (int64_t)a.epi_size;
-            const double* p = dptr(r, a.epi_off_pos);
-            EpiDev e{p[0], p[1], p[2], *dptr(r, a.epi_off_rs)};
-            const int64_t row = w.i_off + i;
-            a.out_epi[row] = e;
-            if (a.out_epi_acc) {
-                const double* ac = dptr(r, a.gr_epi_off_acc);
-                a.out_epi_acc[row] = Accp{ac[0], ac[1], ac[2], 0.0};
-            }
-            if (a.out_epi_co) {
-                int64_t id;
-                memcpy(&id, r + a.co_epi_off_id, sizeof(id));
-                a.out_epi_co[row] = make_co_dev(*dptr(r, a.co_epi_off_r_in), *dptr(r, a.co_epi_off_r_out),
-                                                *dptr(r, a.co_epi_off_self_mass), id);
-            }
-            rs_max = fmax(rs_max, e.rs);
-            lo[0] = fmin(lo[0], e.x);
-            lo[1] = fmin(lo[1], e.y);
-            lo[2] = fmin(lo[2], e.z);
-            hi[0] = fmax(hi[0], e.x);
-            hi[1] = fmax(hi[1], e.y);
-            hi[2] = fmax(hi[2], e.z);
-        }
+        __syncthreads();
+        const WalkSrc w = *reinterpret_cast<const WalkSrc*>(wsrc);
+        // First round of EPI words in flight while the id lists are copied.
+        uint64_t ev[kEpiPerThread];
+        const int n0 = part != 0 ? 0 : (w.n_i < per_round ? w.n_i : per_round);
+        load_words(reinterpret_cast<const uint64_t*>(w.epi), (int)((size_t)n0 * a.epi_size / 8), ev);
         unsigned b = 0;
-        for (int q = t; q < w.n_epj; q += kGatherThreads) {
-            const int32_t v = w.id_epj[q];
-            b |= (unsigned)v >= (unsigned)a.n_epj_tot;
-            a.out_id_epj[w.e_off + q] = v;
+        const int e0 = (int)((int64_t)w.n_epj * part / kIdParts), e1 = (int)((int64_t)w.n_epj * (part + 1) / kIdParts);
+        const int s0 = (int)((int64_t)w.n_spj * part / kIdParts), s1 = (int)((int64_t)w.n_spj * (part + 1) / kIdParts);
+        const int n_id = e1 - e0 > s1 - s0 ? e1 - e0 : s1 - s0;
+        for (int q0 = 0; q0 < n_id; q0 += kIdBatch * kGatherThreads) {
+            int32_t ve[kIdBatch], vs[kIdBatch];
+#pragma unroll
+            for (int u = 0; u < kIdBatch; ++u) {
+                const int q = q0 + u * kGatherThreads + t;
+                ve[u] = e0 + q < e1 ? w.id_epj[e0 + q] : 0;
+                vs[u] = s0 + q < s1 ? w.id_spj[s0 + q] : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < kIdBatch; ++u) {
+                const int q = q0 + u * kGatherThreads + t;
+                if (e0 + q < e1) {
+                    b |= (unsigned)ve[u] >= (unsigned)a.n_epj_tot;
+                    a.out_id_epj[w.e_off + e0 + q] = ve[u];
+                }
+                if (s0 + q < s1) {
+                    b |= (unsigned)vs[u] >= (unsigned)a.n_spj_tot;
+                    a.out_id_spj[w.s_off + s0 + q] = vs[u];
+                }
+            }
         }
-        for (int q = t; q < w.n_spj; q += kGatherThreads) {
-            const int32_t v = w.id_spj[q];
-            b |= (unsigned)v >= (unsigned)a.n_spj_tot;
-            a.out_id_spj[w.s_off + q] = v;
+        if (b) atomicOr(&bad, 1u);
+        __syncthreads();
+        if (t == 0 && bad) {
+            atomicOr(a.err, 1);
+            atomicMax(a.err + 1, w.walk);
+        }
+        if (part != 0) {
+            __syncthreads();  // wsrc and bad are rewritten by the next unit
+            continue;
+        }
+        double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL}, rs_max = 0.0;
+        for (int i0 = 0; i0 < w.n_i; i0 += per_round) {
+            const int nr = w.n_i - i0 < per_round ? w.n_i - i0 : per_round;
+            const int nw = (int)((size_t)nr * a.epi_size / 8);
+            if (i0 > 0) {
+                __syncthreads();  // the previous round's records are parsed
+                load_words(reinterpret_cast<const uint64_t*>(w.epi + (size_t)i0 * a.epi_size), nw, ev);
+            }
+#pragma unroll
+            for (int u = 0; u < kEpiPerThread; ++u) {
+                const int q = u * kGatherThreads + t;
+                if (q < nw) ebuf[q] = ev[u];
+            }
+            __syncthreads();
+            for (int i = t; i < nr; i += kGatherThreads) {
+                const char* r = reinterpret_cast<const char*>(ebuf) + (size_t)i * a.epi_size;
+                const double* p = dptr(r, a.epi_off_pos);
+                const EpiDev e{p[0], p[1], p[2], *dptr(r, a.epi_off_rs)};
+                Accp ac{0.0, 0.0, 0.0, 0.0};
+                if (a.out_epi_acc) {
+                    const double* q = dptr(r, a.gr_epi_off_acc);
+                    ac = Accp{q[0], q[1], q[2], 0.0};
+                }
+                CoRec co{};
+                if (a.out_epi_co) {
+                    int64_t id;
+                    memcpy(&id, r + a.co_epi_off_id, sizeof(id));
+                    co = make_co_dev(*dptr(r, a.co_epi_off_r_in), *dptr(r, a.co_epi_off_r_out),
+                                     *dptr(r, a.co_epi_off_self_mass), id);
+                }
+                write_rows(a, w, i0 + i, e, ac, co);
+                rs_max = fmax(rs_max, e.rs);
+                lo[0] = fmin(lo[0], e.x);
+                lo[1] = fmin(lo[1], e.y);
+                lo[2] = fmin(lo[2], e.z);
+                hi[0] = fmax(hi[0], e.x);
+                hi[1] = fmax(hi[1], e.y);
+                hi[2] = fmax(hi[2], e.z);
+            }
         }
         for (int d = 0; d < 3; ++d) {
             red[d][t] = lo[d];
@@ -189,7 +275,6 @@ __global__ __launch_bounds__(kGatherThreads) void gather_walks_kernel(HdWalkArgs
         }
         red[6][t] = rs_max;
         __syncthreads();
-        if (b) atomicOr(&bad, 1u);
         for (int s = kGatherThreads / 2; s > 0; s >>= 1) {
             if (t < s) {
                 for (int d = 0; d < 3; ++d) {
@@ -201,10 +286,6 @@ __global__ __launch_bounds__(kGatherThreads) void gather_walks_kernel(HdWalkArgs
             __syncthreads();
         }
         if (t == 0) {
-            if (bad) {
-                atomicOr(a.err, 1);
-                atomicMax(a.err + 1, w.walk);
-            }
             WalkDesc d;
             d.epj_begin = w.e_off;
             d.spj_begin = w.s_off;
@@ -249,8 +330,21 @@ __global__ __launch_bounds__(kGatherThreads) void gather_walks_kernel(HdWalkArgs
                     a.out_walks[w.desc1 + j - 1] = q;
                 }
             }
+            if (w.parts > 1) a.out_splits[w.split] = SplitRec{(int32_t)w.i_off, (int32_t)w.rows1, w.n_i, w.parts};
         }
         __syncthreads();
+    }
+    // The verdict: the last CTA to finish sees every CTA's atomics.
+    if (t == 0) {
+        __threadfence();
+        if (atomicAdd(a.err + 2, 1) == (int)gridDim.x - 1) {
+            __threadfence();
+            const int32_t f = atomicExch(a.err, 0), wmax = atomicExch(a.err + 1, 0);
+            a.err[2] = 0;
+            a.err[3] = f;
+            a.err_host[0] = f;
+            a.err_host[1] = wmax;
+        }
     }
 }
 
@@ -258,6 +352,11 @@ __global__ __launch_bounds__(kGatherThreads) void gather_walks_kernel(HdWalkArgs
 // (4 or 8 bytes) and the modes' extra fields, overwritten as RetrieveForceCUDA
 // does (src/force_gpu_cuda.cu:866-875).
 __global__ __launch_bounds__(256) void scatter_results_kernel(HdScatterArgs a) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        for (int q = 0; q < 4; ++q) a.flags_host[q] = a.flags_dev[q];
+        a.flags_dev[2] = 0;
+        a.flags_dev[3] = 0;
+    }
     for (int k = blockIdx.x; k < a.n_walk; k += gridDim.x) {
         const ForceDst f = a.dst[k];
         for (int i = threadIdx.x; i < f.n; i += blockDim.x) {
@@ -304,15 +403,16 @@ cudaError_t launch_gather_j(const HdSendArgs& a, int num_sms, cudaStream_t s) {
 }
 
 cudaError_t launch_gather_walks(const HdWalkArgs& a, int num_sms, cudaStream_t s) {
-    if (a.n_walk <= 0) return cudaSuccess;
-    const int grid = a.n_walk < num_sms * 8 ? a.n_walk : num_sms * 8;
+    const int64_t units = (int64_t)a.n_walk * kIdParts;
+    int grid = units < num_sms * 8 ? (int)units : num_sms * 8;
+    if (grid < 1) grid = 1;  // the verdict is published even with no walk
     gather_walks_kernel<<<grid, kGatherThreads, 0, s>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_scatter_results(const HdScatterArgs& a, int num_sms, cudaStream_t s) {
-    if (a.n_walk <= 0) return cudaSuccess;
-    const int grid = a.n_walk < num_sms * 8 ? a.n_walk : num_sms * 8;
+    int grid = a.n_walk < num_sms * 8 ? a.n_walk : num_sms * 8;
+    if (grid < 1) grid = 1;  // the status words move even with no walk
     scatter_results_kernel<<<grid, 256, 0, s>>>(a);
     return cudaGetLastError();
 }

@@ -249,6 +249,8 @@ struct WalkSrc {
     int32_t walk;           // the caller's walk index (error reports)
     int32_t parts;          // 1, or the parts of a split walk
     int32_t desc1;          // split walks: descriptor index of part 1
+    int32_t split;          // split walks: index of its SplitRec
+    int32_t pad;
 };
 
 // Where retrieve writes walk k's results.
@@ -283,9 +285,12 @@ struct HdSendArgs {
 };
 
 struct HdWalkArgs {
-    const WalkSrc* src;
+    const WalkSrc* src;         // pinned host table, read in place
     int n_walk;
-    int pad;
+    int n_desc;                 // work-queue entries (walks and parts)
+    const int32_t* order_src;   // pinned host work-queue order, copied to order_dst
+    int32_t* order_dst;
+    SplitRec* out_splits;       // split walks' records (combine kernel)
     size_t epi_size, epi_off_pos, epi_off_rs;
     size_t gr_epi_off_acc;  // gradient mode (out_epi_acc non-null)
     size_t co_epi_off_id, co_epi_off_r_in, co_epi_off_r_out, co_epi_off_self_mass;  // changeover (out_epi_co)
@@ -296,7 +301,12 @@ struct HdWalkArgs {
     int32_t* out_id_epj;
     int32_t* out_id_spj;
     WalkDesc* out_walks;
-    int32_t* err;  // [0] set when an id is out of range, [1] the largest such caller walk index
+    // [0] set when an id is out of range, [1] the largest such caller walk
+    // index, [2] finished CTAs, [3] the verdict the force kernels read.  The
+    // last CTA moves [0], [1] into err_host[0], [1] (pinned) and [3], and
+    // clears [0..2] for the next dispatch.
+    int32_t* err;
+    int32_t* err_host;
 };
 
 struct HdScatterArgs {
@@ -311,6 +321,10 @@ struct HdScatterArgs {
     const int32_t* nnb;
     const double* pot_soft;  // changeover mode, else null
     const Accp* acorr;       // gradient mode, else null
+    // Status words of the evaluation (the device error word and the re-test
+    // total at [2], [3]): copied to flags_host and cleared by the kernel.
+    int32_t* flags_dev;
+    int32_t* flags_host;
 };
 
 cudaError_t launch_gather_j(const HdSendArgs& a, int num_sms, cudaStream_t s);
