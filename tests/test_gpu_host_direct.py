@@ -122,3 +122,46 @@ def test_bad_id_rejected_before_any_force_kernel():
         wb.id_epj = good
     res = gpuforce.compute(wb)
     assert_mixed_parity(res["acc"], res["pot"], res["nnb"], oracle.force(wb), label="after bad id")
+
+
+def test_packed_records_take_the_host_path():
+    """Packed record types (FP64 fields at 4-byte offsets) are not read or
+    written in place by the GPU: send, dispatch and retrieve fall back to the
+    host packing, and the results equal the staged path's bit for bit."""
+    wb = walks.build_walks(ics.make_plummer_cluster(41, 40000, 0.006, binary_fraction=0.5))
+    epi_dt = np.dtype([("tag", "<i4"), ("id", "<i8"), ("pos", "<f8", 3), ("r_search", "<f8")])
+    epj_dt = np.dtype([("tag", "<i4"), ("id", "<i8"), ("mass", "<f8"), ("pos", "<f8", 3), ("r_search", "<f8")])
+    spj_dt = np.dtype([("tag", "<i4"), ("mass", "<f8"), ("pos", "<f8", 3), ("quad", "<f8", 6)])
+    force_dt = np.dtype([("tag", "<i4"), ("acc", "<f8", 3), ("pot", "<f8"), ("n_ngb", "<i8")])
+    assert epi_dt.fields["pos"][1] % 8 and force_dt.fields["acc"][1] % 8
+    ni = wb.epi_rs.size
+    epi = np.zeros(ni, epi_dt)
+    epi["pos"], epi["r_search"], epi["id"] = wb.epi_pos, wb.epi_rs, np.arange(ni)
+    epj = np.zeros(wb.epj_mass.size, epj_dt)
+    epj["mass"], epj["pos"], epj["r_search"] = wb.epj_mass, wb.epj_pos, wb.epj_rs
+    spj = np.zeros(wb.spj_mass.size, spj_dt)
+    spj["mass"], spj["pos"], spj["quad"] = wb.spj_mass, wb.spj_pos, wb.spj_quad
+    id_epj = np.ascontiguousarray(wb.id_epj, np.int32)
+    id_spj = np.ascontiguousarray(wb.id_spj, np.int32)
+    n_epi = np.diff(wb.epi_disp).astype(np.int32)
+    n_epj = np.diff(wb.epj_disp).astype(np.int32)
+    n_spj = np.diff(wb.spj_disp).astype(np.int32)
+    p_epi = [epi[wb.epi_disp[w]:wb.epi_disp[w + 1]] for w in range(wb.n_walk)]
+    p_id_epj = [id_epj[wb.epj_disp[w]:wb.epj_disp[w + 1]] for w in range(wb.n_walk)]
+    p_id_spj = [id_spj[wb.spj_disp[w]:wb.spj_disp[w + 1]] for w in range(wb.n_walk)]
+
+    def run():
+        f = gpuforce.CalcForceWithLinearCutoffCUDAMultiWalk(0, wb.eps2, wb.rcut2, wb.G)
+        f(0, 0, None, None, None, None, None, None, epj, epj.size, spj, spj.size, True)
+        f(0, wb.n_walk, p_epi, n_epi, p_id_epj, n_epj, p_id_spj, n_spj, epj, epj.size, spj, spj.size, False)
+        force = np.zeros(ni, force_dt)
+        force["tag"] = 31
+        parts = [force[wb.epi_disp[w]:wb.epi_disp[w + 1]] for w in range(wb.n_walk)]
+        gpuforce.RetrieveForceCUDA(0, wb.n_walk, n_epi, parts, force_dtype=force_dt)
+        return force
+
+    a, b = both(run)
+    for k in force_dt.names:
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    assert (b["tag"] == 31).all()
+    assert_mixed_parity(b["acc"], b["pot"], b["n_ngb"], oracle.force(wb), label="packed records")
