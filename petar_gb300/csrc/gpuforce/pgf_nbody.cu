@@ -91,6 +91,7 @@ struct TreeHdr {
     int32_t cursor[kBuckets];
     int32_t sample_slot;  // next record slot of the per-step sample
     int32_t pad2;
+    unsigned long long walk_cursor[2];  // next task of the count and fill passes
 };
 
 // Cell fields the walk reads.
@@ -112,7 +113,7 @@ struct __align__(16) TCellW {
     float in_lo[3], in_hi[3];
     float out_lo[3], out_hi[3];
     int32_t begin, end, first_child, n_child;
-    int32_t leaf, parent, pad0, pad1;
+    int32_t leaf, parent, level, pad1;
 };
 static_assert(sizeof(TCellW) == 96, "TCellW layout");
 
@@ -558,7 +559,8 @@ __global__ __launch_bounds__(256) void moments_kernel(const TreeHdr* h, TCell* c
         w.n_child = cc.n_child;
         w.leaf = cc.leaf;
         w.parent = cc.parent;
-        w.pad0 = w.pad1 = 0;
+        w.level = cc.level;
+        w.pad1 = 0;
         cw[c] = w;
         CMom& o = mom[c];
         o.m = m;
@@ -800,43 +802,55 @@ __device__ void walk_subtree(const WalkCtx& x, int f, const TCellW& fw, int& ne,
 // Frontier cells f0 .. f1-1 (consecutive in frontier order) for one group.
 // A frontier cell is walked if the group opens all its ancestors; a closed
 // ancestor ends it and is listed by the frontier cell that starts its range.
-// The decisions along the current ancestor chain are kept, so consecutive
-// frontier cells test only the ancestors they do not share.
+// The decisions along the current ancestor chain are kept by level, so a
+// frontier cell climbs its parent links only up to the deepest ancestor it
+// shares with the previous one (cells are in Morton order, so an ancestor of
+// two frontier cells is an ancestor of every frontier cell between them) and
+// tests only the ancestors below it.
 template <bool FILL>
 __device__ void walk_chunk(const WalkCtx& x, const int32_t* __restrict__ fronts, int f0, int f1, int& ne, int& ns,
                            int32_t* __restrict__ oe, int32_t* __restrict__ os) {
     ne = ns = 0;
-    int cache_c[kLevels];
-    bool cache_open[kLevels];
-    int n_cached = 0;
+    int cache_c[kLevels];        // ancestor of the current chain at each level, all tested
+    int n_cached = 0;            // levels [0, n_cached) are valid
+    int first_closed = kLevels;  // the closed one among them (only the last can be)
     for (int fi = f0; fi < f1; ++fi) {
         const int f = fronts[fi];
         const TCellW fw = x.cw[f];
-        int chain[kLevels];  // ancestors, parent first
-        int na = 0;
-        for (int c = fw.parent; c >= 0 && na < kLevels; c = x.cw[c].parent) chain[na++] = c;
-        bool closed = false;
-        for (int k = 0; k < na; ++k) {  // root first
-            const int a = chain[na - 1 - k];
-            bool op;
-            if (k < n_cached && cache_c[k] == a) {
-                op = cache_open[k];
-            } else {
-                op = open_cell(x, a, x.cw[a]);
-                cache_c[k] = a;
-                cache_open[k] = op;
-                n_cached = k + 1;
-            }
-            if (!op) {
-                if (fw.begin == x.cw[a].begin) {
-                    if (FILL) os[ns] = a;
-                    ++ns;
+        // Climb to the deepest cached ancestor; the others are new.
+        int fresh[kLevels];  // new ancestors, deepest first
+        int nf = 0;
+        int c = fw.parent, lvl = fw.level - 1;
+        while (c >= 0 && !(lvl < n_cached && cache_c[lvl] == c)) {
+            fresh[nf++] = c;
+            c = x.cw[c].parent;
+            --lvl;
+        }
+        n_cached = lvl + 1;
+        if (first_closed >= n_cached) first_closed = kLevels;
+        int closed_at = -1;
+        if (first_closed < kLevels) {
+            closed_at = cache_c[first_closed];
+        } else {
+            for (int k = nf - 1; k >= 0; --k) {  // root side first
+                const int a = fresh[k];
+                const bool op = open_cell(x, a, x.cw[a]);
+                cache_c[n_cached++] = a;
+                if (!op) {
+                    first_closed = n_cached - 1;
+                    closed_at = a;
+                    break;
                 }
-                closed = true;
-                break;
             }
         }
-        if (!closed) walk_subtree<FILL>(x, f, fw, ne, ns, oe, os);
+        if (closed_at >= 0) {
+            if (fw.begin == x.cw[closed_at].begin) {
+                if (FILL) os[ns] = closed_at;
+                ++ns;
+            }
+            continue;
+        }
+        walk_subtree<FILL>(x, f, fw, ne, ns, oe, os);
     }
 }
 
@@ -851,14 +865,27 @@ constexpr int kChunk = 8;  // frontier cells per task
 __device__ __forceinline__ int64_t n_chunks(const TreeHdr* h) { return (h->n_fronts + kChunk - 1) / kChunk; }
 
 __global__ void task_check_kernel(TreeHdr* h, int64_t cap_tasks) {
-    if (threadIdx.x != 0 || h->err) return;
+    if (threadIdx.x != 0) return;
+    h->walk_cursor[0] = h->walk_cursor[1] = 0;
+    if (h->err) return;
     if ((int64_t)h->n_groups * n_chunks(h) > cap_tasks) h->err |= kErrTasks;
+}
+
+// The walk passes take tasks a warp at a time from a counter: task costs
+// differ by orders of magnitude (a chunk next to the group against one whose
+// ancestors the group closes), so a static split leaves SMs idle at the end.
+// Lane l of a warp takes task base + l, so a warp walks one chunk for 32
+// neighbouring groups.
+__device__ __forceinline__ int64_t next_tasks(unsigned long long* cursor) {
+    unsigned long long base = 0;
+    if ((threadIdx.x & 31) == 0) base = atomicAdd(cursor, 32ull);
+    return (int64_t)__shfl_sync(0xffffffffu, base, 0);
 }
 
 // Task t = (chunk q = t / n_groups, group g = t % n_groups) walks frontier
 // cells kChunk q .. kChunk q + kChunk - 1 for group g: the threads of a warp
 // walk the same subtrees for neighbouring groups.  Counts are stored at t.
-__global__ __launch_bounds__(128) void walk_task_count_kernel(const TreeHdr* h, const TCellW* __restrict__ cw,
+__global__ __launch_bounds__(128) void walk_task_count_kernel(TreeHdr* h, const TCellW* __restrict__ cw,
                                                               const TCell* __restrict__ cells,
                                                               const int32_t* __restrict__ groups,
                                                               const int32_t* __restrict__ fronts, int32_t* task_e,
@@ -866,7 +893,10 @@ __global__ __launch_bounds__(128) void walk_task_count_kernel(const TreeHdr* h, 
     if (h->err) return;
     const int64_t ng = h->n_groups, nf = h->n_fronts, T = ng * n_chunks(h);
     const float X = h->xmax;
-    for (int64_t t = gtid(); t < T; t += gstride()) {
+    for (;;) {
+        const int64_t t = next_tasks(&h->walk_cursor[0]) + (threadIdx.x & 31);
+        if (t - (threadIdx.x & 31) >= T) break;
+        if (t >= T) continue;
         const int q = (int)(t / ng), g = (int)(t - (int64_t)q * ng);
         WalkCtx x;
         load_ctx(x, cw, cells, groups[g], X, open_all);
@@ -972,7 +1002,7 @@ __global__ __launch_bounds__(kScanThreads) void walk_scan_kernel(TreeHdr* h, Wal
     }
 }
 
-__global__ __launch_bounds__(128) void walk_task_fill_kernel(const TreeHdr* h, const TCellW* __restrict__ cw,
+__global__ __launch_bounds__(128) void walk_task_fill_kernel(TreeHdr* h, const TCellW* __restrict__ cw,
                                                              const TCell* __restrict__ cells,
                                                              const int32_t* __restrict__ groups,
                                                              const int32_t* __restrict__ fronts,
@@ -983,7 +1013,10 @@ __global__ __launch_bounds__(128) void walk_task_fill_kernel(const TreeHdr* h, c
     if (h->err) return;
     const int64_t ng = h->n_groups, nf = h->n_fronts, T = ng * n_chunks(h);
     const float X = h->xmax;
-    for (int64_t t = gtid(); t < T; t += gstride()) {
+    for (;;) {
+        const int64_t t = next_tasks(&h->walk_cursor[1]) + (threadIdx.x & 31);
+        if (t - (threadIdx.x & 31) >= T) break;
+        if (t >= T) continue;
         const int q = (int)(t / ng), g = (int)(t - (int64_t)q * ng);
         WalkCtx x;
         load_ctx(x, cw, cells, groups[g], X, open_all);
