@@ -36,8 +36,9 @@
 // creation with room to grow; a build that would overflow any capacity sets
 // an error bit, runs no force kernel and the host reports PGF_ERR_CAPACITY.
 //
-// The walks run as one thread per (group, run of 8 frontier cells).  The
-// frontier cells are the topmost cells with at most n / 1024 particles (or
+// The walks run as one thread per (group, pair of frontier cells), taken a
+// warp at a time from a counter.  The frontier cells are the topmost cells
+// with at most n / 512 particles (at least n_group_limit) (or
 // leaves); they partition the particles in Morton order, so the depth-first
 // list of a group is the concatenation, in frontier order, of the lists of
 // the frontier subtrees (a cell above the frontier that the group does not
@@ -860,7 +861,7 @@ __device__ __forceinline__ int cost_bucket(float cost) {
     return b < kBuckets ? b : kBuckets - 1;
 }
 
-constexpr int kChunk = 8;  // frontier cells per task
+constexpr int kChunk = 2;  // frontier cells per task
 
 __device__ __forceinline__ int64_t n_chunks(const TreeHdr* h) { return (h->n_fronts + kChunk - 1) / kChunk; }
 
@@ -1677,7 +1678,7 @@ int pgf_nbody_create(const pgf_nbody_config* cfg, int64_t n, const double* pos, 
     for (auto* a : {&h->group_at, &h->groups, &h->cnt_e, &h->cnt_s, &h->bucket, &h->queue, &h->front_at, &h->fronts,
                     &h->inv_order})
         NB_TRY(a->alloc(n));
-    h->front_limit = (int)std::max<int64_t>(cfg->n_group_limit, n / 1024);
+    h->front_limit = (int)std::max<int64_t>(cfg->n_group_limit, n / 512);
     NB_TRY(alloc_tasks(h, 64 * (n / std::max(1, cfg->n_group_limit / 4) + 1) + 4096));
     NB_TRY(h->walks.alloc(n));
     h->cap_e = 8 * n + 1024;  // first guesses; the first build sizes them
@@ -1936,7 +1937,7 @@ int pgf_nbody_set_group_limit(pgf_nbody* h, int n_group_limit) {
     if (n_group_limit < 1) return nb_fail(PGF_ERR_ARG, "n_group_limit must be >= 1");
     NB_CUDA(cudaStreamSynchronize(h->stream));
     h->cfg.n_group_limit = n_group_limit;
-    h->front_limit = (int)std::max<int64_t>(n_group_limit, h->n / 1024);
+    h->front_limit = (int)std::max<int64_t>(n_group_limit, h->n / 512);
     drop_graph(h);  // the captured steps build other lists now
     if (int r = build_fit(h)) return r;
     return pgf_nbody_force(h);
