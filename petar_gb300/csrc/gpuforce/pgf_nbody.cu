@@ -129,6 +129,17 @@ struct CMom {
 __device__ __forceinline__ double dmin(double a, double b) { return b < a ? b : a; }  // std::min
 __device__ __forceinline__ double dmax(double a, double b) { return a < b ? b : a; }  // std::max
 
+// The same for non-NaN values on the integer pipe (GB300 runs FP64 at 1/64 of
+// the FP32 rate): doubles ordered as signed 64-bit keys, -0 and +0 equal as
+// the FP64 comparison sees them, ties returning a as above.
+__device__ __forceinline__ int64_t order_key(double x) {
+    int64_t b = __double_as_longlong(x);
+    if (b == (int64_t)0x8000000000000000ull) b = 0;
+    return b < 0 ? (b ^ 0x7fffffffffffffffll) : b;
+}
+__device__ __forceinline__ double kmin(double a, double b) { return order_key(b) < order_key(a) ? b : a; }
+__device__ __forceinline__ double kmax(double a, double b) { return order_key(a) < order_key(b) ? b : a; }
+
 __device__ __forceinline__ uint64_t spread3(uint64_t v) {
     v &= 0x1fffff;
     v = (v | (v << 32)) & 0x1f00000000ffffULL;
@@ -485,12 +496,12 @@ __global__ __launch_bounds__(256) void moments_kernel(const TreeHdr* h, TCell* c
                 m += mi;
                 for (int d = 0; d < 3; ++d) {
                     mx[d] += mi * x[d];
-                    ilo[d] = dmin(ilo[d], x[d]);
-                    ihi[d] = dmax(ihi[d], x[d]);
-                    olo[d] = dmin(olo[d], x[d] - e.rs);
-                    ohi[d] = dmax(ohi[d], x[d] + e.rs);
+                    ilo[d] = kmin(ilo[d], x[d]);
+                    ihi[d] = kmax(ihi[d], x[d]);
+                    olo[d] = kmin(olo[d], x[d] - e.rs);
+                    ohi[d] = kmax(ohi[d], x[d] + e.rs);
                 }
-                rsm = dmax(rsm, e.rs);
+                rsm = kmax(rsm, e.rs);
             }
         } else {
             for (int k = 0; k < cc.n_child; ++k) {
@@ -500,12 +511,12 @@ __global__ __launch_bounds__(256) void moments_kernel(const TreeHdr* h, TCell* c
                 m += cm.m;
                 for (int d = 0; d < 3; ++d) {
                     mx[d] += cm.mx[d];
-                    ilo[d] = dmin(ilo[d], ch.in_lo[d]);
-                    ihi[d] = dmax(ihi[d], ch.in_hi[d]);
-                    olo[d] = dmin(olo[d], ch.out_lo[d]);
-                    ohi[d] = dmax(ohi[d], ch.out_hi[d]);
+                    ilo[d] = kmin(ilo[d], ch.in_lo[d]);
+                    ihi[d] = kmax(ihi[d], ch.in_hi[d]);
+                    olo[d] = kmin(olo[d], ch.out_lo[d]);
+                    ohi[d] = kmax(ohi[d], ch.out_hi[d]);
                 }
-                rsm = dmax(rsm, (double)ch.rs_max);
+                rsm = kmax(rsm, (double)ch.rs_max);
             }
         }
         double com[3];
