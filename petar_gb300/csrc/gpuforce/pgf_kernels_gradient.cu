@@ -13,9 +13,9 @@
 // evaluation, but it runs once per step).  256 threads pop walks from the
 // cost-sorted queue; a pass holds up to 512 i, two per thread, and the
 // threads form floor(256 / ceil(n_i / 2)) j-slices.  The pair arithmetic is
-// packed FP32x2 over pairs of j.  Threads stage 128-entry
+// packed FP32x2 over pairs of j.  Threads stage 256-entry
 // EPJ tiles (positions as walk-relative (hi, lo) pairs from the FP32 split
-// arrays, accelerations as (hi, lo) pairs) and 128-entry SPJ tiles in shared
+// arrays, accelerations as (hi, lo) pairs) and 256-entry SPJ tiles in shared
 // memory.  Pair arithmetic is FP32 with both halves, so dr and da are accurate
 // to an ulp of themselves for close pairs; partial sums are flushed into
 // (hi, lo) FP32 accumulators and the slices are combined in FP64.
@@ -25,8 +25,8 @@ namespace pgf {
 namespace {
 
 constexpr int kThreadsG = 256;
-constexpr int kTileEPG = 128;
-constexpr int kTileSPG = 128;  // as many pairs per tile as an EP tile
+constexpr int kTileEPG = 256;
+constexpr int kTileSPG = 256;  // as many pairs per tile as an EP tile
 constexpr int kFlushG = 256;
 
 __device__ __forceinline__ float rsqrt_approx_g(float x) {

@@ -386,8 +386,9 @@ __device__ __forceinline__ int cta256_excl_scan(int v, int* total) {
     return base + x - v;
 }
 
-__global__ __launch_bounds__(256) void split_kernel(TreeHdr* h, TCell* cells, int32_t* nch, int32_t* blocksum,
-                                                    const uint64_t* __restrict__ skey, int L, int n_leaf) {
+__global__ __launch_bounds__(256) void split_kernel(TreeHdr* h, TCell* cells, int32_t* nch, int4* bnd,
+                                                    int32_t* blocksum, const uint64_t* __restrict__ skey, int L,
+                                                    int n_leaf) {
     if (h->err) return;
     int c0, c1;
     level_chunk(h, L, c0, c1);
@@ -402,6 +403,9 @@ __global__ __launch_bounds__(256) void split_kernel(TreeHdr* h, TCell* cells, in
             int b[9];
             octants(skey, cc.begin, cc.end, L, b);
             for (int o = 0; o < 8; ++o) k += b[o + 1] > b[o];
+            // The octant ends, for the fill of this level.
+            bnd[2 * (c - lb)] = make_int4(b[1], b[2], b[3], b[4]);
+            bnd[2 * (c - lb) + 1] = make_int4(b[5], b[6], b[7], b[8]);
         }
         cc.leaf = leaf;
         cc.n_child = k;
@@ -430,8 +434,8 @@ __global__ __launch_bounds__(kScanThreads) void level_scan_kernel(TreeHdr* h, in
 }
 
 __global__ __launch_bounds__(256) void fill_kernel(TreeHdr* h, TCell* cells, const int32_t* __restrict__ nch,
-                                                   const int32_t* __restrict__ blockoff,
-                                                   const uint64_t* __restrict__ skey, int L) {
+                                                   const int4* __restrict__ bnd, const int32_t* __restrict__ blockoff,
+                                                   int L) {
     if (h->err) return;
     int c0, c1;
     level_chunk(h, L, c0, c1);
@@ -446,8 +450,8 @@ __global__ __launch_bounds__(256) void fill_kernel(TreeHdr* h, TCell* cells, con
             TCell& cc = cells[c];
             const int first = run + off;
             cc.first_child = first;
-            int b[9];
-            octants(skey, cc.begin, cc.end, L, b);
+            const int4 u = bnd[2 * (c - lb)], v = bnd[2 * (c - lb) + 1];
+            const int b[9] = {cc.begin, u.x, u.y, u.z, u.w, v.x, v.y, v.z, v.w};
             int k = 0;
             for (int o = 0; o < 8; ++o) {
                 if (b[o + 1] <= b[o]) continue;
@@ -1333,6 +1337,7 @@ struct pgf_nbody {
     DArr<TCellW> cw;
     DArr<CMom> mom;
     DArr<int32_t> nch;
+    DArr<int4> bnd;  // per cell of the level being split: its octant ends (2 x 4)
     DArr<int32_t> blocksum;  // per-CTA child counts of one level, then their offsets
     DArr<SpjMix> spj;
     DArr<SpjF32> spj32;
@@ -1417,10 +1422,10 @@ cudaError_t enqueue_build(pgf_nbody* h) {
                                      h->epj_rs64.d, h->epj32.d, h->inv_order.d);
     const int gc = grid_for(h, h->cap_cells, 256);
     for (int L = 0; L < kLevels; ++L) {
-        split_kernel<<<kLevelBlocks, 256, 0, s>>>(hd, h->cells.d, h->nch.d, h->blocksum.d, h->key_out.d, L,
+        split_kernel<<<kLevelBlocks, 256, 0, s>>>(hd, h->cells.d, h->nch.d, h->bnd.d, h->blocksum.d, h->key_out.d, L,
                                                   h->cfg.n_leaf_limit);
         level_scan_kernel<<<1, kScanThreads, 0, s>>>(hd, h->blocksum.d, L, h->cap_cells);
-        fill_kernel<<<kLevelBlocks, 256, 0, s>>>(hd, h->cells.d, h->nch.d, h->blocksum.d, h->key_out.d, L);
+        fill_kernel<<<kLevelBlocks, 256, 0, s>>>(hd, h->cells.d, h->nch.d, h->bnd.d, h->blocksum.d, L);
     }
     moments_kernel<true><<<gc, 256, 0, s>>>(hd, h->cells.d, h->cw.d, h->mom.d, h->epi.d, h->epj_m64.d, 0,
                                             h->inv_theta2, h->spj.d, h->spj32.d, h->spjq.d);
@@ -1538,6 +1543,7 @@ cudaError_t alloc_cells(pgf_nbody* h, int cap) {
     if ((e = h->cw.alloc(cap)) != cudaSuccess) return e;
     if ((e = h->mom.alloc(cap)) != cudaSuccess) return e;
     if ((e = h->nch.alloc(cap)) != cudaSuccess) return e;
+    if ((e = h->bnd.alloc(2 * (size_t)cap)) != cudaSuccess) return e;
     if ((e = h->spj.alloc(cap)) != cudaSuccess) return e;
     if ((e = h->spj32.alloc(cap)) != cudaSuccess) return e;
     return h->spjq.alloc(cap);
