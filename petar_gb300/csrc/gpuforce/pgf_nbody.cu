@@ -936,7 +936,7 @@ __global__ __launch_bounds__(128) void group_reduce_kernel(TreeHdr* h, const TCe
         // Counts are read kB chunks at a time before their offsets are
         // written back: loads that follow a store to the same array would
         // otherwise wait one memory latency per chunk.
-        constexpr int kB = 8;
+        constexpr int kB = 32;
         int64_t re = 0, rs = 0;
         for (int64_t q0 = 0; q0 < nq; q0 += kB) {
             int e[kB], s[kB];
