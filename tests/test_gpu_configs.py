@@ -41,7 +41,7 @@ def _errors(res, o, rows=None):
 def test_plummer1m_bin50_headline_config():
     """The bench workload itself (1,572,864 particles, 10,882 walks): the
     default mixed-precision kernel at the full parity bar, the plain FP64
-    kernel to 1e-12, counts exact for both."""
+    kernel to 1e-12, counts exact for both; then the gradient pass."""
     cl = ics.make_plummer_cluster(3, 1048576, 0.003, binary_fraction=0.5, theta=0.3)
     wb = walks.build_walks(cl)
     assert cl.n == 1572864
@@ -64,6 +64,16 @@ def test_plummer1m_bin50_headline_config():
     for e in (rel_err_vec(res["acc"], f64["acc"]), rel_err(res["pot"], f64["pot"])):
         s = stats(e)
         assert s["median"] <= MIXED_MEDIAN and s["p999"] <= MIXED_P999 and s["max"] <= MIXED_MAX, s
+    # The KDKDK_4TH gradient pass on the same walks, with the FP64 forces as
+    # each particle's a_i: acorr, acc and pot at the full bar on the sample.
+    acc = f64["acc"]
+    gr = gpuforce.compute_gradient(wb, acc, acc)
+    og = oracle.gradient(wb.subset(sw), acc[rows], acc)
+    for key in ("acorr", "acc", "pot"):
+        e = rel_err(gr[key][rows], og[key]) if key == "pot" else rel_err_vec(gr[key][rows], og[key])
+        s = stats(e)
+        assert s["median"] <= MIXED_MEDIAN and s["p999"] <= MIXED_P999 and s["max"] <= MIXED_MAX, (key, s)
+    assert (gr["nnb"] == 0).all()
 
 
 def test_plummer65k_against_oracle_and_direct_sum():

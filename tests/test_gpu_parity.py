@@ -501,6 +501,27 @@ def test_walk_split_matches_unsplit_and_oracle(precision):
     check(wb, split, precision, label="split")
 
 
+def test_walk_split_unit_changes_summation_order_only():
+    """The split unit decides how many parts the expensive walks run as; the
+    results stay within summation order of each other and counts exact."""
+    cl = ics.make_plummer_cluster(2, 65536, 0.008)
+    wb = walks.build_walks(cl)
+    out = {}
+    try:
+        for div in (1, 8, 64):
+            gpuforce.set_walk_split_unit(div)
+            out[div] = gpuforce.compute(wb, PGF_PRECISION_MIXED)
+    finally:
+        gpuforce.set_walk_split_unit(8)
+    with pytest.raises(gpuforce.GpuForceError):
+        gpuforce.set_walk_split_unit(0)
+    for div in (1, 64):
+        np.testing.assert_array_equal(out[div]["nnb"], out[8]["nnb"])
+        st = stats(rel_err_vec(out[div]["acc"], out[8]["acc"]))
+        assert st["median"] <= MIXED_MEDIAN and st["p999"] <= MIXED_P999, (div, st)
+    check(wb, out[64], PGF_PRECISION_MIXED, label="split unit 1/64")
+
+
 def test_walk_split_changeover_and_gradient_modes():
     """Split walks in the modes with per-i terms: the changeover
     self-potential and the gradient pass's a_i are added once; results agree
