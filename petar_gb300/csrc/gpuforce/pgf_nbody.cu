@@ -394,23 +394,64 @@ __global__ __launch_bounds__(256) void split_kernel(TreeHdr* h, TCell* cells, in
     level_chunk(h, L, c0, c1);
     const int lb = h->level_begin[L];
     int sum = 0;
-    for (int c = c0 + (int)threadIdx.x; c < c1; c += blockDim.x) {
-        TCell& cc = cells[c];
-        const int cnt = cc.end - cc.begin;
-        const bool leaf = cnt <= n_leaf || L >= kMaxLevel;
-        int k = 0;
-        if (!leaf) {
+    if (c1 - c0 <= (int)(blockDim.x >> 5)) {
+        // Few, large cells (the upper levels): a warp per cell, its seven
+        // binary searches run by seven lanes at once instead of one after
+        // another (each is a chain of dependent key loads).
+        const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        if (c0 + w < c1) {
+            const int c = c0 + w;
+            TCell& cc = cells[c];
+            const int cnt = cc.end - cc.begin;
+            const bool leaf = cnt <= n_leaf || L >= kMaxLevel;
+            int bo = cc.end;
+            if (!leaf && lane < 7) {
+                const int shift = 3 * (kMaxLevel - 1 - L);
+                int lo = cc.begin, hi = cc.end;  // first index with digit >= lane + 1
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if ((int)((skey[mid] >> shift) & 7) < lane + 1) lo = mid + 1;
+                    else hi = mid;
+                }
+                bo = lo;
+            }
             int b[9];
-            octants(skey, cc.begin, cc.end, L, b);
-            for (int o = 0; o < 8; ++o) k += b[o + 1] > b[o];
-            // The octant ends, for the fill of this level.
-            bnd[2 * (c - lb)] = make_int4(b[1], b[2], b[3], b[4]);
-            bnd[2 * (c - lb) + 1] = make_int4(b[5], b[6], b[7], b[8]);
+            b[0] = cc.begin;
+            b[8] = cc.end;
+#pragma unroll
+            for (int o = 1; o < 8; ++o) b[o] = __shfl_sync(0xffffffffu, bo, o - 1);
+            if (lane == 0) {
+                int k = 0;
+                if (!leaf) {
+                    for (int o = 0; o < 8; ++o) k += b[o + 1] > b[o];
+                    bnd[2 * (c - lb)] = make_int4(b[1], b[2], b[3], b[4]);
+                    bnd[2 * (c - lb) + 1] = make_int4(b[5], b[6], b[7], b[8]);
+                }
+                cc.leaf = leaf;
+                cc.n_child = k;
+                nch[c - lb] = k;
+                sum = k;
+            }
         }
-        cc.leaf = leaf;
-        cc.n_child = k;
-        nch[c - lb] = k;
-        sum += k;
+    } else {
+        for (int c = c0 + (int)threadIdx.x; c < c1; c += blockDim.x) {
+            TCell& cc = cells[c];
+            const int cnt = cc.end - cc.begin;
+            const bool leaf = cnt <= n_leaf || L >= kMaxLevel;
+            int k = 0;
+            if (!leaf) {
+                int b[9];
+                octants(skey, cc.begin, cc.end, L, b);
+                for (int o = 0; o < 8; ++o) k += b[o + 1] > b[o];
+                // The octant ends, for the fill of this level.
+                bnd[2 * (c - lb)] = make_int4(b[1], b[2], b[3], b[4]);
+                bnd[2 * (c - lb) + 1] = make_int4(b[5], b[6], b[7], b[8]);
+            }
+            cc.leaf = leaf;
+            cc.n_child = k;
+            nch[c - lb] = k;
+            sum += k;
+        }
     }
     int tot;
     (void)cta256_excl_scan(sum, &tot);
