@@ -68,7 +68,8 @@ constexpr int kMaxLevel = 21;          // 3 x 21 bits of Morton key
 constexpr int kLevels = kMaxLevel + 1;  // levels 0 .. 21
 constexpr int kStack = 160;            // DFS stack: 1 + 7 x 21 entries at most
 constexpr int kBuckets = 256;          // work-queue cost buckets
-constexpr int kLeafBins = 64;          // leaf size classes of the moments launch
+constexpr int kLeafBins = 64;          // leaf size classes of the moments launches
+constexpr int kCellBins = kLeafBins + 8 * kLevels;  // and inner cells by level and child count
 constexpr int kScanThreads = 1024;
 
 enum : int32_t { kErrCells = 1, kErrEpj = 2, kErrSpj = 4, kErrTasks = 8 };
@@ -91,8 +92,8 @@ struct TreeHdr {
     unsigned long long total_epep, total_epsp;
     int32_t hist[kBuckets];
     int32_t cursor[kBuckets];
-    int32_t leaf_hist[kLeafBins];    // leaves by particle count
-    int32_t leaf_cursor[kLeafBins];  // their slots in the size-ordered leaf list
+    int32_t cell_hist[kCellBins];    // cells by moments class
+    int32_t cell_cursor[kCellBins];  // their slots in the class-ordered cell list
     int32_t sample_slot;  // next record slot of the per-step sample
     int32_t pad2;
     unsigned long long walk_cursor[2];  // next task of the count and fill passes
@@ -518,55 +519,61 @@ __global__ __launch_bounds__(256) void fill_kernel(TreeHdr* h, TCell* cells, con
 // Moments, boxes and the SPJ records: LEAVES, every leaf of the tree from
 // its particles; otherwise the inner cells of level L from their children
 // (run deepest level first).
-// The leaves in order of particle count (largest class first), so that the
-// threads of a warp run leaf loops of the same length: GB300 issues each FP64
-// instruction for the whole warp, whatever its active lanes.
-__device__ __forceinline__ int leaf_bin(const TCell& c) {
-    const int n = c.end - c.begin;
-    return kLeafBins - 1 - (n < kLeafBins - 1 ? n : kLeafBins - 1);
+// The cells in moments classes, so that the threads of a warp run loops of
+// the same length (GB300 issues each FP64 instruction for the whole warp,
+// whatever its active lanes): leaves by particle count, largest first, then
+// the inner cells of each level by child count, most first.
+__device__ __forceinline__ int cell_bin(const TCell& c) {
+    if (c.leaf) {
+        const int n = c.end - c.begin;
+        return kLeafBins - 1 - (n < kLeafBins - 1 ? n : kLeafBins - 1);
+    }
+    return kLeafBins + 8 * c.level + (8 - c.n_child);
 }
 
-__global__ __launch_bounds__(256) void leaf_hist_kernel(TreeHdr* h, const TCell* __restrict__ cells) {
-    __shared__ int hs[kLeafBins];
-    for (int b = threadIdx.x; b < kLeafBins; b += blockDim.x) hs[b] = 0;
+// First slot of class b in the cell list (after the scatter).
+__device__ __forceinline__ int bin_start(const TreeHdr* h, int b) { return b == 0 ? 0 : h->cell_cursor[b - 1]; }
+
+__global__ __launch_bounds__(256) void cell_hist_kernel(TreeHdr* h, const TCell* __restrict__ cells) {
+    __shared__ int hs[kCellBins];
+    for (int b = threadIdx.x; b < kCellBins; b += blockDim.x) hs[b] = 0;
     __syncthreads();
     if (!h->err) {
         const int nc = h->level_begin[kLevels];
-        for (int64_t c = gtid(); c < nc; c += gstride())
-            if (cells[c].leaf) atomicAdd(&hs[leaf_bin(cells[c])], 1);
+        for (int64_t c = gtid(); c < nc; c += gstride()) atomicAdd(&hs[cell_bin(cells[c])], 1);
     }
     __syncthreads();
-    for (int b = threadIdx.x; b < kLeafBins; b += blockDim.x)
-        if (hs[b]) atomicAdd(&h->leaf_hist[b], hs[b]);
+    for (int b = threadIdx.x; b < kCellBins; b += blockDim.x)
+        if (hs[b]) atomicAdd(&h->cell_hist[b], hs[b]);
 }
 
-__global__ void leaf_scan_kernel(TreeHdr* h) {
+__global__ void cell_scan_kernel(TreeHdr* h) {
     if (threadIdx.x != 0) return;
     int run = 0;
-    for (int b = 0; b < kLeafBins; ++b) {
-        h->leaf_cursor[b] = run;
-        run += h->leaf_hist[b];
+    for (int b = 0; b < kCellBins; ++b) {
+        h->cell_cursor[b] = run;
+        run += h->cell_hist[b];
     }
 }
 
-__global__ __launch_bounds__(256) void leaf_scatter_kernel(TreeHdr* h, const TCell* __restrict__ cells,
-                                                           int32_t* __restrict__ leaves) {
-    __shared__ int hs[kLeafBins], base[kLeafBins];
+__global__ __launch_bounds__(256) void cell_scatter_kernel(TreeHdr* h, const TCell* __restrict__ cells,
+                                                           int32_t* __restrict__ order) {
+    __shared__ int hs[kCellBins], base[kCellBins];
     const int nc = h->err ? 0 : h->level_begin[kLevels];
     for (int64_t c0 = (int64_t)blockIdx.x * blockDim.x; c0 < nc; c0 += gstride()) {
-        for (int b = threadIdx.x; b < kLeafBins; b += blockDim.x) hs[b] = 0;
+        for (int b = threadIdx.x; b < kCellBins; b += blockDim.x) hs[b] = 0;
         __syncthreads();
         const int64_t c = c0 + threadIdx.x;
         int b = -1, r = 0;
-        if (c < nc && cells[c].leaf) {
-            b = leaf_bin(cells[c]);
+        if (c < nc) {
+            b = cell_bin(cells[c]);
             r = atomicAdd(&hs[b], 1);
         }
         __syncthreads();
-        for (int k = threadIdx.x; k < kLeafBins; k += blockDim.x)
-            base[k] = hs[k] ? atomicAdd(&h->leaf_cursor[k], hs[k]) : 0;
+        for (int k = threadIdx.x; k < kCellBins; k += blockDim.x)
+            base[k] = hs[k] ? atomicAdd(&h->cell_cursor[k], hs[k]) : 0;
         __syncthreads();
-        if (b >= 0) leaves[base[b] + r] = (int32_t)c;
+        if (b >= 0) order[base[b] + r] = (int32_t)c;
         __syncthreads();
     }
 }
@@ -575,20 +582,13 @@ template <bool LEAVES>
 __global__ __launch_bounds__(256) void moments_kernel(const TreeHdr* h, TCell* cells, TCellW* cw, CMom* mom,
                                                       const EpiDev* __restrict__ epi, const double* __restrict__ m64,
                                                       int L, double inv_theta2, SpjMix* spj, SpjF32* spj32,
-                                                      SpjQ64* spjq, const int32_t* __restrict__ leaves) {
+                                                      SpjQ64* spjq, const int32_t* __restrict__ order) {
     if (h->err) return;
-    int lb, le;
-    if (LEAVES) {
-        lb = 0;
-        le = h->leaf_cursor[kLeafBins - 1];  // the leaf count, after the scatter
-    } else {
-        lb = h->level_begin[L];
-        le = h->level_begin[L + 1];
-    }
+    const int lb = LEAVES ? 0 : bin_start(h, kLeafBins + 8 * L);
+    const int le = LEAVES ? bin_start(h, kLeafBins) : bin_start(h, kLeafBins + 8 * L + 8);
     for (int64_t t = lb + gtid(); t < le; t += gstride()) {
-        const int64_t c = LEAVES ? (int64_t)leaves[t] : t;
+        const int64_t c = order[t];
         TCell& cc = cells[c];
-        if (cc.leaf != (int)LEAVES) continue;
         const double side = ldexp(h->side0, -cc.level);
         double m = 0, mx[3] = {0, 0, 0}, q[6] = {0, 0, 0, 0, 0, 0};
         double ilo[3], ihi[3], olo[3], ohi[3];
@@ -1442,7 +1442,7 @@ struct pgf_nbody {
     DArr<TCellW> cw;
     DArr<CMom> mom;
     DArr<int32_t> nch;
-    DArr<int32_t> leaves;  // leaf cells by particle count
+    DArr<int32_t> cell_order;  // cells by moments class (cell_bin)
     DArr<int4> bnd;  // per cell of the level being split: its octant ends (2 x 4)
     DArr<int32_t> blocksum;  // per-CTA child counts of one level, then their offsets
     DArr<SpjMix> spj;
@@ -1518,7 +1518,7 @@ cudaError_t enqueue_build(pgf_nbody* h) {
     TreeHdr* hd = h->hdr.d;
     bbox_partial_kernel<<<h->bbox_blocks, 256, 0, s>>>(h->pos.d, n, h->part.d);
     bbox_final_kernel<<<1, 256, 0, s>>>(h->part.d, h->bbox_blocks, n, hd, h->cells.d);
-    cudaError_t e = cudaMemsetAsync(hd->hist, 0, sizeof(int32_t) * 2 * (kBuckets + kLeafBins), s);
+    cudaError_t e = cudaMemsetAsync(hd->hist, 0, sizeof(int32_t) * 2 * (kBuckets + kCellBins), s);
     if (e != cudaSuccess) return e;
     const int gn = grid_for(h, n, 256);
     keys_kernel<<<gn, 256, 0, s>>>(h->pos.d, n, hd, h->key_in.d, h->val_in.d);
@@ -1533,15 +1533,15 @@ cudaError_t enqueue_build(pgf_nbody* h) {
         level_scan_kernel<<<1, kScanThreads, 0, s>>>(hd, h->blocksum.d, L, h->cap_cells);
         fill_kernel<<<kLevelBlocks, 256, 0, s>>>(hd, h->cells.d, h->nch.d, h->bnd.d, h->blocksum.d, L);
     }
-    leaf_hist_kernel<<<h->num_sms * 2, 256, 0, s>>>(hd, h->cells.d);
-    leaf_scan_kernel<<<1, 32, 0, s>>>(hd);
-    leaf_scatter_kernel<<<h->num_sms * 2, 256, 0, s>>>(hd, h->cells.d, h->leaves.d);
+    cell_hist_kernel<<<h->num_sms * 2, 256, 0, s>>>(hd, h->cells.d);
+    cell_scan_kernel<<<1, 32, 0, s>>>(hd);
+    cell_scatter_kernel<<<h->num_sms * 2, 256, 0, s>>>(hd, h->cells.d, h->cell_order.d);
     moments_kernel<true><<<gc, 256, 0, s>>>(hd, h->cells.d, h->cw.d, h->mom.d, h->epi.d, h->epj_m64.d, 0,
-                                            h->inv_theta2, h->spj.d, h->spj32.d, h->spjq.d, h->leaves.d);
+                                            h->inv_theta2, h->spj.d, h->spj32.d, h->spjq.d, h->cell_order.d);
     const int gm = h->num_sms * 2;
     for (int L = kLevels - 1; L >= 0; --L)
         moments_kernel<false><<<gm, 256, 0, s>>>(hd, h->cells.d, h->cw.d, h->mom.d, h->epi.d, h->epj_m64.d, L,
-                                                 h->inv_theta2, h->spj.d, h->spj32.d, h->spjq.d, nullptr);
+                                                 h->inv_theta2, h->spj.d, h->spj32.d, h->spjq.d, h->cell_order.d);
     if ((e = cudaMemsetAsync(h->group_at.d, 0xff, sizeof(int32_t) * n, s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(h->front_at.d, 0xff, sizeof(int32_t) * n, s)) != cudaSuccess) return e;
     group_mark_kernel<<<gc, 256, 0, s>>>(hd, h->cells.d, h->group_at.d, h->cfg.n_group_limit);
@@ -1652,7 +1652,7 @@ cudaError_t alloc_cells(pgf_nbody* h, int cap) {
     if ((e = h->cw.alloc(cap)) != cudaSuccess) return e;
     if ((e = h->mom.alloc(cap)) != cudaSuccess) return e;
     if ((e = h->nch.alloc(cap)) != cudaSuccess) return e;
-    if ((e = h->leaves.alloc(cap)) != cudaSuccess) return e;
+    if ((e = h->cell_order.alloc(cap)) != cudaSuccess) return e;
     if ((e = h->bnd.alloc(2 * (size_t)cap)) != cudaSuccess) return e;
     if ((e = h->spj.alloc(cap)) != cudaSuccess) return e;
     if ((e = h->spj32.alloc(cap)) != cudaSuccess) return e;
