@@ -196,14 +196,14 @@ int pgf_set_dispatch_stages(int stages);
 
 /* Walk splitting in single-launch dispatches (1, the default, or 0 = off).
  * When a dispatch has few walks for the GPU's CTAs, each walk costing more
- * than an eighth of one SM's even share runs as up to 16 parts over slices
+ * than a sixteenth of one SM's even share runs as up to 16 parts over slices
  * of its EPJ and SPJ lists, and the parts are added in a fixed order; results then differ
  * from an unsplit launch by FP32 summation order only (counts are exact).
  * All modes; no counterpart in the reference. */
 int pgf_set_walk_split(int enable);
 
 /* Split unit of walk splitting: a walk is split when it costs more than
- * 1/div of one SM's even share of the dispatch (default 8; 1..256).
+ * 1/div of one SM's even share of the dispatch (default 16; 1..256).
  * pgf_autotune_dispatch sets it too.  Results are as for pgf_set_walk_split. */
 int pgf_set_walk_split_unit(int div);
 
@@ -249,8 +249,8 @@ int pgf_autotune(int tag, int repeats, int *best_variant, double *best_ms);
  * `repeats` timed runs after a warm-up, and keeps the fastest for later
  * dispatches.  Candidates: pipeline stage counts 1, 2, 4 and 8 (how many
  * launches a dispatch is cut into, each overlapping the next stage's packing
- * and copies), and for single launches the walk-split unit (an eighth of one
- * SM's even share by default; 4, 16 and 32 also tried).  The force records
+ * and copies), and for single launches the walk-split unit (a sixteenth of
+ * one SM's even share by default; 4, 8 and 32 also tried).  The force records
  * hold the last run's results.  The reference fixes its walks per launch at
  * compile time (N_WALK_LIMIT, src/force_gpu_cuda.cu:12-17) and PeTar its
  * n_walk_limit (src/petar.hpp:888). */

@@ -168,7 +168,7 @@ struct State {
     int variant = PGF_DEFAULT_KERNEL_VARIANT;  // mixed-precision kernel variant (pgf_set_kernel_variant)
     int stages = 0;   // dispatch pipeline stages (pgf_set_dispatch_stages); 0 = by size
     bool walk_split = true;  // split the largest walks of small dispatches (pgf_set_walk_split)
-    int split_div = 8;       // split unit: 1/split_div of one SM's even share (pgf_autotune_dispatch)
+    int split_div = 16;      // split unit: 1/split_div of one SM's even share (pgf_autotune_dispatch)
     uint64_t wait_limit_ns = 0;  // bounded waits of the kernels (pgf_set_wait_limit_ns; 0: 1 s)
     int stall_after_items = 0;   // test hook (pgf_test_stall_producer)
     // Host-direct data movement (pgf_set_host_direct): the device reads the
@@ -997,16 +997,16 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
         n_chunks == 1 && use_hd() && hd_walks_ok(n_walk, epi, n_epi, il, id_epj, n_epj, id_spj, n_spj, t.mode);
 
     // Split plan.  In a single launch the most expensive walks bound the
-    // launch time when there are few walks per CTA.  The unit is an eighth
+    // launch time when there are few walks per CTA.  The unit is a sixteenth
     // of one SM's even share of the dispatch's cost; each walk that costs
     // more than a unit runs as parts of at most a unit (at most 16 parts, at
     // least 256 list entries each), each with a slice of its EPJ and SPJ
     // lists and its own copy of the walk's EPI rows (made on the device), and
     // a combine kernel adds the parts up.  The kernels add per-i terms
     // (changeover self-potential, the gradient pass's a_i) in part 0 only.
-    // On 200-walk batches of the 1M binary Plummer workload an eighth runs
+    // On 200-walk batches of the 1M binary Plummer workload an eighth ran
     // the kernels 24% faster than parts of a quarter share split only above
-    // two units.
+    // two units, and a sixteenth another 5% faster than an eighth.
     std::vector<SplitPlan> plan;
     int64_t ni_all = ni;
     int n_desc = n_walk;
@@ -1522,7 +1522,7 @@ int pgf_autotune_dispatch(int tag, int n_walk, const void* const* epi, const int
     };
     std::vector<Cand> cands;
     for (int st : {1, 2, 4, 8}) cands.push_back({st, g.split_div});
-    for (int dv : {4, 16, 32}) cands.push_back({1, dv});
+    for (int dv : {4, 8, 32}) cands.push_back({1, dv});
     double best_t = HUGE_VAL;
     Cand best{saved_stages, saved_div};
     for (const Cand& c : cands) {

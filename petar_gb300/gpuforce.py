@@ -245,7 +245,7 @@ def set_walk_split(enable: bool) -> None:
 
 
 def set_walk_split_unit(div: int) -> None:
-    """Split walks costing more than 1/div of one SM's even share (default 8)."""
+    """Split walks costing more than 1/div of one SM's even share (default 16)."""
     _check(load().pgf_set_walk_split_unit(div))
 
 

@@ -508,16 +508,16 @@ def test_walk_split_unit_changes_summation_order_only():
     wb = walks.build_walks(cl)
     out = {}
     try:
-        for div in (1, 8, 64):
+        for div in (1, 16, 64):
             gpuforce.set_walk_split_unit(div)
             out[div] = gpuforce.compute(wb, PGF_PRECISION_MIXED)
     finally:
-        gpuforce.set_walk_split_unit(8)
+        gpuforce.set_walk_split_unit(16)
     with pytest.raises(gpuforce.GpuForceError):
         gpuforce.set_walk_split_unit(0)
     for div in (1, 64):
-        np.testing.assert_array_equal(out[div]["nnb"], out[8]["nnb"])
-        st = stats(rel_err_vec(out[div]["acc"], out[8]["acc"]))
+        np.testing.assert_array_equal(out[div]["nnb"], out[16]["nnb"])
+        st = stats(rel_err_vec(out[div]["acc"], out[16]["acc"]))
         assert st["median"] <= MIXED_MEDIAN and st["p999"] <= MIXED_P999, (div, st)
     check(wb, out[64], PGF_PRECISION_MIXED, label="split unit 1/64")
 
