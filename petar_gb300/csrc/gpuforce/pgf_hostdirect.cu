@@ -136,9 +136,11 @@ __global__ __launch_bounds__(256) void gather_j_kernel(HdSendArgs a) {
     }
 }
 
-// One CTA per walk (grid-stride over walks): EPI rows (with the copies that
-// the parts of a split walk read), the walk's box and descriptor(s), and its
-// id lists, checked against the sent arrays.  Host memory answers in
+// kIdParts CTAs per walk (grid-stride over the units): each copies a slice
+// of the walk's id lists and checks it against the sent arrays; the first
+// also writes the walk's EPI rows (with the copies that the parts of a split
+// walk read), its box and descriptor(s) and its split record.  Host memory
+// answers in
 // microseconds and serves whole lines best, so a CTA reads a walk's EPI
 // records as contiguous 8-byte words into shared memory (up to kEpiWords per
 // round) and its id lists as contiguous 4-byte words, and each thread issues
