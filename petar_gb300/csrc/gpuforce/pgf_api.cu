@@ -169,6 +169,7 @@ struct State {
     int stages = 0;   // dispatch pipeline stages (pgf_set_dispatch_stages); 0 = by size
     bool walk_split = true;  // split the largest walks of small dispatches (pgf_set_walk_split)
     int split_div = 16;      // split unit: 1/split_div of one SM's even share (pgf_autotune_dispatch)
+    int gr_compensated = 0;  // gradient pass far pairs: 0 FP32, 1 compensated r^2 and 1/r
     uint64_t wait_limit_ns = 0;  // bounded waits of the kernels (pgf_set_wait_limit_ns; 0: 1 s)
     int stall_after_items = 0;   // test hook (pgf_test_stall_producer)
     // Host-direct data movement (pgf_set_host_direct): the device reads the
@@ -1095,6 +1096,7 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
     p.walks = t.walks.d;
     p.order = t.order.d;
     p.n_walk = n_desc;
+    p.gr_compensated = g.gr_compensated;
     // The neighbour search tests r^2 < max(rs_i, rs_j)^2 without softening
     // (src/soft_force.hpp:11-34); the force kernels include eps^2.
     p.eps2 = t.mode == PGF_MODE_NEIGHBOR_SEARCH ? 0.0 : g.eps2;
@@ -1451,6 +1453,12 @@ int pgf_get_host_direct(int* active) {
 
 int pgf_set_walk_split(int enable) {
     g.walk_split = enable != 0;
+    return PGF_OK;
+}
+
+int pgf_set_gradient_accuracy(int mode) {
+    if (mode != 0 && mode != 1) return fail(PGF_ERR_ARG, "gradient accuracy mode %d is not 0 or 1", mode);
+    g.gr_compensated = mode;
     return PGF_OK;
 }
 

@@ -170,7 +170,7 @@ struct Params {
     uint64_t wait_limit_ns;
     // Test hook: > 0 makes their producer stop after that many ring items.
     int32_t stall_after_items;
-    int32_t pad2;
+    int32_t gr_compensated;  // gradient pass: r^2 and 1/r of far pairs to about 2^-40 (pgf_set_gradient_accuracy)
     // Result of the device-side check of a host-direct dispatch's ids, or
     // null: when it is non-zero the force kernels run nothing.
     const int32_t* input_err;

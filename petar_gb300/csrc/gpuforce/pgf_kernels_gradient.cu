@@ -62,6 +62,45 @@ __device__ __forceinline__ void flush_into(float2& v, float x) {
     v.y += e;
 }
 
+// Far pairs with r^2 and 1/r carried beyond FP32 (the compensated option).
+// r^2 = dx^2 + dy^2 + dz^2 + eps^2 as a (hi, lo) pair: exact squares by FMA
+// and error-free sums (the Dot2 scheme of Ogita, Rump and Oishi, 2005).  1/r
+// from y = rsqrt(hi) and the residual t = 1 - r^2 y^2, evaluated with the
+// exact square of y, so that r^-3 = y^3 (1 + 1.5 t) and r^-2 = y^2 (1 + t)
+// to O(t^2) (t is a few 2^-23).  Gives m r^-3 and r^-2.
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+// s = fl(a + b) and the exact error a + b - s (Knuth's two-sum), packed.
+__device__ __forceinline__ float2 two_sum2_err(float2 a, float2 b, float2& s) {
+    s = __fadd2_rn(a, b);
+    const float2 bb = __fadd2_rn(s, neg2(a));
+    const float2 ab = __fadd2_rn(s, neg2(bb));
+    return __fadd2_rn(__fadd2_rn(a, neg2(ab)), __fadd2_rn(b, neg2(bb)));
+}
+
+__device__ __forceinline__ void far_r3_compensated(float2 dx, float2 dy, float2 dz, float2 e2, float2 M, float rcut2,
+                                                   float2& mr3, float2& ri2) {
+    const float2 px = __fmul2_rn(dx, dx), py = __fmul2_rn(dy, dy), pz = __fmul2_rn(dz, dz);
+    const float2 ex = __ffma2_rn(dx, dx, neg2(px));
+    const float2 ey = __ffma2_rn(dy, dy, neg2(py));
+    const float2 ez = __ffma2_rn(dz, dz, neg2(pz));
+    float2 s1, hi;
+    const float2 c1 = two_sum2_err(px, py, s1);
+    const float2 c2 = two_sum2_err(s1, pz, hi);
+    // r^2 = hi + lo with |lo| of order ulp(hi)
+    const float2 lo = __fadd2_rn(__fadd2_rn(__fadd2_rn(ex, ey), __fadd2_rn(ez, e2)), __fadd2_rn(c1, c2));
+    // far pairs have r >= r_out; the clamp only guards rounding at the edge
+    const float2 y = make_float2(rsqrt_approx_g(fmaxf(hi.x, rcut2)), rsqrt_approx_g(fmaxf(hi.y, rcut2)));
+    const float2 h = __fmul2_rn(y, y);
+    const float2 hl = __ffma2_rn(y, y, neg2(h));
+    float2 t = __ffma2_rn(neg2(hi), h, make_float2(1.f, 1.f));
+    t = __ffma2_rn(neg2(hi), hl, t);
+    t = __ffma2_rn(neg2(lo), h, t);
+    const float2 m3 = __fmul2_rn(__fmul2_rn(M, y), h);
+    mr3 = __ffma2_rn(m3, __fmul2_rn(t, make_float2(1.5f, 1.5f)), m3);
+    ri2 = __ffma2_rn(h, t, __fadd2_rn(h, hl));
+}
+
 // KU i-particles per thread: i = li + k S (k < KU) of a pass of up to
 // 256 KU i, with S = ceil(n_i / KU) threads per j-slice.  Tiles are stored
 // as interleaved pairs of j, so that one FP32x2 instruction evaluates two
@@ -86,7 +125,7 @@ struct SmemGP {
     int w;
 };
 
-template <int KU>
+template <int KU, bool CMP>
 __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
     if (p.input_err && *p.input_err) return;  // the inputs failed their check: run nothing
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -178,6 +217,18 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
                     }
                 since = 0;
             };
+            // The acorr partial sums alone (the compensated mode flushes them
+            // every 8 j pairs: the sum over j cancels, and long FP32 partial
+            // sums would round away what the compensated terms keep).
+            auto flush_acorr = [&]() {
+#pragma unroll
+                for (int k = 0; k < KU; ++k)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        flush_into(s.acc[k][q][tid], g[k][q].x + g[k][q].y);
+                        g[k][q] = make_float2(0.f, 0.f);
+                    }
+            };
             const float2 e2 = make_float2(eps2, eps2);
             // EPJ tiles: the gradient correction of every pair.
             for (int t = 0; t < wd.n_epj; t += kTileEPG) {
@@ -260,19 +311,27 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
                             const float2 dax = __fadd2_rn(__fadd2_rn(AXh, nah[k][0]), __fadd2_rn(AXl, nal[k][0]));
                             const float2 day = __fadd2_rn(__fadd2_rn(AYh, nah[k][1]), __fadd2_rn(AYl, nal[k][1]));
                             const float2 daz = __fadd2_rn(__fadd2_rn(AZh, nah[k][2]), __fadd2_rn(AZl, nal[k][2]));
-                            float2 r2 = __ffma2_rn(dx, dx, e2);
-                            r2 = __ffma2_rn(dy, dy, r2);
-                            r2 = __ffma2_rn(dz, dz, r2);
-                            const float2 ri = make_float2(rsqrt_approx_g(fmaxf(r2.x, rcut2)),
-                                                          rsqrt_approx_g(fmaxf(r2.y, rcut2)));
-                            const float2 ri2 = __fmul2_rn(ri, ri);
-                            const float2 mr3 = __fmul2_rn(__fmul2_rn(M, ri), ri2);
+                            float2 ri2, mr3;
+                            if constexpr (CMP) {
+                                far_r3_compensated(dx, dy, dz, e2, M, rcut2, mr3, ri2);
+                            } else {
+                                float2 r2 = __ffma2_rn(dx, dx, e2);
+                                r2 = __ffma2_rn(dy, dy, r2);
+                                r2 = __ffma2_rn(dz, dz, r2);
+                                const float2 ri = make_float2(rsqrt_approx_g(fmaxf(r2.x, rcut2)),
+                                                              rsqrt_approx_g(fmaxf(r2.y, rcut2)));
+                                ri2 = __fmul2_rn(ri, ri);
+                                mr3 = __fmul2_rn(__fmul2_rn(M, ri), ri2);
+                            }
                             const float2 drda = __ffma2_rn(dx, dax, __ffma2_rn(dy, day, __fmul2_rn(dz, daz)));
                             // -alpha = -3 (dr.da) / r^2
                             const float2 nal_ = __fmul2_rn(__fmul2_rn(drda, ri2), make_float2(-3.f, -3.f));
                             g[k][0] = __ffma2_rn(mr3, __ffma2_rn(nal_, dx, dax), g[k][0]);
                             g[k][1] = __ffma2_rn(mr3, __ffma2_rn(nal_, dy, day), g[k][1]);
                             g[k][2] = __ffma2_rn(mr3, __ffma2_rn(nal_, dz, daz), g[k][2]);
+                        }
+                        if constexpr (CMP) {
+                            if (((j - j0) & 7) == 7) flush_acorr();
                         }
                     }
                     since += 2 * (j1 - j0);
@@ -328,9 +387,19 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
                                     const float e0 = (q2.x + nah[k][0].x) + (q3.x + nal[k][0].x);
                                     const float e1 = (q2.y + nah[k][1].x) + (q3.y + nal[k][1].x);
                                     const float e2_ = (q2.z + nah[k][2].x) + (q3.z + nal[k][2].x);
-                                    const float ri = rsqrt_approx_g(r2);
-                                    const float ri2 = ri * ri;
-                                    mr3 = (q0.w * ri) * ri2;
+                                    float ri2;
+                                    if constexpr (CMP) {
+                                        float2 m2, r22;
+                                        far_r3_compensated(make_float2(d0, d0), make_float2(d1, d1),
+                                                           make_float2(d2, d2), make_float2(eps2, eps2),
+                                                           make_float2(q0.w, q0.w), rcut2, m2, r22);
+                                        mr3 = m2.x;
+                                        ri2 = r22.x;
+                                    } else {
+                                        const float ri = rsqrt_approx_g(r2);
+                                        ri2 = ri * ri;
+                                        mr3 = (q0.w * ri) * ri2;
+                                    }
                                     const float nl3 = -3.f * (fmaf(d0, e0, fmaf(d1, e1, d2 * e2_)) * ri2);
                                     v[0] = fmaf(nl3, d0, e0);
                                     v[1] = fmaf(nl3, d1, e1);
@@ -444,26 +513,32 @@ __global__ __launch_bounds__(kThreadsG, 2) void gradient_kernel_pk(Params p) {
 
 constexpr int kKuG = 2;  // i per thread
 
-}  // namespace
-
-cudaError_t launch_gradient(const Params& p, cudaStream_t s, int num_sms) {
-    cudaError_t e = cudaMemsetAsync(p.queue_head, 0, sizeof(int32_t), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), s);
-    if (e != cudaSuccess || p.n_walk <= 0) return e;
+template <bool CMP>
+cudaError_t launch_gradient_t(const Params& p, cudaStream_t s, int num_sms) {
     static int per_sm = 0;
+    cudaError_t e;
     if (per_sm == 0) {
-        e = cudaFuncSetAttribute(gradient_kernel_pk<kKuG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(gradient_kernel_pk<kKuG, CMP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sizeof(SmemGP<kKuG>));
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gradient_kernel_pk<kKuG>, kThreadsG,
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gradient_kernel_pk<kKuG, CMP>, kThreadsG,
                                                           sizeof(SmemGP<kKuG>));
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
     int grid = num_sms * per_sm;
     if (grid > p.n_walk) grid = p.n_walk;
-    gradient_kernel_pk<kKuG><<<grid, kThreadsG, sizeof(SmemGP<kKuG>), s>>>(p);
+    gradient_kernel_pk<kKuG, CMP><<<grid, kThreadsG, sizeof(SmemGP<kKuG>), s>>>(p);
     return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_gradient(const Params& p, cudaStream_t s, int num_sms) {
+    cudaError_t e = cudaMemsetAsync(p.queue_head, 0, sizeof(int32_t), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p.n_retest, 0, sizeof(int32_t), s);
+    if (e != cudaSuccess || p.n_walk <= 0) return e;
+    return p.gr_compensated ? launch_gradient_t<true>(p, s, num_sms) : launch_gradient_t<false>(p, s, num_sms);
 }
 
 }  // namespace pgf

@@ -158,6 +158,7 @@ def load(build: bool = True) -> ctypes.CDLL:
         "pgf_set_dispatch_stages": [ci],
         "pgf_set_walk_split": [ci],
         "pgf_set_walk_split_unit": [ci],
+        "pgf_set_gradient_accuracy": [ci],
         "pgf_set_host_direct": [ci],
         "pgf_set_wait_limit_ns": [ctypes.c_uint64],
         "pgf_test_stall_producer": [ci],
@@ -247,6 +248,11 @@ def set_walk_split(enable: bool) -> None:
 def set_walk_split_unit(div: int) -> None:
     """Split walks costing more than 1/div of one SM's even share (default 16)."""
     _check(load().pgf_set_walk_split_unit(div))
+
+
+def set_gradient_accuracy(mode: int) -> None:
+    """Gradient pass far pairs: 0 FP32 (default), 1 compensated r^2 and 1/r."""
+    _check(load().pgf_set_gradient_accuracy(mode))
 
 
 def set_host_direct(enable: bool) -> None:

@@ -501,6 +501,28 @@ def test_walk_split_matches_unsplit_and_oracle(precision):
     check(wb, split, precision, label="split")
 
 
+@pytest.mark.parametrize("case", ["seed33_members", "seed34", "seed35"])
+def test_gradient_compensated_meets_full_bar(case):
+    """The compensated gradient mode (r^2 and 1/r of the far pairs carried
+    beyond FP32) meets the full mixed bar on every binary-rich case,
+    including those where the FP32 far pairs' rounding shows (see
+    GRADIENT_CANCEL_P999)."""
+    seed = int(case[4:6])
+    cl = ics.make_plummer_cluster(seed, 20000, 0.004, binary_fraction=0.5)
+    wb = walks.build_walks(cl)
+    if case.endswith("members"):
+        wb, _ = walks.make_changeover(wb, cl.r_in, cl.r_out, seed=4)
+    acc = oracle.force(wb)["acc"]
+    try:
+        gpuforce.set_gradient_accuracy(1)
+        res = gpuforce.compute_gradient(wb, acc, acc)
+    finally:
+        gpuforce.set_gradient_accuracy(0)
+    _gradient_check(res, oracle.gradient(wb, acc, acc), f"compensated {case}")
+    with pytest.raises(gpuforce.GpuForceError):
+        gpuforce.set_gradient_accuracy(2)
+
+
 def test_walk_split_unit_changes_summation_order_only():
     """The split unit decides how many parts the expensive walks run as; the
     results stay within summation order of each other and counts exact."""
