@@ -556,13 +556,20 @@ def run_ours(args):
         gpuforce.set_gradient_layout(rec_gr)
         gpuforce.set_mode(gpuforce.PGF_MODE_GRADIENT)
         try:
-            gpuforce.dispatch(rec_gr, tag=3)
-            gpuforce.retrieve(rec_gr, tag=3)
-            t = time_recompute(3)
+            t_mode = {}
+            for acc_mode in (0, 1):  # plain FP32 far pairs, then the default compensated ones
+                gpuforce.set_gradient_accuracy(acc_mode)
+                gpuforce.dispatch(rec_gr, tag=3)
+                gpuforce.retrieve(rec_gr, tag=3)
+                t_mode[acc_mode] = time_recompute(3)
+            t = t_mode[1]
         finally:
+            gpuforce.set_gradient_accuracy(1)
             gpuforce.set_mode(gpuforce.PGF_MODE_FORCE)
             gpuforce.set_gradient_layout(None)
         modes["gradient_kdkdk"] = {"ms_per_step": t, "value": n_int / t / 1e6, "unit": "Ginteractions/s",
+                                   "accuracy_mode": "compensated (default)",
+                                   "fp32_far_pairs_ms_per_step": t_mode[0],
                                    "parity": "tests/test_gpu_parity.py::test_gradient_mode_*"}
 
     # ---- the other named configurations: Plummer 65k and the 64-cluster ensemble ----

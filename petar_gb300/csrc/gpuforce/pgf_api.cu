@@ -169,7 +169,7 @@ struct State {
     int stages = 0;   // dispatch pipeline stages (pgf_set_dispatch_stages); 0 = by size
     bool walk_split = true;  // split the largest walks of small dispatches (pgf_set_walk_split)
     int split_div = 16;      // split unit: 1/split_div of one SM's even share (pgf_autotune_dispatch)
-    int gr_compensated = 0;  // gradient pass far pairs: 0 FP32, 1 compensated r^2 and 1/r
+    int gr_compensated = 1;  // gradient pass far pairs: 1 compensated r^2 and 1/r (default), 0 FP32
     uint64_t wait_limit_ns = 0;  // bounded waits of the kernels (pgf_set_wait_limit_ns; 0: 1 s)
     int stall_after_items = 0;   // test hook (pgf_test_stall_producer)
     // Host-direct data movement (pgf_set_host_direct): the device reads the

@@ -251,7 +251,7 @@ def set_walk_split_unit(div: int) -> None:
 
 
 def set_gradient_accuracy(mode: int) -> None:
-    """Gradient pass far pairs: 0 FP32 (default), 1 compensated r^2 and 1/r."""
+    """Gradient pass far pairs: 1 compensated r^2 and 1/r (default), 0 FP32."""
     _check(load().pgf_set_gradient_accuracy(mode))
 
 

@@ -434,9 +434,10 @@ def test_changeover_mode_pipelined_and_without_layout():
         gpuforce.set_mode(gpuforce.PGF_MODE_FORCE)
 
 
-# acorr p99.9 bound for the one case whose sum over j cancels hardest (see
-# test_walk_split_changeover_and_gradient_modes); every other gradient case
-# meets MIXED_P999.
+# acorr p99.9 bound of the plain FP32 accuracy mode of the gradient pass on
+# the binary-rich cases whose sum over j cancels hardest (see
+# test_gradient_accuracy_modes); the default compensated mode meets
+# MIXED_P999 everywhere.
 GRADIENT_CANCEL_P999 = 2e-5
 
 
@@ -502,23 +503,39 @@ def test_walk_split_matches_unsplit_and_oracle(precision):
 
 
 @pytest.mark.parametrize("case", ["seed33_members", "seed34", "seed35"])
-def test_gradient_compensated_meets_full_bar(case):
-    """The compensated gradient mode (r^2 and 1/r of the far pairs carried
-    beyond FP32) meets the full mixed bar on every binary-rich case,
-    including those where the FP32 far pairs' rounding shows (see
-    GRADIENT_CANCEL_P999)."""
+def test_gradient_accuracy_modes(case):
+    """Binary-rich clusters with each particle's own soft acceleration as a_i.
+    The compensated mode (the default: r^2 and 1/r of the far pairs carried
+    beyond FP32, acorr partials flushed every 8 j pairs) meets the full
+    mixed bar on every case.  The plain FP32 mode meets it on acc and pot and
+    on acorr's median and max; acorr's p99.9 has its own bound there, since
+    the sum over j cancels 100-200-fold for some binary members and FP32
+    rounding of r^2 and 1/r shows at about 1e-5 (1.6e-5 measured on seed
+    35); seed 34 is under 1e-5 in both modes."""
     seed = int(case[4:6])
     cl = ics.make_plummer_cluster(seed, 20000, 0.004, binary_fraction=0.5)
     wb = walks.build_walks(cl)
     if case.endswith("members"):
         wb, _ = walks.make_changeover(wb, cl.r_in, cl.r_out, seed=4)
     acc = oracle.force(wb)["acc"]
+    o = oracle.gradient(wb, acc, acc)
+    res = {}
     try:
-        gpuforce.set_gradient_accuracy(1)
-        res = gpuforce.compute_gradient(wb, acc, acc)
+        for mode in (1, 0):
+            gpuforce.set_gradient_accuracy(mode)
+            res[mode] = gpuforce.compute_gradient(wb, acc, acc)
     finally:
-        gpuforce.set_gradient_accuracy(0)
-    _gradient_check(res, oracle.gradient(wb, acc, acc), f"compensated {case}")
+        gpuforce.set_gradient_accuracy(1)
+    _gradient_check(res[1], o, f"compensated {case}")
+    if case == "seed34":
+        _gradient_check(res[0], o, f"fp32 {case}")
+    else:
+        for key in ("acc", "pot"):
+            e = rel_err_vec(res[0][key], o[key]) if key == "acc" else rel_err(res[0][key], o[key])
+            st = stats(e)
+            assert st["median"] <= MIXED_MEDIAN and st["p999"] <= MIXED_P999 and st["max"] <= MIXED_MAX, (key, st)
+        st = stats(rel_err_vec(res[0]["acorr"], o["acorr"]))
+        assert st["median"] <= MIXED_MEDIAN and st["p999"] <= GRADIENT_CANCEL_P999 and st["max"] <= MIXED_MAX, st
     with pytest.raises(gpuforce.GpuForceError):
         gpuforce.set_gradient_accuracy(2)
 
@@ -573,24 +590,11 @@ def test_walk_split_changeover_and_gradient_modes():
     for k in ("acorr", "acc"):
         st = stats(rel_err_vec(gr[True][k], gr[False][k]))
         assert st["median"] <= MIXED_MEDIAN and st["p999"] <= MIXED_P999, (k, st)
-    # Both passes against the oracle: the full bar on acc and pot, and on
-    # acorr's median and max.  acorr's p99.9 has its own bound on this case
-    # (binaries plus 10% massless members): the sum over j cancels, its terms'
-    # absolute sum reaching ~100x the result at the 99.9th percentile, so the
-    # half-ulp rounding of dr, da, 1/r and (dr.da)/r^2 in the FP32 far pairs
-    # shows at about 1e-5 (measured 1.06e-5 unsplit); pairs inside r_out are
-    # evaluated in double-float and do not set it.
+    # Both passes against the oracle at the full bar (the default,
+    # compensated accuracy mode of the gradient pass).
     o = oracle.gradient(wb, acc, acc)
     for split in (False, True):
-        for key in ("acc", "pot"):
-            e = rel_err_vec(gr[split][key], o[key]) if key == "acc" else rel_err(gr[split][key], o[key])
-            st = stats(e)
-            assert st["median"] <= MIXED_MEDIAN and st["p999"] <= MIXED_P999 and st["max"] <= MIXED_MAX, \
-                (split, key, st)
-        st = stats(rel_err_vec(gr[split]["acorr"], o["acorr"]))
-        assert st["median"] <= MIXED_MEDIAN and st["p999"] <= GRADIENT_CANCEL_P999 and st["max"] <= MIXED_MAX, \
-            (split, "acorr", st)
-        assert (gr[split]["nnb"] == 0).all()
+        _gradient_check(gr[split], o, f"gradient split={split}")
 
 
 def test_bounded_wait_runs_out_and_is_reported():
