@@ -146,7 +146,7 @@ struct TagState {
     HostBuf<SplitRec> h_splits;
     // Host-direct tables, read by the kernels in place: where the gather
     // kernel reads each walk, and where the scatter kernel writes its
-    // results; h_hd_err receives the gather's id-check verdict.
+    // results; h_hd_err receives the gather's id-check outcome.
     HostBuf<WalkSrc> h_src;
     HostBuf<ForceDst> h_dst;
     HostBuf<int32_t> h_hd_err;
@@ -923,13 +923,13 @@ int dispatch_host_direct(TagState& t, int n_walk, const std::vector<int32_t>& or
     }
     PGF_CUDA(cudaEventRecord(t.ev_in, g.stream));
     // The force kernels are queued right behind the gather, with no host
-    // round trip between: they read the check's verdict themselves and run
+    // round trip between: they read the check's outcome themselves and run
     // nothing when an id was out of range.
     t.params.input_err = a.err + 3;
     t.n_split = (int)plan.size();
     if (int r = launch_tag(t)) return r;
     // The caller's arrays are only valid during the call: return once the
-    // gather has read them, with the check's verdict.
+    // gather has read them, with the check's outcome.
     PGF_CUDA(cudaEventSynchronize(t.ev_in));
     if (t.h_hd_err.h[0] != 0) {
         t.dispatched = false;

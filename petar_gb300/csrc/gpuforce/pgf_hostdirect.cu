@@ -147,7 +147,7 @@ __global__ __launch_bounds__(256) void gather_j_kernel(HdSendArgs a) {
 // all its loads of a round before its first store.  The host sends only
 // 8-byte aligned records whose size and offsets are multiples of 8, at most
 // 4 KB each.  The CTAs also copy the work-queue order from the pinned host
-// table, and the last CTA to finish publishes the id check's verdict.
+// table, and the last CTA to finish publishes the id check's outcome.
 constexpr int kGatherThreads = 256;
 constexpr int kIdBatch = 8;
 constexpr int kIdParts = 4;  // CTAs per walk for the id lists
@@ -336,7 +336,7 @@ __global__ __launch_bounds__(kGatherThreads) void gather_walks_kernel(HdWalkArgs
         }
         __syncthreads();
     }
-    // The verdict: the last CTA to finish sees every CTA's atomics.
+    // The outcome: the last CTA to finish sees every CTA's atomics.
     if (t == 0) {
         __threadfence();
         if (atomicAdd(a.err + 2, 1) == (int)gridDim.x - 1) {
@@ -407,7 +407,7 @@ cudaError_t launch_gather_j(const HdSendArgs& a, int num_sms, cudaStream_t s) {
 cudaError_t launch_gather_walks(const HdWalkArgs& a, int num_sms, cudaStream_t s) {
     const int64_t units = (int64_t)a.n_walk * kIdParts;
     int grid = units < num_sms * 8 ? (int)units : num_sms * 8;
-    if (grid < 1) grid = 1;  // the verdict is published even with no walk
+    if (grid < 1) grid = 1;  // the outcome is published even with no walk
     gather_walks_kernel<<<grid, kGatherThreads, 0, s>>>(a);
     return cudaGetLastError();
 }

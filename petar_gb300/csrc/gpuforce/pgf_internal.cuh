@@ -302,7 +302,7 @@ struct HdWalkArgs {
     int32_t* out_id_spj;
     WalkDesc* out_walks;
     // [0] set when an id is out of range, [1] the largest such caller walk
-    // index, [2] finished CTAs, [3] the verdict the force kernels read.  The
+    // index, [2] finished CTAs, [3] the outcome the force kernels read.  The
     // last CTA moves [0], [1] into err_host[0], [1] (pinned) and [3], and
     // clears [0..2] for the next dispatch.
     int32_t* err;
