@@ -821,13 +821,18 @@ void queue_order(const std::vector<std::pair<double, int>>& cq, int32_t* out) {
         std::memcpy(&bits, &c, sizeof(bits));
         return bits >> 49;  // exponent and 3 mantissa bits: monotonic in c > 0
     };
+    const size_t n = cq.size();
+    std::vector<int64_t> keys(n);
     int64_t kmax = 0;
-    for (const auto& e : cq) kmax = std::max(kmax, key(e.first));
+    for (size_t k = 0; k < n; ++k) {
+        keys[k] = key(cq[k].first);
+        kmax = std::max(kmax, keys[k]);
+    }
     int count[kBuckets + 1] = {};
-    auto bucket = [&](double c) { return (int)std::min<int64_t>(kBuckets - 1, kmax - key(c)); };
-    for (const auto& e : cq) ++count[bucket(e.first) + 1];
+    auto bucket = [&](size_t k) { return (int)std::min<int64_t>(kBuckets - 1, kmax - keys[k]); };
+    for (size_t k = 0; k < n; ++k) ++count[bucket(k) + 1];
     for (int b = 0; b < kBuckets; ++b) count[b + 1] += count[b];
-    for (const auto& e : cq) out[count[bucket(e.first)]++] = e.second;
+    for (size_t k = 0; k < n; ++k) out[count[bucket(k)]++] = cq[k].second;
 }
 
 // The walk phase of a single-launch index dispatch, host-direct: the host
@@ -965,10 +970,16 @@ int dispatch_walks(int tag, int n_walk, const void* const* epi, const int* n_epi
             (n_spj[w] > 0 && (!id_spj || !id_spj[w])))
             return fail(PGF_ERR_ARG, "NULL array for walk %d", w);
     }
-    std::vector<int32_t> ord(n_walk);
-    std::iota(ord.begin(), ord.end(), 0);
     auto cost = [&](int w) { return (double)n_epi[w] * ((double)n_epj[w] + 2.0 * (double)n_spj[w]); };
-    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return cost(a) > cost(b); });
+    // Descending cost, ties in walk order (the order a stable sort gives),
+    // with the costs computed once.
+    std::vector<std::pair<double, int32_t>> by_cost(n_walk);
+    for (int w = 0; w < n_walk; ++w) by_cost[w] = {cost(w), w};
+    std::sort(by_cost.begin(), by_cost.end(), [](const std::pair<double, int32_t>& a, const std::pair<double, int32_t>& b) {
+        return a.first > b.first || (a.first == b.first && a.second < b.second);
+    });
+    std::vector<int32_t> ord(n_walk);
+    for (int k = 0; k < n_walk; ++k) ord[k] = by_cost[k].second;
     std::vector<Slot3> off(n_walk + 1);
     off[0] = Slot3{0, 0, 0};
     t.epi_disp.assign(n_walk, 0);
