@@ -49,6 +49,20 @@ def test_status_codes_without_device_or_state():
     assert lib.pgf_recompute(0) == 4
 
 
+def test_setter_arguments_checked_without_device():
+    """The tuning and accuracy setters validate their arguments on the host."""
+    lib = gpuforce.load()
+    assert lib.pgf_set_walk_split_unit(0) == 1 and lib.pgf_set_walk_split_unit(257) == 1
+    assert lib.pgf_set_walk_split_unit(16) == 0
+    assert lib.pgf_set_gradient_accuracy(2) == 1 and lib.pgf_set_gradient_accuracy(-1) == 1
+    assert lib.pgf_set_gradient_accuracy(1) == 0
+    assert lib.pgf_set_dispatch_stages(9) == 1 and lib.pgf_set_dispatch_stages(0) == 0
+    with pytest.raises(gpuforce.GpuForceError):
+        gpuforce.set_gradient_accuracy(3)
+    with pytest.raises(gpuforce.GpuForceError):
+        gpuforce.set_walk_split_unit(1000)
+
+
 def test_bad_initialize_arguments():
     lib = gpuforce.load()
     assert lib.pgf_initialize(0, -1.0, 1e-4, 1.0) == 1
